@@ -1,0 +1,146 @@
+"""Python access to the oracle (TEST INFRASTRUCTURE ONLY).
+
+Two CPU implementations of the reference Tay path, with one calling convention:
+  port      oracle/_build/liboracle.so - the C restatement (tay_oracle.c), FP32 and FP64
+  reference oracle/_ref/libtayref.so   - the reference's own sources built by
+                                         oracle/ref/Makefile (only where the reference
+                                         source tree is available)
+
+Both take AoS agent records in id order and return them in id order.  The record
+layouts below mirror oracle/oracle_models.h (and, for the test model, the reference's
+test/agent.h:2-10).  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+leg use this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libtayref.so")
+
+MODEL_TEST, MODEL_BOIDS, MODEL_SPH = 0, 1, 2
+SPACE = {"simple": 1, "kd_tree": 2, "grid": 4, "z_grid": 5}
+PASS_SEE0, PASS_ACT0, PASS_SEE1, PASS_ACT1 = 1, 2, 4, 8
+
+
+def _rec(real):
+    f = "<f4" if real == np.float32 else "<f8"
+    test = np.dtype([("tag", "<u4", 2), ("p", f, 4), ("v", f, 4), ("b_buffer", f, 4), ("b_buffer_count", "<i4"),
+                     ("f_buffer", f, 4), ("id", "<i4")])
+    boid = np.dtype([("tag", "<u4", 2), ("p", f, 4), ("v", f, 4), ("coh", f, 4), ("ali", f, 4), ("sep", f, 4),
+                     ("count", "<i4"), ("id", "<i4")])
+    sph = np.dtype([("tag", "<u4", 2), ("p", f, 4), ("v", f, 4), ("a", f, 4), ("rho", f), ("P", f), ("id", "<i4"),
+                    ("pad", "<i4")])
+    return {MODEL_TEST: test, MODEL_BOIDS: boid, MODEL_SPH: sph}
+
+
+RECORDS = {np.float32: _rec(np.float32), np.float64: _rec(np.float64)}
+assert RECORDS[np.float32][MODEL_TEST].itemsize == 80
+assert RECORDS[np.float32][MODEL_BOIDS].itemsize == 96
+assert RECORDS[np.float32][MODEL_SPH].itemsize == 72
+
+
+def boids_context(real, r=10.0, w_sep=1.5, w_ali=1.0, w_coh=1.0, max_speed=2.0, dt=1.0):
+    r = real(r)
+    return np.array([r, r * r, w_sep, w_ali, w_coh, max_speed, dt, 0.0], dtype=real)
+
+
+def sph_context(real, h=0.02, dx=0.01, rho0=1000.0, c0=20.0, alpha=0.05, dt=1e-4, g=(0.0, 0.0, -9.81),
+                tank_min=(0.0, 0.0, 0.0), tank_max=(2.0, 1.5, 0.8)):
+    """Context values are computed in float64 and rounded once to `real`."""
+    m = rho0 * dx ** 3
+    vals = [h, 1.0 / h, (2.0 * h) ** 2, 1.0 / (np.pi * h ** 3), m, rho0, c0 * c0 * rho0 / 7.0, c0, alpha,
+            0.01 * h * h, dt, *g, *tank_min, *tank_max]
+    return np.array(vals, dtype=real)
+
+
+def test_act_context(real, lo=0.0, hi=1000.0):
+    return np.array([lo, lo, lo, 0.0, hi, hi, hi, 0.0], dtype=real)
+
+
+def make_records(model, p, v, real=np.float32):
+    """AoS records for positions/velocities ([N,4] arrays); ids 0..N-1, accumulators zero."""
+    n = p.shape[0]
+    rec = np.zeros(n, RECORDS[real][model])
+    rec["p"] = p
+    rec["v"] = v
+    rec["id"] = np.arange(n, dtype=np.int32)
+    return rec
+
+
+def build_port():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def build_reference(ref_root):
+    subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={ref_root}"], check=True)
+
+
+_ARGTYPES = None
+
+
+def _bind(lib, name, real_c):
+    fn = getattr(lib, name)
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                   real_c, real_c, ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.c_int,
+                   ctypes.POINTER(ctypes.c_double)]
+    return fn
+
+
+@dataclass
+class RunResult:
+    records: np.ndarray
+    ms_per_step: float
+
+
+class _Impl:
+    def __init__(self, so, names):
+        if not os.path.exists(so):
+            raise FileNotFoundError(so)
+        self.lib = ctypes.CDLL(so)
+        self.fns = {real: _bind(self.lib, nm, c) for real, (nm, c) in names.items()}
+
+    def run(self, model, space, records, see_ctx, act_ctx, radius, part_size, steps, pass_mask, threads=0, mb=250,
+            real=np.float32):
+        fn = self.fns[real]
+        rec = np.ascontiguousarray(records.copy())
+        see = np.ascontiguousarray(see_ctx) if see_ctx is not None else np.zeros(4, real)
+        act = np.ascontiguousarray(act_ctx) if act_ctx is not None else see
+        ms = ctypes.c_double()
+        sp = SPACE[space] if isinstance(space, str) else int(space)
+        ran = fn(model, sp, rec.shape[0], rec.ctypes.data, see.ctypes.data, act.ctypes.data, real(radius),
+                 real(part_size), mb, steps, pass_mask, threads, ctypes.byref(ms))
+        if ran != steps:
+            raise RuntimeError(f"oracle run failed ({ran} of {steps} steps)")
+        return RunResult(rec, ms.value)
+
+
+_port = None
+_ref = None
+
+
+def port():
+    global _port
+    if _port is None:
+        if not os.path.exists(PORT_SO):
+            build_port()
+        _port = _Impl(PORT_SO, {np.float32: ("oracle_run_f32", ctypes.c_float),
+                                np.float64: ("oracle_run_f64", ctypes.c_double)})
+    return _port
+
+
+def reference():
+    """The reference's own CPU path, or None when it was not built on this machine."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_SO):
+            return None
+        _ref = _Impl(REF_SO, {np.float32: ("ref_run", ctypes.c_float)})
+    return _ref

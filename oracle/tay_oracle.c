@@ -1,0 +1,598 @@
+/* ORACLE (test infrastructure, not the product).
+ *
+ * A plain-C restatement of the reference Tay CPU path for one group of point agents:
+ * the step loop (tay/state.c:194-323), the CpuSimple, CpuGrid and CpuZGrid structures
+ * (tay/cpu_simple.c, tay/cpu_grid.c, tay/cpu_z_grid.c), the point-point pairing kernels
+ * (tay/space.c:62-68, 106-148), the act pass (tay/space.c:250-263) and the static thread
+ * split (tay/thread.c:244-250), on a POSIX thread pool.
+ *
+ * It is compiled twice into oracle/_build/liboracle.so: REAL=float with
+ * -ffp-contract=off (the FP32 oracle, pinned against the reference itself and against
+ * the committed golden vectors) and REAL=double (the FP64 oracle that every FP32 float
+ * result is also compared with).  Only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline leg load it.
+ */
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#include <unistd.h>
+
+#ifndef REAL
+#define REAL float
+#endif
+#ifndef SUFFIX
+#define SUFFIX _f32
+#endif
+
+#include "oracle_models.h"
+
+#define O_CAT2(a, b) a##b
+#define O_CAT(a, b) O_CAT2(a, b)
+#define O_NAME(x) O_CAT(x, SUFFIX)
+
+#if defined(ORACLE_DOUBLE)
+#define O_FLOOR floor
+#define O_CEIL ceil
+#define O_POW pow
+#define O_BIG DBL_MAX
+#else
+#define O_FLOOR floorf
+#define O_CEIL ceilf
+#define O_POW powf
+#define O_BIG FLT_MAX
+#endif
+
+enum { O_SPACE_SIMPLE = 1, O_SPACE_GRID = 4, O_SPACE_Z_GRID = 5 };
+enum { O_MODEL_TEST = 0, O_MODEL_BOIDS = 1, O_MODEL_SPH = 2 };
+enum { O_PASS_SEE0 = 1, O_PASS_ACT0 = 2, O_PASS_SEE1 = 4, O_PASS_ACT1 = 8 };
+
+typedef void (*OSeeFn)(void *, void *, void *);
+typedef void (*OActFn)(void *, void *);
+
+/* ------------------------------------------------------------------ thread pool */
+
+typedef struct OTask OTask;
+typedef void (*OTaskFn)(OTask *task, int thread_i, int threads);
+struct OTask {
+    OTaskFn fn;
+    void *arg;
+};
+
+static struct {
+    int count;
+    pthread_t handles[64];
+    pthread_mutex_t lock;
+    pthread_cond_t go, done;
+    unsigned long long generation;
+    int remaining;
+    int stop;
+    OTask *task;
+} O_NAME(pool) = {0, {0}, PTHREAD_MUTEX_INITIALIZER, PTHREAD_COND_INITIALIZER, PTHREAD_COND_INITIALIZER, 0, 0, 0, 0};
+#define POOL O_NAME(pool)
+
+typedef struct {
+    int index;
+} OWorkerArg;
+static OWorkerArg O_NAME(worker_args)[64];
+
+static void *O_NAME(worker)(void *varg) {
+    int index = ((OWorkerArg *)varg)->index;
+    unsigned long long seen = 0;
+    for (;;) {
+        pthread_mutex_lock(&POOL.lock);
+        while (POOL.generation == seen)
+            pthread_cond_wait(&POOL.go, &POOL.lock);
+        seen = POOL.generation;
+        int stop = POOL.stop;
+        OTask *task = POOL.task;
+        pthread_mutex_unlock(&POOL.lock);
+        if (!stop)
+            task->fn(task, index, POOL.count);
+        pthread_mutex_lock(&POOL.lock);
+        if (--POOL.remaining == 0)
+            pthread_cond_signal(&POOL.done);
+        pthread_mutex_unlock(&POOL.lock);
+        if (stop)
+            return 0;
+    }
+}
+
+static void O_NAME(pool_run)(OTask *task) {
+    pthread_mutex_lock(&POOL.lock);
+    POOL.task = task;
+    POOL.remaining = POOL.count;
+    ++POOL.generation;
+    pthread_cond_broadcast(&POOL.go);
+    while (POOL.remaining > 0)
+        pthread_cond_wait(&POOL.done, &POOL.lock);
+    pthread_mutex_unlock(&POOL.lock);
+}
+
+static void O_NAME(pool_stop)(void) {
+    if (!POOL.count)
+        return;
+    POOL.stop = 1;
+    OTask none = {0, 0};
+    O_NAME(pool_run)(&none);
+    for (int i = 0; i < POOL.count; ++i)
+        pthread_join(POOL.handles[i], 0);
+    POOL.count = 0;
+    POOL.stop = 0;
+}
+
+static void O_NAME(pool_start)(int threads) {
+    if (threads <= 0) {
+        long online = sysconf(_SC_NPROCESSORS_ONLN);
+        threads = online > 0 ? (int)online : 1;
+    }
+    if (threads > 64)
+        threads = 64;
+    if (POOL.count == threads)
+        return;
+    O_NAME(pool_stop)();
+    POOL.count = threads;
+    for (int i = 0; i < threads; ++i) {
+        O_NAME(worker_args)[i].index = i;
+        pthread_create(&POOL.handles[i], 0, O_NAME(worker), &O_NAME(worker_args)[i]);
+    }
+}
+
+/* tay/thread.c:244-250: equal shares, the last thread takes the remainder */
+static inline void o_range(unsigned count, int thread_i, int threads, unsigned *beg, unsigned *end) {
+    unsigned share = count / (unsigned)threads;
+    *beg = share * (unsigned)thread_i;
+    *end = (thread_i + 1 < threads) ? *beg + share : count;
+}
+
+/* ------------------------------------------------------------------ group and space */
+
+typedef struct {
+    unsigned count;
+    unsigned first;
+} OZCell;
+
+typedef struct OGCell {
+    struct OGCell *next;
+    unsigned count;
+    unsigned first;
+    int idx[3];
+} OGCell;
+
+typedef struct {
+    char *storage;
+    char *sort_storage;
+    unsigned agent_size;
+    unsigned count;
+    int space;
+    REAL part[3];
+    REAL box_min[3], box_max[3];
+    /* grids */
+    REAL origin[3];
+    REAL cell_size[3];
+    int cell_counts[3];
+    unsigned cells_count;
+    unsigned max_cells;
+    OZCell *zcells;
+    OGCell *gcells;
+    OGCell *first_gcell;
+} OGroup;
+
+typedef struct {
+    int is_see;
+    OSeeFn see;
+    OActFn act;
+    REAL radii[3];
+    int self_see;
+    void *ctx;
+} OPass;
+
+static inline REAL *o_pos(const OGroup *g, unsigned i) {
+    return (REAL *)(g->storage + (size_t)g->agent_size * i + sizeof(OTag));
+}
+
+static inline OTag *o_tag(const OGroup *g, unsigned i) {
+    return (OTag *)(g->storage + (size_t)g->agent_size * i);
+}
+
+/* tay/space.c:9-48 */
+static void o_update_box(OGroup *g) {
+    for (int i = 0; i < 3; ++i) {
+        g->box_min[i] = O_BIG;
+        g->box_max[i] = -O_BIG;
+    }
+    for (unsigned a = 0; a < g->count; ++a) {
+        const REAL *p = o_pos(g, a);
+        for (int i = 0; i < 3; ++i) {
+            if (p[i] < g->box_min[i])
+                g->box_min[i] = p[i];
+            if (p[i] > g->box_max[i])
+                g->box_max[i] = p[i];
+        }
+    }
+}
+
+/* 10 bits per axis, x at bit 0 (tay/cpu_z_grid.c:57-77) */
+static inline unsigned o_spread10(unsigned v) {
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+static inline unsigned o_morton3(int x, int y, int z) {
+    return o_spread10((unsigned)x) | (o_spread10((unsigned)y) << 1) | (o_spread10((unsigned)z) << 2);
+}
+
+static inline unsigned o_compact10(unsigned v) {
+    v &= 0x09249249u;
+    v = (v | (v >> 2)) & 0x030c30c3u;
+    v = (v | (v >> 4)) & 0x0300f00fu;
+    v = (v | (v >> 8)) & 0xff0000ffu;
+    v = (v | (v >> 16)) & 0x000003ffu;
+    return v;
+}
+
+static inline void o_cell_indices(const REAL *p, const REAL *o, const REAL *s, int *idx) {
+    for (int i = 0; i < 3; ++i)
+        idx[i] = (int)O_FLOOR((p[i] - o[i]) / s[i]);
+}
+
+/* tay/cpu_z_grid.c:156-221 */
+static void o_z_grid_sort(OGroup *g) {
+    o_update_box(g);
+    unsigned n = 0;
+    for (int i = 0; i < 3; ++i) {
+        REAL cs = g->part[i];
+        REAL size = g->box_max[i] - g->box_min[i] + cs * (REAL)0.001;
+        unsigned cells = (unsigned)O_FLOOR(size / cs);
+        unsigned side_n = 0;
+        while ((1u << (side_n + 1u)) <= cells)
+            ++side_n;
+        if (side_n > n)
+            n = side_n;
+    }
+    for (;;) {
+        unsigned side = 1u << (n + 1u);
+        if (side * side * side <= g->max_cells)
+            break;
+        --n;
+    }
+    for (int i = 0; i < 3; ++i) {
+        REAL cs = g->part[i];
+        REAL size = g->box_max[i] - g->box_min[i] + cs * (REAL)0.001;
+        g->origin[i] = g->box_min[i];
+        g->cell_counts[i] = 1 << n;
+        g->cell_size[i] = size / (REAL)g->cell_counts[i];
+    }
+    g->cells_count = (1u << n) * (1u << n) * (1u << n);
+
+    for (unsigned a = 0; a < g->count; ++a) {
+        int idx[3];
+        o_cell_indices(o_pos(g, a), g->origin, g->cell_size, idx);
+        unsigned cell_i = o_morton3(idx[0], idx[1], idx[2]);
+        OTag *tag = o_tag(g, a);
+        tag->part_i = cell_i;
+        tag->cell_agent_i = g->zcells[cell_i].count++;
+    }
+    unsigned first = 0;
+    for (unsigned c = 0; c < g->cells_count; ++c) {
+        g->zcells[c].first = first;
+        first += g->zcells[c].count;
+    }
+    for (unsigned a = 0; a < g->count; ++a) {
+        OTag *tag = o_tag(g, a);
+        unsigned dst = g->zcells[tag->part_i].first + tag->cell_agent_i;
+        memcpy(g->sort_storage + (size_t)g->agent_size * dst, tag, g->agent_size);
+    }
+    char *t = g->storage;
+    g->storage = g->sort_storage;
+    g->sort_storage = t;
+}
+
+/* tay/cpu_grid.c:74-156 */
+static void o_grid_sort(OGroup *g) {
+    o_update_box(g);
+    g->first_gcell = 0;
+    unsigned long long cells_count = 1;
+    for (int i = 0; i < 3; ++i) {
+        g->origin[i] = g->box_min[i];
+        REAL cs = g->part[i];
+        REAL size = g->box_max[i] - g->box_min[i] + cs * (REAL)0.001;
+        g->cell_counts[i] = (int)O_CEIL(size / cs);
+        g->cell_size[i] = size / (REAL)g->cell_counts[i];
+        cells_count *= (unsigned long long)g->cell_counts[i];
+    }
+    if (cells_count > g->max_cells) {
+        REAL volume_ratio = (REAL)cells_count / (REAL)g->max_cells;
+        REAL ratio = O_POW(volume_ratio, (REAL)1 / (REAL)3);
+        for (int i = 0; i < 3; ++i) {
+            REAL cs = g->part[i];
+            REAL size = g->box_max[i] - g->box_min[i] + cs * (REAL)0.001;
+            g->cell_counts[i] = (int)O_CEIL(g->cell_counts[i] / ratio);
+            g->cell_size[i] = size / (REAL)g->cell_counts[i];
+        }
+    }
+    for (unsigned a = 0; a < g->count; ++a) {
+        int idx[3];
+        o_cell_indices(o_pos(g, a), g->origin, g->cell_size, idx);
+        unsigned cell_i = (unsigned)(idx[2] * g->cell_counts[0] * g->cell_counts[1] + idx[1] * g->cell_counts[0] + idx[0]);
+        OGCell *cell = g->gcells + cell_i;
+        if (cell->count == 0) {
+            cell->next = g->first_gcell;
+            g->first_gcell = cell;
+            cell->idx[0] = idx[0];
+            cell->idx[1] = idx[1];
+            cell->idx[2] = idx[2];
+        }
+        OTag *tag = o_tag(g, a);
+        tag->part_i = cell_i;
+        tag->cell_agent_i = cell->count++;
+    }
+    unsigned first = 0;
+    for (OGCell *c = g->first_gcell; c; c = c->next) {
+        c->first = first;
+        first += c->count;
+    }
+    for (unsigned a = 0; a < g->count; ++a) {
+        OTag *tag = o_tag(g, a);
+        unsigned dst = g->gcells[tag->part_i].first + tag->cell_agent_i;
+        memcpy(g->sort_storage + (size_t)g->agent_size * dst, tag, g->agent_size);
+    }
+    char *t = g->storage;
+    g->storage = g->sort_storage;
+    g->sort_storage = t;
+}
+
+static void o_unsort(OGroup *g) {
+    if (g->space == O_SPACE_Z_GRID)
+        memset(g->zcells, 0, sizeof(OZCell) * g->cells_count); /* tay/cpu_z_grid.c:223-225 */
+    else if (g->space == O_SPACE_GRID)
+        for (OGCell *c = g->first_gcell; c; c = c->next) /* tay/cpu_grid.c:153-156 */
+            c->count = 0;
+}
+
+/* ------------------------------------------------------------------ pairing */
+
+/* tay/space.c:106-148; `skip_self` selects space_see_point_point (same group, no
+ * self-see) over space_see_point_point_self_see */
+static void o_pair(const OGroup *g, const OPass *pass, unsigned seer_beg, unsigned seer_end, unsigned seen_beg,
+                   unsigned seen_end, int skip_self) {
+    for (unsigned s = seer_beg; s < seer_end; ++s) {
+        char *seer = g->storage + (size_t)g->agent_size * s;
+        const REAL *sp = o_pos(g, s);
+        for (unsigned b = seen_beg; b < seen_end; ++b) {
+            if (skip_self && s == b)
+                continue;
+            const REAL *bp = o_pos(g, b);
+            int skip = 0;
+            for (int i = 0; i < 3; ++i) {
+                REAL d = sp[i] - bp[i];
+                if (d < -pass->radii[i] || d > pass->radii[i]) {
+                    skip = 1;
+                    break;
+                }
+            }
+            if (skip)
+                continue;
+            pass->see(seer, g->storage + (size_t)g->agent_size * b, pass->ctx);
+        }
+    }
+}
+
+/* neighbour cell index box for a seer box (tay/cpu_z_grid.c:232-247, tay/cpu_grid.c:158-174) */
+static void o_index_box(const OGroup *g, const REAL *bmin, const REAL *bmax, int *lo, int *hi) {
+    o_cell_indices(bmin, g->origin, g->cell_size, lo);
+    o_cell_indices(bmax, g->origin, g->cell_size, hi);
+    for (int i = 0; i < 3; ++i) {
+        if (lo[i] < 0) lo[i] = 0;
+        if (hi[i] < 0) hi[i] = 0;
+        if (lo[i] >= g->cell_counts[i]) lo[i] = g->cell_counts[i] - 1;
+        if (hi[i] >= g->cell_counts[i]) hi[i] = g->cell_counts[i] - 1;
+    }
+}
+
+typedef struct {
+    OGroup *g;
+    OPass *pass;
+} OPassArg;
+
+static void o_see_task(OTask *task, int thread_i, int threads) {
+    OPassArg *arg = (OPassArg *)task->arg;
+    OGroup *g = arg->g;
+    OPass *pass = arg->pass;
+    int skip_self = !pass->self_see;
+    unsigned beg, end;
+    o_range(g->count, thread_i, threads, &beg, &end);
+
+    if (g->space == O_SPACE_SIMPLE) { /* tay/cpu_simple.c:6-38 */
+        o_pair(g, pass, beg, end, 0, g->count, skip_self);
+        return;
+    }
+
+    /* tay/cpu_z_grid.c:283-321 and tay/cpu_grid.c:244-281: seers walked cell run by cell run */
+    unsigned s = beg;
+    while (s < end) {
+        const OTag *tag = o_tag(g, s);
+        int idx[3];
+        unsigned run_end;
+        if (g->space == O_SPACE_Z_GRID) {
+            idx[0] = (int)o_compact10(tag->part_i);
+            idx[1] = (int)o_compact10(tag->part_i >> 1);
+            idx[2] = (int)o_compact10(tag->part_i >> 2);
+            const OZCell *cell = g->zcells + tag->part_i;
+            run_end = cell->first + cell->count;
+        }
+        else {
+            const OGCell *cell = g->gcells + tag->part_i;
+            idx[0] = cell->idx[0];
+            idx[1] = cell->idx[1];
+            idx[2] = cell->idx[2];
+            run_end = cell->first + cell->count;
+        }
+        if (run_end > end)
+            run_end = end;
+        REAL bmin[3], bmax[3];
+        for (int i = 0; i < 3; ++i) {
+            REAL m = g->origin[i] + idx[i] * g->cell_size[i];
+            bmin[i] = m - pass->radii[i];
+            bmax[i] = m + g->cell_size[i] + pass->radii[i];
+        }
+        int lo[3], hi[3];
+        o_index_box(g, bmin, bmax, lo, hi);
+        for (int x = lo[0]; x <= hi[0]; ++x)
+            for (int y = lo[1]; y <= hi[1]; ++y)
+                for (int z = lo[2]; z <= hi[2]; ++z) {
+                    unsigned first, count;
+                    if (g->space == O_SPACE_Z_GRID) {
+                        const OZCell *c = g->zcells + o_morton3(x, y, z);
+                        first = c->first;
+                        count = c->count;
+                    }
+                    else {
+                        const OGCell *c = g->gcells + (z * g->cell_counts[0] * g->cell_counts[1] + y * g->cell_counts[0] + x);
+                        first = c->first;
+                        count = c->count;
+                    }
+                    o_pair(g, pass, s, run_end, first, first + count, skip_self);
+                }
+        s = run_end;
+    }
+}
+
+static void o_act_task(OTask *task, int thread_i, int threads) {
+    OPassArg *arg = (OPassArg *)task->arg;
+    unsigned beg, end;
+    o_range(arg->g->count, thread_i, threads, &beg, &end);
+    for (unsigned a = beg; a < end; ++a)
+        arg->pass->act(arg->g->storage + (size_t)arg->g->agent_size * a, arg->pass->ctx);
+}
+
+/* ------------------------------------------------------------------ entry point */
+
+static unsigned o_agent_size(int model) {
+    switch (model) {
+        case O_MODEL_TEST: return (unsigned)sizeof(OTestAgent);
+        case O_MODEL_BOIDS: return (unsigned)sizeof(OBoid);
+        case O_MODEL_SPH: return (unsigned)sizeof(OSphParticle);
+        default: return 0;
+    }
+}
+
+static int o_agent_id(int model, const char *a) {
+    switch (model) {
+        case O_MODEL_TEST: return ((const OTestAgent *)a)->result_index;
+        case O_MODEL_BOIDS: return ((const OBoid *)a)->id;
+        default: return ((const OSphParticle *)a)->id;
+    }
+}
+
+unsigned O_NAME(oracle_agent_size)(int model) {
+    return o_agent_size(model);
+}
+
+/* Runs `steps` steps of one model on one group.  Same contract as the reference driver:
+ * `agents` holds n AoS records in id order on entry and on return; the pass mask selects
+ * which of the model's passes are registered, in the model's order; returns the number
+ * of steps run (0 on error) and the wall-clock ms per step (tay/state.c:204-206,317-320). */
+int O_NAME(oracle_run)(int model, int space, int n, void *agents, const void *see_ctx, const void *act_ctx,
+                       REAL radius, REAL part_size, int mb, int steps, unsigned pass_mask, int threads,
+                       double *ms_per_step) {
+    unsigned agent_size = o_agent_size(model);
+    if (!agent_size || n <= 0 || steps < 0)
+        return 0;
+    if (space != O_SPACE_SIMPLE && space != O_SPACE_GRID && space != O_SPACE_Z_GRID)
+        return 0;
+    O_NAME(pool_start)(threads);
+
+    OGroup g;
+    memset(&g, 0, sizeof(g));
+    g.agent_size = agent_size;
+    g.count = (unsigned)n;
+    g.space = space;
+    g.part[0] = g.part[1] = g.part[2] = part_size;
+    g.storage = (char *)malloc((size_t)agent_size * n);
+    g.sort_storage = (char *)malloc((size_t)agent_size * n);
+    memcpy(g.storage, agents, (size_t)agent_size * n);
+    size_t shared = (size_t)mb << 20;
+    if (space == O_SPACE_Z_GRID) {
+        g.max_cells = (unsigned)(shared / 8u); /* sizeof(ZGridCell), tay/cpu_z_grid.c:7-10,152 */
+        g.zcells = (OZCell *)calloc(g.max_cells, sizeof(OZCell));
+    }
+    else if (space == O_SPACE_GRID) {
+        g.max_cells = (unsigned)(shared / 32u); /* sizeof(GridCell) on LP64, tay/cpu_grid.c:6-11,62 */
+        g.gcells = (OGCell *)calloc(g.max_cells, sizeof(OGCell));
+    }
+
+    /* contexts are copied, as the OpenCL path copies them per run (tay/ocl.c:252-259) */
+    OTestActContext test_act;
+    OBoidsContext boids;
+    OSphContext sph;
+    OPass passes[4];
+    int passes_count = 0;
+    REAL radii[3] = {radius, radius, radius};
+    if (model == O_MODEL_TEST) {
+        memcpy(&test_act, act_ctx, sizeof(test_act));
+        if (pass_mask & O_PASS_SEE0)
+            passes[passes_count++] = (OPass){1, o_test_see, 0, {radii[0], radii[1], radii[2]}, 0, 0};
+        if (pass_mask & O_PASS_ACT0)
+            passes[passes_count++] = (OPass){0, 0, o_test_act, {0, 0, 0}, 0, &test_act};
+    }
+    else if (model == O_MODEL_BOIDS) {
+        memcpy(&boids, see_ctx, sizeof(boids));
+        if (pass_mask & O_PASS_SEE0)
+            passes[passes_count++] = (OPass){1, o_boids_see, 0, {radii[0], radii[1], radii[2]}, 0, &boids};
+        if (pass_mask & O_PASS_ACT0)
+            passes[passes_count++] = (OPass){0, 0, o_boids_act, {0, 0, 0}, 0, &boids};
+    }
+    else {
+        memcpy(&sph, see_ctx, sizeof(sph));
+        if (pass_mask & O_PASS_SEE0)
+            passes[passes_count++] = (OPass){1, o_sph_density, 0, {radii[0], radii[1], radii[2]}, 1, &sph};
+        if (pass_mask & O_PASS_ACT0)
+            passes[passes_count++] = (OPass){0, 0, o_sph_pressure, {0, 0, 0}, 0, &sph};
+        if (pass_mask & O_PASS_SEE1)
+            passes[passes_count++] = (OPass){1, o_sph_force, 0, {radii[0], radii[1], radii[2]}, 0, &sph};
+        if (pass_mask & O_PASS_ACT1)
+            passes[passes_count++] = (OPass){0, 0, o_sph_integrate, {0, 0, 0}, 0, &sph};
+    }
+
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    for (int step = 0; step < steps; ++step) {
+        if (space == O_SPACE_Z_GRID)
+            o_z_grid_sort(&g);
+        else if (space == O_SPACE_GRID)
+            o_grid_sort(&g);
+        for (int p = 0; p < passes_count; ++p) {
+            OPassArg arg = {&g, passes + p};
+            OTask task = {passes[p].is_see ? o_see_task : o_act_task, &arg};
+            O_NAME(pool_run)(&task);
+        }
+        o_unsort(&g);
+    }
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    if (ms_per_step) {
+        double t = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+        *ms_per_step = steps ? t / steps * 1000.0 : 0.0;
+    }
+
+    int ok = steps;
+    for (unsigned a = 0; a < g.count; ++a) {
+        const char *rec = g.storage + (size_t)agent_size * a;
+        int id = o_agent_id(model, rec);
+        if (id < 0 || id >= n) {
+            ok = 0;
+            break;
+        }
+        memcpy((char *)agents + (size_t)agent_size * id, rec, agent_size);
+    }
+    free(g.storage);
+    free(g.sort_storage);
+    free(g.zcells);
+    free(g.gcells);
+    return ok;
+}
