@@ -1,0 +1,112 @@
+/* C ABI of the GB300 Z-grid engine (libtay_gb300.so).
+ *
+ * This is the layer that replaces the reference's OpenCL device layer for Z-grid
+ * groups: program text generation and compilation (tay/ocl.c:100-177), buffer creation,
+ * push and fetch (tay/ocl.c:59-98, 238-272), the grid sort launcher
+ * (tay/ocl_grid.c:241-374) and the per-pass see/act launches (tay/ocl.c:208-236), plus
+ * the CPU thread pool those passes ran on for CPU structures (tay/thread.c).  The
+ * reference-compatible API in tay.h is implemented on top of it; hosts may also call it
+ * directly (plain pointers and sizes, no C++ or torch types).
+ *
+ * A "batch" holds one or more groups that share a model and a pass sequence.  Each
+ * group becomes one segment of concatenated device buffers; tgpu_batch_run advances all
+ * of them with one launch per kernel per step.  Every function returns TGPU_OK or an
+ * error code; tgpu_last_error() describes the last failure of the calling thread.
+ */
+#ifndef TAY_GPU_H
+#define TAY_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct TgpuBatch TgpuBatch;
+
+enum {
+    TGPU_OK = 0,
+    TGPU_ERR_ARG = 1,          /* bad argument, or groups that cannot share a batch */
+    TGPU_ERR_UNKNOWN_FUNC = 2, /* a func_name no registered device model provides */
+    TGPU_ERR_PROGRAM = 3,      /* pass sequence the model does not support */
+    TGPU_ERR_CUDA = 4,         /* a CUDA call failed (message has the CUDA error) */
+    TGPU_ERR_DEVICE = 5        /* a kernel reported an error through the device error word */
+};
+
+/* One registered pass, as stored by tay_add_see / tay_add_act
+ * (tay/state.c:135-158): func_name selects the device function. */
+typedef struct TgpuPass {
+    const char *func_name;
+    int is_see;
+    float radii[4];
+    int self_see;
+    const void *context;      /* borrowed; copied at create and by tgpu_batch_set_contexts */
+    unsigned context_size;
+} TgpuPass;
+
+/* One group (tay_add_group + tay_configure_space + tay_fix_space_box,
+ * tay/state.c:73-125). */
+typedef struct TgpuGroup {
+    unsigned agent_size;      /* bytes per AoS record */
+    unsigned count;           /* agents */
+    float min_part_sizes[4];  /* minimum cell edge per axis */
+    int shared_megabytes;     /* memory for the structure (bounds the dense cell table) */
+    int box_fixed;
+    float box_min[4];
+    float box_max[4];
+    int pass_count;
+    const TgpuPass *passes;
+} TgpuGroup;
+
+/* Creates a batch of `group_count` groups; all must resolve to the same model and the
+ * same pass sequence. */
+int tgpu_batch_create(const TgpuGroup *groups, int group_count, TgpuBatch **out);
+void tgpu_batch_destroy(TgpuBatch *batch);
+
+/* Copies the pass contexts of group `group` again (contexts are borrowed by the host
+ * API and re-read at every tay_run, as tay/ocl.c:252-259 does). */
+int tgpu_batch_set_contexts(TgpuBatch *batch, int group, const TgpuGroup *desc);
+
+/* Uploads `count` AoS records (as given at create) of group `group`. */
+int tgpu_batch_push(TgpuBatch *batch, int group, const void *host_records);
+
+/* Runs `steps` steps (sort, passes, table clear) and waits for them. */
+int tgpu_batch_run(TgpuBatch *batch, int steps);
+
+/* Same as tgpu_batch_run but only enqueues; tgpu_batch_sync waits. */
+int tgpu_batch_enqueue(TgpuBatch *batch, int steps);
+int tgpu_batch_sync(TgpuBatch *batch);
+
+/* Downloads the records of group `group` in the current (cell) order, as
+ * tay_get_agent exposes them (tay/state.c:178-181). */
+int tgpu_batch_fetch(TgpuBatch *batch, int group, void *host_records);
+
+/* Device time in ms of the last tgpu_batch_run / enqueue+sync, from CUDA events on the
+ * batch's stream, and the number of pairs that passed the box test in it. */
+double tgpu_batch_last_device_ms(const TgpuBatch *batch);
+unsigned long long tgpu_batch_last_pairs(const TgpuBatch *batch);
+
+/* Number of kernel launches one step enqueues. */
+int tgpu_batch_launches_per_step(const TgpuBatch *batch);
+
+/* Name of the model the batch runs ("test_basic", "boids", "sph"), and the index of the
+ * pass sequence within the model. */
+const char *tgpu_batch_model(const TgpuBatch *batch);
+int tgpu_batch_program(const TgpuBatch *batch);
+
+/* Tuning knobs (0 = default): agents staged per see CTA, halo cells per see CTA,
+ * cell-size multiple applied to min_part_sizes, and CUDA-graph use. Apply to batches
+ * created afterwards. */
+void tgpu_set_tuning(unsigned stage_cap, unsigned stage_cells, float cell_multiple, int use_graphs);
+
+/* Resolves a func_name to its model; returns the model name or NULL. */
+const char *tgpu_model_of(const char *func_name);
+
+/* Number of CUDA devices visible to the process (0 when none or no driver). */
+int tgpu_device_count(void);
+
+const char *tgpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

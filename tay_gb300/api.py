@@ -1,0 +1,221 @@
+"""ctypes mirror of the Tay C API (include/tay.h) and of the engine ABI (include/tay_gpu.h).
+
+The shared library tay_gb300/libtay_gb300.so is built in-tree by tay_gb300._build.
+Loading it is mandatory: there is no fallback implementation, and every entry point
+raises when the library is missing or a call fails.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libtay_gb300.so")
+
+TAY_FALSE, TAY_TRUE = 0, 1
+(TAY_SPACE_NONE, TAY_CPU_SIMPLE, TAY_CPU_KD_TREE, TAY_CPU_AABB_TREE, TAY_CPU_GRID, TAY_CPU_Z_GRID,
+ TAY_GPU_Z_GRID) = range(7)
+ERRORS = ["TAY_ERROR_NONE", "TAY_ERROR_POINT_NONPOINT_MISMATCH", "TAY_ERROR_SPACE_INDEX_OUT_OF_RANGE",
+          "TAY_ERROR_GROUP_INDEX_OUT_OF_RANGE", "TAY_ERROR_STATE_STATUS", "TAY_ERROR_NOT_IMPLEMENTED",
+          "TAY_ERROR_OCL", "TAY_ERROR_CUDA", "TAY_ERROR_DEVICE_MODEL", "TAY_ERROR_BATCH"]
+
+
+class Float4(ctypes.Structure):
+    _pack_ = 1
+    _fields_ = [("x", ctypes.c_float), ("y", ctypes.c_float), ("z", ctypes.c_float), ("w", ctypes.c_float)]
+
+
+def f4(x, y=None, z=None, w=0.0) -> Float4:
+    if y is None:
+        y = z = x
+    return Float4(float(x), float(y), float(z), float(w))
+
+
+class TayError(RuntimeError):
+    pass
+
+
+_VP = ctypes.c_void_p
+# (name, restype, argtypes) of every exported symbol declared in include/tay.h and include/tay_gpu.h
+TAY_SYMBOLS = [
+    ("tay_create_state", _VP, []),
+    ("tay_destroy_state", None, [_VP]),
+    ("tay_switch_to_ocl", ctypes.c_int, [_VP]),
+    ("tay_switch_to_host", ctypes.c_int, [_VP]),
+    ("tay_get_error", ctypes.c_int, [_VP]),
+    ("tay_add_group", _VP, [_VP, ctypes.c_uint, ctypes.c_uint, ctypes.c_int]),
+    ("tay_configure_space", None, [_VP, _VP, ctypes.c_int, ctypes.c_int, Float4, ctypes.c_int]),
+    ("tay_fix_space_box", None, [_VP, _VP, Float4, Float4]),
+    ("tay_add_see", None, [_VP, _VP, _VP, _VP, ctypes.c_char_p, Float4, ctypes.c_int, _VP, ctypes.c_uint]),
+    ("tay_add_act", None, [_VP, _VP, _VP, ctypes.c_char_p, _VP, ctypes.c_uint]),
+    ("tay_clear_all_agents", None, [_VP, _VP]),
+    ("tay_get_available_agent", _VP, [_VP, _VP]),
+    ("tay_commit_available_agent", None, [_VP, _VP]),
+    ("tay_get_agent", _VP, [_VP, _VP, ctypes.c_int]),
+    ("tay_simulation_start", None, [_VP]),
+    ("tay_run", ctypes.c_int, [_VP, ctypes.c_int]),
+    ("tay_simulation_end", None, [_VP]),
+    ("tay_get_ms_per_step_for_last_run", ctypes.c_double, [_VP]),
+    ("tay_log", None, [_VP, ctypes.c_char_p]),
+    ("ocl_add_source", None, [_VP, ctypes.c_char_p]),
+    ("tay_threads_start", None, [ctypes.c_uint, ctypes.c_uint]),
+    ("tay_threads_stop", None, []),
+    ("tay_get_number_of_threads", ctypes.c_uint, []),
+    ("tay_run_batch", ctypes.c_int, [ctypes.POINTER(_VP), ctypes.c_int, ctypes.c_int]),
+    ("tay_get_pairs_for_last_run", ctypes.c_ulonglong, [_VP]),
+    ("tay_get_device_ms_for_last_run", ctypes.c_double, [_VP]),
+    ("tay_commit_agents", ctypes.c_uint, [_VP, _VP, _VP, ctypes.c_uint]),
+    ("tay_get_agent_count", ctypes.c_uint, [_VP, _VP]),
+    ("tay_get_error_message", ctypes.c_char_p, [_VP]),
+]
+TGPU_SYMBOLS = [
+    ("tgpu_batch_create", ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(_VP)]),
+    ("tgpu_batch_destroy", None, [_VP]),
+    ("tgpu_batch_set_contexts", ctypes.c_int, [_VP, ctypes.c_int, _VP]),
+    ("tgpu_batch_push", ctypes.c_int, [_VP, ctypes.c_int, _VP]),
+    ("tgpu_batch_run", ctypes.c_int, [_VP, ctypes.c_int]),
+    ("tgpu_batch_enqueue", ctypes.c_int, [_VP, ctypes.c_int]),
+    ("tgpu_batch_sync", ctypes.c_int, [_VP]),
+    ("tgpu_batch_fetch", ctypes.c_int, [_VP, ctypes.c_int, _VP]),
+    ("tgpu_batch_last_device_ms", ctypes.c_double, [_VP]),
+    ("tgpu_batch_last_pairs", ctypes.c_ulonglong, [_VP]),
+    ("tgpu_batch_launches_per_step", ctypes.c_int, [_VP]),
+    ("tgpu_batch_model", ctypes.c_char_p, [_VP]),
+    ("tgpu_batch_program", ctypes.c_int, [_VP]),
+    ("tgpu_set_tuning", None, [ctypes.c_uint, ctypes.c_uint, ctypes.c_float, ctypes.c_int]),
+    ("tgpu_model_of", ctypes.c_char_p, [ctypes.c_char_p]),
+    ("tgpu_device_count", ctypes.c_int, []),
+    ("tgpu_last_error", ctypes.c_char_p, []),
+]
+
+_lib = None
+
+
+def lib():
+    """Loads libtay_gb300.so (raises when it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python -m tay_gb300._build`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, res, args in TAY_SYMBOLS + TGPU_SYMBOLS:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+class State:
+    """One TayState with the reference's call sequence (test/test_basic.c:92-165)."""
+
+    def __init__(self):
+        self.L = lib()
+        self.ptr = self.L.tay_create_state()
+        if not self.ptr:
+            raise TayError("tay_create_state failed")
+        self._keep = []  # contexts are borrowed by the C side: keep them alive
+
+    def close(self):
+        if self.ptr:
+            self.L.tay_destroy_state(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def error(self):
+        return self.L.tay_get_error(self.ptr)
+
+    def message(self):
+        m = self.L.tay_get_error_message(self.ptr)
+        return m.decode() if m else ""
+
+    def check(self, what):
+        e = self.error()
+        if e:
+            raise TayError(f"{what}: {ERRORS[e] if e < len(ERRORS) else e}: {self.message()}")
+
+    def add_group(self, agent_size, capacity, is_point=True):
+        g = self.L.tay_add_group(self.ptr, agent_size, capacity, 1 if is_point else 0)
+        if not g:
+            self.check("tay_add_group")
+        return g
+
+    def configure_space(self, group, space_type, dims, part, mb):
+        self.L.tay_configure_space(self.ptr, group, space_type, dims, part if isinstance(part, Float4) else f4(part),
+                                   int(mb))
+
+    def fix_space_box(self, group, lo, hi):
+        self.L.tay_fix_space_box(self.ptr, group, lo, hi)
+
+    def add_see(self, seer, seen, func_name, radii, self_see, ctx):
+        buf = None if ctx is None else np.ascontiguousarray(ctx)
+        self._keep.append(buf)
+        self.L.tay_add_see(self.ptr, seer, seen, None, func_name.encode(),
+                           radii if isinstance(radii, Float4) else f4(radii), 1 if self_see else 0,
+                           None if buf is None else buf.ctypes.data, 0 if buf is None else buf.nbytes)
+
+    def add_act(self, group, func_name, ctx):
+        buf = None if ctx is None else np.ascontiguousarray(ctx)
+        self._keep.append(buf)
+        self.L.tay_add_act(self.ptr, group, None, func_name.encode(), None if buf is None else buf.ctypes.data,
+                           0 if buf is None else buf.nbytes)
+
+    def commit(self, group, records: np.ndarray):
+        rec = np.ascontiguousarray(records)
+        n = self.L.tay_commit_agents(self.ptr, group, rec.ctypes.data, rec.shape[0])
+        if n != rec.shape[0]:
+            self.check("tay_commit_agents")
+        return n
+
+    def agents(self, group, dtype) -> np.ndarray:
+        """Copy of the group's committed agents, in storage (cell) order."""
+        n = self.L.tay_get_agent_count(self.ptr, group)
+        if n == 0:
+            return np.zeros(0, dtype)
+        p = self.L.tay_get_agent(self.ptr, group, 0)
+        raw = ctypes.string_at(p, n * dtype.itemsize)
+        return np.frombuffer(raw, dtype=dtype).copy()
+
+    def start(self):
+        self.L.tay_simulation_start(self.ptr)
+        self.check("tay_simulation_start")
+
+    def run(self, steps):
+        r = self.L.tay_run(self.ptr, steps)
+        if r != steps:
+            self.check("tay_run")
+            raise TayError(f"tay_run ran {r} of {steps} steps")
+        return r
+
+    def end(self):
+        self.L.tay_simulation_end(self.ptr)
+
+    def ms_per_step(self):
+        return self.L.tay_get_ms_per_step_for_last_run(self.ptr)
+
+    def device_ms(self):
+        return self.L.tay_get_device_ms_for_last_run(self.ptr)
+
+    def pairs(self):
+        return self.L.tay_get_pairs_for_last_run(self.ptr)
+
+
+def run_batch(states, steps):
+    L = lib()
+    arr = (ctypes.c_void_p * len(states))(*[s.ptr for s in states])
+    r = L.tay_run_batch(arr, len(states), steps)
+    if r != steps:
+        states[0].check("tay_run_batch")
+        raise TayError("tay_run_batch failed")
+    return r
+
+
+def set_tuning(stage_cap=0, stage_cells=0, cell_multiple=1.0, use_graphs=True):
+    lib().tgpu_set_tuning(stage_cap, stage_cells, cell_multiple, 1 if use_graphs else 0)

@@ -1,0 +1,97 @@
+// Device model registry: the GB300 counterpart of the reference's "func_name + model
+// source pasted into an OpenCL program" mechanism (tay/ocl.c:100-177, 274-291).
+//
+// A model is a set of __device__ see/act functions compiled into the library.  It is
+// found by the func_name strings the host passes to tay_add_see / tay_add_act, exactly
+// the names the reference's OpenCL path keys its generated kernels on
+// (tay/ocl.c:284-291).  For every pass sequence the model supports, it provides kernels
+// in which an act pass that directly follows a see pass of the same group is fused into
+// the see kernel's epilogue.
+#pragma once
+
+#include "see.cuh"
+
+namespace tgpu {
+
+enum StreamRole : uint8_t {
+    kState = 0,  // persistent, reordered by every sort
+    kStep = 1,   // valid within one step only, written before it is read
+};
+
+// One kernel of a model's step program: a see pass (optionally with the following act
+// fused in) or a standalone act pass.
+struct KernelDesc {
+    const char *see;                   // see func name, or nullptr for an act-only kernel
+    const char *act;                   // act func name (fused when see != nullptr), or nullptr
+    uint32_t writes_f4;                // float4 streams the kernel writes
+    uint32_t writes_u32;               // u32 streams the kernel writes
+    uint32_t seen_f4;                  // float4 streams read from other agents (staged)
+    int staged_f4;                     // number of staged float4 streams per agent
+    // launch with the descriptor filled by the runtime
+    void (*launch_see)(const SeeLaunch &L, size_t smem, cudaStream_t st);
+    void (*launch_act)(const ActLaunch &L, cudaStream_t st);
+    cudaError_t (*prepare)(size_t smem);  // raises the kernel's dynamic shared memory limit
+};
+
+// A supported pass sequence: the func names in registration order, and the kernels
+// that run it.
+struct ProgramDesc {
+    int passes;
+    const char *names[4];
+    int kernels;
+    int kernel_index[4];  // into ModelDesc::kernels
+};
+
+struct ModelDesc {
+    const char *name;
+    uint32_t agent_bytes;
+    int nf4, nu32;
+    uint8_t role_f4[kMaxF4];
+    uint8_t role_u32[kMaxU32];
+    uint32_t see_ctx_bytes;   // bytes of the device see context (host context is copied in)
+    uint32_t act_ctx_bytes;
+    const KernelDesc *kernels;
+    int nkernels;
+    const ProgramDesc *programs;
+    int nprograms;
+    void (*pack)(const uint32_t *aos, uint32_t n, const PassIO &io, cudaStream_t st);
+    void (*unpack)(uint32_t *aos, uint32_t n, const PassIO &io, uint32_t program, cudaStream_t st);
+};
+
+const ModelDesc *model_test_basic();
+const ModelDesc *model_boids();
+const ModelDesc *model_sph();
+
+// helpers used by the model translation units
+template <class P>
+void launch_see_t(const SeeLaunch &L, size_t smem, cudaStream_t st) {
+    if (L.ctas) see_kernel<P><<<L.ctas, kSeeThreads, smem, st>>>(L);
+}
+template <class A>
+void launch_act_t(const ActLaunch &L, cudaStream_t st) {
+    if (L.tiles) act_kernel<A><<<L.tiles, kSortThreads, 0, st>>>(L);
+}
+template <class P>
+cudaError_t prepare_see_t(size_t smem) {
+    return cudaFuncSetAttribute(see_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+template <class M>
+void pack_t(const uint32_t *aos, uint32_t n, const PassIO &io, cudaStream_t st) {
+    if (n) pack_kernel<M><<<(n + 255) / 256, 256, 0, st>>>(aos, n, io);
+}
+template <class M>
+void unpack_t(uint32_t *aos, uint32_t n, const PassIO &io, uint32_t program, cudaStream_t st) {
+    if (n) unpack_kernel<M><<<(n + 255) / 256, 256, 0, st>>>(aos, n, io, program);
+}
+
+TGPU_D float4 ld_words4(const uint32_t *w) {
+    return make_float4(__uint_as_float(w[0]), __uint_as_float(w[1]), __uint_as_float(w[2]), __uint_as_float(w[3]));
+}
+TGPU_D void st_words4(uint32_t *w, const float4 &v) {
+    w[0] = __float_as_uint(v.x);
+    w[1] = __float_as_uint(v.y);
+    w[2] = __float_as_uint(v.z);
+    w[3] = __float_as_uint(v.w);
+}
+
+}  // namespace tgpu

@@ -1,0 +1,180 @@
+// Boids on the GPU, registered as "boids_see" / "boids_act".
+//
+// Model (separation / alignment / cohesion inside a sphere of radius r):
+//   see(a, b):  d = b.p - a.p, d2 = (dx*dx + dy*dy) + dz*dz, each product and sum rounded
+//               separately (no FMA), so the neighbour decision 0 < d2 < r2 is bit-identical
+//               to an IEEE evaluation of the same expression on the CPU;
+//               count++, coh += d, ali += b.v, sep -= d * (1 / d2)
+//   act(a):     if count > 0: acc = w_sep*sep/n + w_ali*(ali/n - v) + w_coh*(coh/n)/r,
+//               v += dt*acc; clamp |v| to max_speed; p += dt*v
+// Accumulators are per-step outputs: every see pass starts them from zero and the act
+// pass consumes them, so after a see+act step they read back as zero.
+//
+// AoS record (96 bytes): tag u32[2] @0, p float4 @8, v float4 @24, coh float4 @40,
+// ali float4 @56, sep float4 @72, count int @88, id int @92.
+// Streams: f4[0] POS, f4[1] VEL, u32[0] ID (state); f4[2] ACC0 = coh.xyz + count,
+// f4[3] ACC1 = ali.xyz, f4[4] ACC2 = sep.xyz (per-step).
+#include "model.cuh"
+
+namespace tgpu {
+namespace boids {
+
+enum { POS = 0, VEL = 1, ACC0 = 2, ACC1 = 3, ACC2 = 4 };
+enum { ID = 0 };
+
+struct Ctx {
+    float r, r2, w_sep, w_ali, w_coh, max_speed, dt, pad;
+};
+
+struct Seer {
+    float cx, cy, cz, ax, ay, az, sx, sy, sz;
+    int count;
+    float4 v;
+};
+
+TGPU_D void zero(Seer &s) {
+    s.cx = s.cy = s.cz = 0.0f;
+    s.ax = s.ay = s.az = 0.0f;
+    s.sx = s.sy = s.sz = 0.0f;
+    s.count = 0;
+}
+
+template <class Acc>
+TGPU_D void see_fn(Seer &s, const float4 &a, const float4 &b, const Acc &acc, uint32_t j, const Ctx &c) {
+    const float dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
+    float d2 = __fmul_rn(dx, dx);
+    d2 = __fadd_rn(d2, __fmul_rn(dy, dy));
+    d2 = __fadd_rn(d2, __fmul_rn(dz, dz));
+    if (d2 < c.r2 && d2 > 0.0f) {
+        const float inv = __frcp_rn(d2);
+        const float4 bv = acc.f4(1, j);
+        s.count += 1;
+        s.cx += dx;
+        s.cy += dy;
+        s.cz += dz;
+        s.ax += bv.x;
+        s.ay += bv.y;
+        s.az += bv.z;
+        s.sx -= dx * inv;
+        s.sy -= dy * inv;
+        s.sz -= dz * inv;
+    }
+}
+
+TGPU_D void act_fn(float4 &p, float4 &v, const Seer &s, const Ctx &c) {
+    if (s.count > 0) {
+        const float inv_n = 1.0f / (float)s.count;
+        const float inv_r = 1.0f / c.r;
+        const float accx = (c.w_sep * (s.sx * inv_n) + c.w_ali * (s.ax * inv_n - v.x)) + c.w_coh * ((s.cx * inv_n) * inv_r);
+        const float accy = (c.w_sep * (s.sy * inv_n) + c.w_ali * (s.ay * inv_n - v.y)) + c.w_coh * ((s.cy * inv_n) * inv_r);
+        const float accz = (c.w_sep * (s.sz * inv_n) + c.w_ali * (s.az * inv_n - v.z)) + c.w_coh * ((s.cz * inv_n) * inv_r);
+        v.x = v.x + c.dt * accx;
+        v.y = v.y + c.dt * accy;
+        v.z = v.z + c.dt * accz;
+    }
+    float s2 = v.x * v.x;
+    s2 = s2 + v.y * v.y;
+    s2 = s2 + v.z * v.z;
+    const float speed = sqrtf(s2);
+    if (speed > c.max_speed) {
+        const float k = c.max_speed / speed;
+        v.x *= k;
+        v.y *= k;
+        v.z *= k;
+    }
+    p.x = p.x + c.dt * v.x;
+    p.y = p.y + c.dt * v.y;
+    p.z = p.z + c.dt * v.z;
+}
+
+struct SeeOnly {
+    using SeeCtx = Ctx;
+    using ActCtx = Ctx;
+    using Seer = boids::Seer;
+    static constexpr int kSeenF4 = 2;
+    TGPU_D static int seen_stream(int k) { return k == 0 ? POS : VEL; }
+    TGPU_D static void load(Seer &s, const PassIO &, uint32_t, const Ctx &, const Ctx &) { zero(s); }
+    template <class Acc>
+    TGPU_D static void see(Seer &s, const float4 &a, const float4 &b, const Acc &acc, uint32_t j, const Ctx &c) {
+        see_fn(s, a, b, acc, j, c);
+    }
+    TGPU_D static void finish(Seer &s, const float4 &, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {
+        io.out_f4[ACC0][i] = make_float4(s.cx, s.cy, s.cz, __int_as_float(s.count));
+        io.out_f4[ACC1][i] = make_float4(s.ax, s.ay, s.az, 0.0f);
+        io.out_f4[ACC2][i] = make_float4(s.sx, s.sy, s.sz, 0.0f);
+    }
+};
+
+struct SeeAct {
+    using SeeCtx = Ctx;
+    using ActCtx = Ctx;
+    using Seer = boids::Seer;
+    static constexpr int kSeenF4 = 2;
+    TGPU_D static int seen_stream(int k) { return k == 0 ? POS : VEL; }
+    TGPU_D static void load(Seer &s, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {
+        zero(s);
+        s.v = io.in_f4[VEL][i];
+    }
+    template <class Acc>
+    TGPU_D static void see(Seer &s, const float4 &a, const float4 &b, const Acc &acc, uint32_t j, const Ctx &c) {
+        see_fn(s, a, b, acc, j, c);
+    }
+    TGPU_D static void finish(Seer &s, const float4 &a, const PassIO &io, uint32_t i, const Ctx &, const Ctx &c) {
+        float4 p = a, v = s.v;
+        act_fn(p, v, s, c);
+        io.out_f4[POS][i] = p;
+        io.out_f4[VEL][i] = v;
+    }
+};
+
+struct Codec {
+    static constexpr uint32_t kAgentBytes = 96;
+    TGPU_D static void pack(const uint32_t *w, const PassIO &io, uint32_t i) {
+        io.out_f4[POS][i] = ld_words4(w + 2);
+        io.out_f4[VEL][i] = ld_words4(w + 6);
+        io.out_u32[ID][i] = w[23];
+    }
+    // program 0: see only (accumulators visible); program 1: see + act (consumed)
+    TGPU_D static void unpack(uint32_t *w, const PassIO &io, uint32_t i, uint32_t program) {
+        w[0] = 0u;
+        w[1] = 0u;
+        st_words4(w + 2, io.in_f4[POS][i]);
+        st_words4(w + 6, io.in_f4[VEL][i]);
+        float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0, a2 = a0;
+        if (program == 0) {
+            a0 = io.in_f4[ACC0][i];
+            a1 = io.in_f4[ACC1][i];
+            a2 = io.in_f4[ACC2][i];
+        }
+        st_words4(w + 10, make_float4(a0.x, a0.y, a0.z, 0.f));
+        st_words4(w + 14, a1);
+        st_words4(w + 18, a2);
+        w[22] = __float_as_uint(a0.w);
+        w[23] = io.in_u32[ID][i];
+    }
+};
+
+constexpr uint32_t bit(int k) { return 1u << k; }
+
+const KernelDesc kKernels[] = {
+    {"boids_see", nullptr, bit(ACC0) | bit(ACC1) | bit(ACC2), 0, bit(POS) | bit(VEL), 2, launch_see_t<SeeOnly>, nullptr,
+     prepare_see_t<SeeOnly>},
+    {"boids_see", "boids_act", bit(POS) | bit(VEL), 0, bit(POS) | bit(VEL), 2, launch_see_t<SeeAct>, nullptr,
+     prepare_see_t<SeeAct>},
+};
+
+const ProgramDesc kPrograms[] = {
+    {1, {"boids_see"}, 1, {0}},
+    {2, {"boids_see", "boids_act"}, 1, {1}},
+};
+
+const ModelDesc kModel = {
+    "boids", 96, 5, 1, {kState, kState, kStep, kStep, kStep}, {kState}, (uint32_t)sizeof(Ctx), (uint32_t)sizeof(Ctx),
+    kKernels, 2, kPrograms, 2, pack_t<Codec>, unpack_t<Codec>,
+};
+
+}  // namespace boids
+
+const ModelDesc *model_boids() { return &boids::kModel; }
+
+}  // namespace tgpu

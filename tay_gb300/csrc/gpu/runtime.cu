@@ -1,0 +1,708 @@
+// Batch runtime behind the C ABI in include/tay_gpu.h.
+//
+// Owns the device buffers of a batch of segments, resolves the registered passes to a
+// device model and its fused kernels, and enqueues each step as:
+//   bounding box -> keys + radix passes -> cell table -> reorder of the state streams
+//   -> the model's pass kernels -> cell table clear
+// (the step of tay/state.c:221-311: sort every group, run the passes in order, unsort).
+// Steps are captured once per buffer-parity pattern into CUDA graphs and replayed.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "model.cuh"
+#include "tay_gpu.h"
+
+using namespace tgpu;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                          \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess)                                                                            \
+            return fail(TGPU_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+struct Tuning {
+    unsigned stage_cap = 0;
+    unsigned stage_cells = 0;
+    float cell_multiple = 1.0f;
+    int use_graphs = 1;
+};
+Tuning g_tuning;
+
+const ModelDesc *model_list(int i) {
+    switch (i) {
+        case 0: return model_test_basic();
+        case 1: return model_boids();
+        case 2: return model_sph();
+        default: return nullptr;
+    }
+}
+
+bool model_has_func(const ModelDesc *m, const char *name) {
+    for (int k = 0; k < m->nkernels; ++k) {
+        const KernelDesc &d = m->kernels[k];
+        if ((d.see && !strcmp(d.see, name)) || (d.act && !strcmp(d.act, name))) return true;
+    }
+    return false;
+}
+
+const ModelDesc *find_model(const char *name) {
+    for (int i = 0; const ModelDesc *m = model_list(i); ++i)
+        if (model_has_func(m, name)) return m;
+    return nullptr;
+}
+
+uint32_t next_pow2(uint32_t v) {
+    uint32_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+uint32_t log2u(uint32_t v) {
+    uint32_t n = 0;
+    while ((1u << n) < v) ++n;
+    return n;
+}
+
+struct KernelRun {
+    const KernelDesc *k;
+    int see_pass;  // index into the group's pass list, or -1
+    int act_pass;
+    float4 *d_radii = nullptr;  // [segments]
+    char *d_see_ctx = nullptr;  // [segments * ctx_stride]
+    char *d_act_ctx = nullptr;
+    size_t smem = 0;
+    uint32_t stage_cap = 0, stage_cells = 0;
+    int skip_self = 0;
+};
+
+struct HostSeg {
+    TgpuGroup g;
+    std::vector<TgpuPass> passes;
+    float host_min[3], host_max[3];
+    bool pushed = false;
+};
+
+}  // namespace
+
+struct TgpuBatch {
+    const ModelDesc *m = nullptr;
+    int program = -1;
+    int nseg = 0;
+    uint32_t total = 0;
+    std::vector<HostSeg> hs;
+    std::vector<SegmentSpec> specs;
+    std::vector<uint32_t> tile_seg;
+    std::vector<uint2> cta;
+    uint32_t tiles = 0, ctas = 0, key_bits = 0;
+    bool specs_dirty = true;
+
+    SegmentSpec *d_specs = nullptr;
+    uint32_t *d_tile_seg = nullptr;
+    uint2 *d_cta = nullptr;
+    BoxAcc *d_box = nullptr;
+    float4 *f4[kMaxF4][2] = {};
+    uint32_t *u32[kMaxU32][2] = {};
+    int cur_f4[kMaxF4] = {};
+    int cur_u32[kMaxU32] = {};
+    uint32_t *keys[2] = {}, *vals[2] = {}, *counts = nullptr, *partials = nullptr;
+    uint2 *table = nullptr;
+    size_t table_entries = 0;
+    uint32_t *d_aos = nullptr;
+    unsigned long long *d_pairs = nullptr;
+    size_t ctx_stride = 0;
+    std::vector<KernelRun> runs;
+    int launches_per_step = 0;
+
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    double last_ms = 0.0;
+    unsigned long long last_pairs = 0;
+    bool use_graphs = true;
+    std::map<uint64_t, cudaGraphExec_t> graphs;
+};
+
+namespace {
+
+void free_batch(TgpuBatch *b) {
+    if (!b) return;
+    for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    cudaFree(b->d_specs);
+    cudaFree(b->d_tile_seg);
+    cudaFree(b->d_cta);
+    cudaFree(b->d_box);
+    for (int c = 0; c < kMaxF4; ++c)
+        for (int k = 0; k < 2; ++k) cudaFree(b->f4[c][k]);
+    for (int c = 0; c < kMaxU32; ++c)
+        for (int k = 0; k < 2; ++k) cudaFree(b->u32[c][k]);
+    for (int k = 0; k < 2; ++k) {
+        cudaFree(b->keys[k]);
+        cudaFree(b->vals[k]);
+    }
+    cudaFree(b->counts);
+    cudaFree(b->partials);
+    cudaFree(b->table);
+    cudaFree(b->d_aos);
+    cudaFree(b->d_pairs);
+    for (auto &r : b->runs) {
+        cudaFree(r.d_radii);
+        cudaFree(r.d_see_ctx);
+        cudaFree(r.d_act_ctx);
+    }
+    if (b->e0) cudaEventDestroy(b->e0);
+    if (b->e1) cudaEventDestroy(b->e1);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+}
+
+// Matches a group's pass list against the model's supported sequences.
+int match_program(const ModelDesc *m, const TgpuGroup &g) {
+    for (int p = 0; p < m->nprograms; ++p) {
+        const ProgramDesc &pd = m->programs[p];
+        if (pd.passes != g.pass_count) continue;
+        bool ok = true;
+        for (int k = 0; k < pd.passes && ok; ++k) ok = !strcmp(pd.names[k], g.passes[k].func_name);
+        if (ok) return p;
+    }
+    return -1;
+}
+
+int pass_index(const TgpuGroup &g, const char *name, int from) {
+    for (int k = from; k < g.pass_count; ++k)
+        if (!strcmp(g.passes[k].func_name, name)) return k;
+    return -1;
+}
+
+int upload_contexts(TgpuBatch *b, int seg) {
+    std::vector<char> buf(b->ctx_stride);
+    const HostSeg &h = b->hs[seg];
+    for (auto &r : b->runs) {
+        for (int which = 0; which < 2; ++which) {
+            int p = which == 0 ? r.see_pass : r.act_pass;
+            char *dst = which == 0 ? r.d_see_ctx : r.d_act_ctx;
+            if (p < 0 || !dst) continue;
+            std::fill(buf.begin(), buf.end(), 0);
+            const TgpuPass &tp = h.passes[p];
+            if (tp.context && tp.context_size)
+                memcpy(buf.data(), tp.context, std::min((size_t)tp.context_size, b->ctx_stride));
+            CK(cudaMemcpyAsync(dst + (size_t)seg * b->ctx_stride, buf.data(), b->ctx_stride, cudaMemcpyHostToDevice,
+                               b->st));
+        }
+        if (r.see_pass >= 0) {
+            const TgpuPass &tp = h.passes[r.see_pass];
+            float4 rr = make_float4(tp.radii[0], tp.radii[1], tp.radii[2], tp.radii[3]);
+            CK(cudaMemcpyAsync(r.d_radii + seg, &rr, sizeof(float4), cudaMemcpyHostToDevice, b->st));
+        }
+    }
+    CK(cudaStreamSynchronize(b->st));
+    return TGPU_OK;
+}
+
+// Per-segment grid bounds from the pushed agents: each axis gets a power-of-two cell
+// budget with 10% headroom over the pushed extent (bounded to 1024, the 10-bit Morton
+// limit); the dense table gets at most shared_megabytes of uint2 entries.
+int prepare_specs(TgpuBatch *b) {
+    if (!b->specs_dirty) return TGPU_OK;
+    b->specs_dirty = false;
+    std::vector<SegmentSpec> next = b->specs;
+    uint64_t table_total = 0;
+    uint32_t max_axis = 2;
+    for (int s = 0; s < b->nseg; ++s) {
+        SegmentSpec &sp = next[s];
+        const HostSeg &h = b->hs[s];
+        uint32_t axis = 2;
+        for (int a = 0; a < 3; ++a) {
+            float lo = h.g.box_fixed ? h.g.box_min[a] : h.host_min[a];
+            float hi = h.g.box_fixed ? h.g.box_max[a] : h.host_max[a];
+            float ext = hi > lo ? hi - lo : 0.0f;
+            double cells = floor((double)ext / (double)sp.part[a]) + 1.0;
+            uint32_t want = (uint32_t)std::min(1024.0, std::max(2.0, ceil(cells * 1.1)));
+            axis = std::max(axis, next_pow2(want));
+        }
+        axis = std::min(axis, 1024u);
+        sp.axis_cells_max = axis;
+        uint64_t cap_mem = ((uint64_t)std::max(h.g.shared_megabytes, 1) << 20) / sizeof(uint2);
+        uint64_t cap_axis = (uint64_t)axis * axis * axis;
+        uint64_t cap = std::min(cap_mem, cap_axis);
+        cap = std::max<uint64_t>(cap, 8);
+        cap = std::min<uint64_t>(cap, 0x7FFFFFFFull);
+        sp.table_base = (uint32_t)table_total;
+        sp.table_cap = (uint32_t)cap;
+        table_total += cap;
+        max_axis = std::max(max_axis, axis);
+    }
+    if (table_total > 0xFFFFFFFFull)
+        return fail(TGPU_ERR_ARG, "cell tables too large (%llu entries)", (unsigned long long)table_total);
+    const uint32_t key_bits = 3 * log2u(max_axis);
+    const bool same = b->table && key_bits == b->key_bits &&
+                      !memcmp(next.data(), b->specs.data(), sizeof(SegmentSpec) * b->nseg);
+    if (same) return TGPU_OK;  // the table is left clean by every completed step
+    b->specs = next;
+    b->key_bits = key_bits;
+    if (table_total > b->table_entries) {
+        cudaFree(b->table);
+        b->table = nullptr;
+        b->table_entries = 0;
+        CK(cudaMalloc(&b->table, table_total * sizeof(uint2)));
+        b->table_entries = table_total;
+    }
+    CK(cudaMemsetAsync(b->table, 0, b->table_entries * sizeof(uint2), b->st));
+    CK(cudaMemcpyAsync(b->d_specs, b->specs.data(), sizeof(SegmentSpec) * b->nseg, cudaMemcpyHostToDevice, b->st));
+    for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    b->graphs.clear();
+    const int passes = (int)((b->key_bits + 7) / 8);
+    b->launches_per_step = 2 + passes * 5 + 1 + 1 + (int)b->runs.size() + 1;
+    return TGPU_OK;
+}
+
+PassIO make_io(TgpuBatch *b, const KernelDesc *k, bool fused_see, uint32_t offset) {
+    PassIO io{};
+    for (int c = 0; c < b->m->nf4; ++c) {
+        if (b->m->role_f4[c] == kState) {
+            io.in_f4[c] = b->f4[c][b->cur_f4[c]] + offset;
+            if (k && (k->writes_f4 >> c & 1u)) {
+                bool alt = fused_see && (k->seen_f4 >> c & 1u);
+                io.out_f4[c] = b->f4[c][alt ? 1 - b->cur_f4[c] : b->cur_f4[c]] + offset;
+            } else {
+                io.out_f4[c] = b->f4[c][b->cur_f4[c]] + offset;
+            }
+        } else {
+            io.in_f4[c] = b->f4[c][0] + offset;
+            io.out_f4[c] = b->f4[c][0] + offset;
+        }
+    }
+    for (int c = 0; c < b->m->nu32; ++c) {
+        io.in_u32[c] = b->u32[c][b->cur_u32[c]] + offset;
+        io.out_u32[c] = b->u32[c][b->cur_u32[c]] + offset;
+    }
+    return io;
+}
+
+SortLaunch sort_launch(TgpuBatch *b) {
+    SortLaunch L{};
+    L.specs = b->d_specs;
+    L.tile_seg = b->d_tile_seg;
+    L.box = b->d_box;
+    L.pos = b->f4[0][b->cur_f4[0]];
+    L.keys[0] = b->keys[0];
+    L.keys[1] = b->keys[1];
+    L.vals[0] = b->vals[0];
+    L.vals[1] = b->vals[1];
+    L.counts = b->counts;
+    L.partials = b->partials;
+    L.table = b->table;
+    L.segments = (uint32_t)b->nseg;
+    L.tiles = b->tiles;
+    L.key_bits = b->key_bits;
+    return L;
+}
+
+void enqueue_step(TgpuBatch *b) {
+    if (b->total == 0 || b->tiles == 0) return;
+    cudaStream_t st = b->st;
+    SortLaunch L = sort_launch(b);
+    launch_box(L, st);
+    uint32_t *skeys = nullptr, *perm = nullptr;
+    launch_sort(L, st, &skeys, &perm);
+    launch_cell_table(L, skeys, 1, st);
+
+    GatherSet g{};
+    for (int c = 0; c < b->m->nf4; ++c) {
+        if (b->m->role_f4[c] != kState) continue;
+        g.src_f4[g.nf4] = b->f4[c][b->cur_f4[c]];
+        g.dst_f4[g.nf4] = b->f4[c][1 - b->cur_f4[c]];
+        b->cur_f4[c] ^= 1;
+        ++g.nf4;
+    }
+    for (int c = 0; c < b->m->nu32; ++c) {
+        if (b->m->role_u32[c] != kState) continue;
+        g.src_u32[g.nu32] = b->u32[c][b->cur_u32[c]];
+        g.dst_u32[g.nu32] = b->u32[c][1 - b->cur_u32[c]];
+        b->cur_u32[c] ^= 1;
+        ++g.nu32;
+    }
+    launch_gather(b->total, perm, g, st);
+
+    for (auto &r : b->runs) {
+        const bool see = r.k->see != nullptr;
+        PassIO io = make_io(b, r.k, see, 0);
+        if (see) {
+            SeeLaunch S{};
+            S.specs = b->d_specs;
+            S.box = b->d_box;
+            S.table = b->table;
+            S.cta_table = b->d_cta;
+            S.radii = r.d_radii;
+            S.ctx = r.d_see_ctx;
+            S.ctx_stride = (uint32_t)b->ctx_stride;
+            S.act_ctx = r.d_act_ctx ? r.d_act_ctx : r.d_see_ctx;
+            S.act_ctx_stride = (uint32_t)b->ctx_stride;
+            S.ctas = b->ctas;
+            S.skip_self = r.skip_self;
+            S.stage_cap = r.stage_cap;
+            S.stage_cells = r.stage_cells;
+            S.pairs = b->d_pairs;
+            S.io = io;
+            r.k->launch_see(S, r.smem, st);
+            for (int c = 0; c < b->m->nf4; ++c)
+                if (b->m->role_f4[c] == kState && (r.k->writes_f4 >> c & 1u) && (r.k->seen_f4 >> c & 1u))
+                    b->cur_f4[c] ^= 1;
+        } else {
+            ActLaunch A{};
+            A.specs = b->d_specs;
+            A.tile_seg = b->d_tile_seg;
+            A.ctx = r.d_act_ctx;
+            A.ctx_stride = (uint32_t)b->ctx_stride;
+            A.tiles = b->tiles;
+            A.io = io;
+            r.k->launch_act(A, st);
+        }
+    }
+    launch_cell_table(L, skeys, 0, st);
+}
+
+uint64_t parity_signature(const TgpuBatch *b) {
+    uint64_t s = 0;
+    for (int c = 0; c < kMaxF4; ++c) s |= (uint64_t)b->cur_f4[c] << c;
+    for (int c = 0; c < kMaxU32; ++c) s |= (uint64_t)b->cur_u32[c] << (kMaxF4 + c);
+    return s;
+}
+
+// Host-side buffer parity after one step, mirroring the flips enqueue_step makes (used
+// when a captured step is replayed instead of re-enqueued).
+void advance_parity(TgpuBatch *b) {
+    for (int c = 0; c < b->m->nf4; ++c)
+        if (b->m->role_f4[c] == kState) b->cur_f4[c] ^= 1;
+    for (int c = 0; c < b->m->nu32; ++c)
+        if (b->m->role_u32[c] == kState) b->cur_u32[c] ^= 1;
+    for (auto &r : b->runs)
+        if (r.k->see)
+            for (int c = 0; c < b->m->nf4; ++c)
+                if (b->m->role_f4[c] == kState && (r.k->writes_f4 >> c & 1u) && (r.k->seen_f4 >> c & 1u))
+                    b->cur_f4[c] ^= 1;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+
+extern "C" {
+
+const char *tgpu_last_error(void) { return g_err.c_str(); }
+
+int tgpu_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+void tgpu_set_tuning(unsigned stage_cap, unsigned stage_cells, float cell_multiple, int use_graphs) {
+    g_tuning.stage_cap = stage_cap;
+    g_tuning.stage_cells = stage_cells;
+    g_tuning.cell_multiple = cell_multiple > 0.0f ? cell_multiple : 1.0f;
+    g_tuning.use_graphs = use_graphs;
+}
+
+const char *tgpu_model_of(const char *func_name) {
+    const ModelDesc *m = func_name ? find_model(func_name) : nullptr;
+    return m ? m->name : nullptr;
+}
+
+const char *tgpu_batch_model(const TgpuBatch *b) { return b && b->m ? b->m->name : nullptr; }
+int tgpu_batch_program(const TgpuBatch *b) { return b ? b->program : -1; }
+double tgpu_batch_last_device_ms(const TgpuBatch *b) { return b ? b->last_ms : 0.0; }
+unsigned long long tgpu_batch_last_pairs(const TgpuBatch *b) { return b ? b->last_pairs : 0ull; }
+int tgpu_batch_launches_per_step(const TgpuBatch *b) { return b ? b->launches_per_step : 0; }
+
+void tgpu_batch_destroy(TgpuBatch *b) { free_batch(b); }
+
+int tgpu_batch_create(const TgpuGroup *groups, int group_count, TgpuBatch **out) {
+    if (!out || !groups || group_count <= 0) return fail(TGPU_ERR_ARG, "no groups");
+    *out = nullptr;
+    const TgpuGroup &g0 = groups[0];
+    if (g0.pass_count <= 0 || !g0.passes) return fail(TGPU_ERR_ARG, "group has no passes");
+    const ModelDesc *m = find_model(g0.passes[0].func_name ? g0.passes[0].func_name : "");
+    if (!m) return fail(TGPU_ERR_UNKNOWN_FUNC, "no device model provides '%s'", g0.passes[0].func_name);
+    for (int k = 0; k < g0.pass_count; ++k)
+        if (!g0.passes[k].func_name || !model_has_func(m, g0.passes[k].func_name))
+            return fail(TGPU_ERR_UNKNOWN_FUNC, "func '%s' is not part of device model '%s'",
+                        g0.passes[k].func_name ? g0.passes[k].func_name : "(null)", m->name);
+    const int program = match_program(m, g0);
+    if (program < 0) return fail(TGPU_ERR_PROGRAM, "pass sequence not supported by device model '%s'", m->name);
+
+    TgpuBatch *b = new TgpuBatch();
+    b->m = m;
+    b->program = program;
+    b->nseg = group_count;
+    b->use_graphs = g_tuning.use_graphs != 0;
+    uint32_t total = 0;
+    for (int s = 0; s < group_count; ++s) {
+        const TgpuGroup &g = groups[s];
+        if (g.agent_size != m->agent_bytes) {
+            free_batch(b);
+            return fail(TGPU_ERR_ARG, "group %d: agent size %u, device model '%s' expects %u", s, g.agent_size, m->name,
+                        m->agent_bytes);
+        }
+        if (match_program(m, g) != program) {
+            free_batch(b);
+            return fail(TGPU_ERR_ARG, "group %d: pass sequence differs from group 0", s);
+        }
+        HostSeg h;
+        h.g = g;
+        h.passes.assign(g.passes, g.passes + g.pass_count);
+        h.g.passes = nullptr;
+        for (int a = 0; a < 3; ++a) {
+            h.host_min[a] = 0.0f;
+            h.host_max[a] = 0.0f;
+        }
+        b->hs.push_back(h);
+        SegmentSpec sp{};
+        sp.begin = total;
+        sp.count = g.count;
+        sp.fixed_box = g.box_fixed ? 1u : 0u;
+        for (int a = 0; a < 3; ++a) {
+            float part = g.min_part_sizes[a] > 0.0f ? g.min_part_sizes[a] : 1.0f;
+            sp.part[a] = part * g_tuning.cell_multiple;
+            sp.box_min[a] = g.box_min[a];
+            sp.box_max[a] = g.box_max[a];
+            float reach = 0.0f;
+            for (int k = 0; k < g.pass_count; ++k)
+                if (g.passes[k].is_see) reach = std::max(reach, g.passes[k].radii[a]);
+            sp.reach[a] = reach;
+        }
+        sp.tile_begin = (uint32_t)b->tile_seg.size();
+        sp.tile_count = (g.count + kSortTile - 1) / kSortTile;
+        for (uint32_t t = 0; t < sp.tile_count; ++t) b->tile_seg.push_back((uint32_t)s);
+        for (uint32_t c = 0; c < g.count; c += kSeeThreads) b->cta.push_back(make_uint2((uint32_t)s, total + c));
+        b->specs.push_back(sp);
+        total += g.count;
+    }
+    b->total = total;
+    b->tiles = (uint32_t)b->tile_seg.size();
+    b->ctas = (uint32_t)b->cta.size();
+
+    auto bail = [&](int code) {
+        free_batch(b);
+        return code;
+    };
+#define CKB(call)                                                                                    \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) {                                                                     \
+            fail(TGPU_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));                     \
+            return bail(TGPU_ERR_CUDA);                                                              \
+        }                                                                                            \
+    } while (0)
+
+    CKB(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+    CKB(cudaEventCreate(&b->e0));
+    CKB(cudaEventCreate(&b->e1));
+    const size_t n = std::max<uint32_t>(total, 1);
+    CKB(cudaMalloc(&b->d_specs, sizeof(SegmentSpec) * b->nseg));
+    CKB(cudaMalloc(&b->d_tile_seg, sizeof(uint32_t) * std::max<uint32_t>(b->tiles, 1)));
+    CKB(cudaMalloc(&b->d_cta, sizeof(uint2) * std::max<uint32_t>(b->ctas, 1)));
+    CKB(cudaMalloc(&b->d_box, sizeof(BoxAcc) * b->nseg));
+    if (b->tiles) CKB(cudaMemcpy(b->d_tile_seg, b->tile_seg.data(), sizeof(uint32_t) * b->tiles, cudaMemcpyHostToDevice));
+    if (b->ctas) CKB(cudaMemcpy(b->d_cta, b->cta.data(), sizeof(uint2) * b->ctas, cudaMemcpyHostToDevice));
+    for (int c = 0; c < m->nf4; ++c) {
+        CKB(cudaMalloc(&b->f4[c][0], sizeof(float4) * n));
+        CKB(cudaMemset(b->f4[c][0], 0, sizeof(float4) * n));
+        if (m->role_f4[c] == kState) {
+            CKB(cudaMalloc(&b->f4[c][1], sizeof(float4) * n));
+            CKB(cudaMemset(b->f4[c][1], 0, sizeof(float4) * n));
+        }
+    }
+    for (int c = 0; c < m->nu32; ++c) {
+        CKB(cudaMalloc(&b->u32[c][0], sizeof(uint32_t) * n));
+        CKB(cudaMalloc(&b->u32[c][1], sizeof(uint32_t) * n));
+    }
+    for (int k = 0; k < 2; ++k) {
+        CKB(cudaMalloc(&b->keys[k], sizeof(uint32_t) * n));
+        CKB(cudaMalloc(&b->vals[k], sizeof(uint32_t) * n));
+    }
+    const size_t ncounts = 256ull * std::max<uint32_t>(b->tiles, 1);
+    CKB(cudaMalloc(&b->counts, sizeof(uint32_t) * ncounts));
+    CKB(cudaMalloc(&b->partials, sizeof(uint32_t) * ((ncounts + 4095) / 4096 + 1)));
+    if ((ncounts + 4095) / 4096 > 4096) {
+        fail(TGPU_ERR_ARG, "batch too large for the scan spine (%u tiles)", b->tiles);
+        return bail(TGPU_ERR_ARG);
+    }
+    CKB(cudaMalloc(&b->d_aos, (size_t)m->agent_bytes * n));
+    CKB(cudaMalloc(&b->d_pairs, sizeof(unsigned long long)));
+
+    b->ctx_stride = (std::max(m->see_ctx_bytes, m->act_ctx_bytes) + 15u) & ~15u;
+    const ProgramDesc &pd = m->programs[program];
+    int cursor = 0;
+    for (int k = 0; k < pd.kernels; ++k) {
+        KernelRun r{};
+        r.k = &m->kernels[pd.kernel_index[k]];
+        r.see_pass = r.k->see ? pass_index(g0, r.k->see, cursor) : -1;
+        r.act_pass = r.k->act ? pass_index(g0, r.k->act, r.see_pass >= 0 ? r.see_pass + 1 : cursor) : -1;
+        cursor = std::max(r.see_pass, r.act_pass) + 1;
+        if (r.see_pass >= 0) {
+            const TgpuPass &tp = g0.passes[r.see_pass];
+            r.skip_self = tp.self_see ? 0 : 1;
+            CKB(cudaMalloc(&r.d_radii, sizeof(float4) * b->nseg));
+            CKB(cudaMalloc(&r.d_see_ctx, b->ctx_stride * b->nseg));
+            const uint32_t cap_default = r.k->staged_f4 <= 1 ? 2048u : 1536u;
+            r.stage_cap = g_tuning.stage_cap ? g_tuning.stage_cap : cap_default;
+            r.stage_cells = g_tuning.stage_cells ? g_tuning.stage_cells : 1024u;
+            r.smem = (size_t)r.k->staged_f4 * r.stage_cap * sizeof(float4) + (2ull * r.stage_cells + 1) * sizeof(uint32_t);
+            if (r.smem > 220 * 1024) {
+                fail(TGPU_ERR_ARG, "staging buffer of %zu bytes exceeds shared memory", r.smem);
+                return bail(TGPU_ERR_ARG);
+            }
+            CKB(r.k->prepare(r.smem));
+        }
+        if (r.act_pass >= 0) CKB(cudaMalloc(&r.d_act_ctx, b->ctx_stride * b->nseg));
+        b->runs.push_back(r);
+    }
+    for (int s = 0; s < b->nseg; ++s) {
+        int rc = upload_contexts(b, s);
+        if (rc) return bail(rc);
+    }
+    *out = b;
+#undef CKB
+    return TGPU_OK;
+}
+
+int tgpu_batch_set_contexts(TgpuBatch *b, int group, const TgpuGroup *desc) {
+    if (!b || !desc || group < 0 || group >= b->nseg) return fail(TGPU_ERR_ARG, "bad group");
+    if (desc->pass_count != (int)b->hs[group].passes.size()) return fail(TGPU_ERR_ARG, "pass count changed");
+    for (int k = 0; k < desc->pass_count; ++k) {
+        b->hs[group].passes[k].context = desc->passes[k].context;
+        b->hs[group].passes[k].context_size = desc->passes[k].context_size;
+        for (int a = 0; a < 4; ++a) b->hs[group].passes[k].radii[a] = desc->passes[k].radii[a];
+    }
+    return upload_contexts(b, group);
+}
+
+int tgpu_batch_push(TgpuBatch *b, int group, const void *host) {
+    if (!b || group < 0 || group >= b->nseg || !host) return fail(TGPU_ERR_ARG, "bad push");
+    HostSeg &h = b->hs[group];
+    const SegmentSpec &sp = b->specs[group];
+    const uint32_t n = sp.count;
+    // extent of the pushed positions (float4 right after the 8-byte tag)
+    float mn[3] = {0.f, 0.f, 0.f}, mx[3] = {0.f, 0.f, 0.f};
+    const char *rec = (const char *)host;
+    for (uint32_t i = 0; i < n; ++i) {
+        float p[3];
+        memcpy(p, rec + (size_t)i * b->m->agent_bytes + 8, sizeof(p));
+        for (int a = 0; a < 3; ++a) {
+            if (i == 0 || p[a] < mn[a]) mn[a] = p[a];
+            if (i == 0 || p[a] > mx[a]) mx[a] = p[a];
+        }
+    }
+    for (int a = 0; a < 3; ++a) {
+        h.host_min[a] = mn[a];
+        h.host_max[a] = mx[a];
+    }
+    h.pushed = true;
+    b->specs_dirty = true;
+    if (!n) return TGPU_OK;
+    uint32_t *aos = b->d_aos + (size_t)sp.begin * (b->m->agent_bytes / 4);
+    CK(cudaMemcpyAsync(aos, host, (size_t)n * b->m->agent_bytes, cudaMemcpyHostToDevice, b->st));
+    // pack into the current buffers of every stream
+    PassIO io{};
+    for (int c = 0; c < b->m->nf4; ++c) {
+        int k = b->m->role_f4[c] == kState ? b->cur_f4[c] : 0;
+        io.out_f4[c] = b->f4[c][k] + sp.begin;
+        io.in_f4[c] = io.out_f4[c];
+    }
+    for (int c = 0; c < b->m->nu32; ++c) {
+        io.out_u32[c] = b->u32[c][b->cur_u32[c]] + sp.begin;
+        io.in_u32[c] = io.out_u32[c];
+    }
+    b->m->pack(aos, n, io, b->st);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(b->st));
+    return TGPU_OK;
+}
+
+int tgpu_batch_enqueue(TgpuBatch *b, int steps) {
+    if (!b || steps < 0) return fail(TGPU_ERR_ARG, "bad run");
+    int rc = prepare_specs(b);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(b->d_pairs, 0, sizeof(unsigned long long), b->st));
+    CK(cudaEventRecord(b->e0, b->st));
+    for (int i = 0; i < steps; ++i) {
+        if (!b->use_graphs) {
+            enqueue_step(b);
+            continue;
+        }
+        const uint64_t sig = parity_signature(b);
+        auto it = b->graphs.find(sig);
+        if (it != b->graphs.end()) {
+            CK(cudaGraphLaunch(it->second, b->st));
+            advance_parity(b);
+            continue;
+        }
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+        enqueue_step(b);
+        CK(cudaStreamEndCapture(b->st, &graph));
+        cudaGraphExec_t exec = nullptr;
+        cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(TGPU_ERR_CUDA, "cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
+        b->graphs.emplace(sig, exec);
+        CK(cudaGraphLaunch(exec, b->st));
+    }
+    CK(cudaEventRecord(b->e1, b->st));
+    CK(cudaGetLastError());
+    return TGPU_OK;
+}
+
+int tgpu_batch_sync(TgpuBatch *b) {
+    if (!b) return fail(TGPU_ERR_ARG, "null batch");
+    CK(cudaStreamSynchronize(b->st));
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, b->e0, b->e1));
+    b->last_ms = ms;
+    CK(cudaMemcpy(&b->last_pairs, b->d_pairs, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    return TGPU_OK;
+}
+
+int tgpu_batch_run(TgpuBatch *b, int steps) {
+    int rc = tgpu_batch_enqueue(b, steps);
+    if (rc) return rc;
+    return tgpu_batch_sync(b);
+}
+
+int tgpu_batch_fetch(TgpuBatch *b, int group, void *host) {
+    if (!b || group < 0 || group >= b->nseg || !host) return fail(TGPU_ERR_ARG, "bad fetch");
+    const SegmentSpec &sp = b->specs[group];
+    if (!sp.count) return TGPU_OK;
+    uint32_t *aos = b->d_aos + (size_t)sp.begin * (b->m->agent_bytes / 4);
+    PassIO io = make_io(b, nullptr, false, sp.begin);
+    b->m->unpack(aos, sp.count, io, (uint32_t)b->program, b->st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(host, aos, (size_t)sp.count * b->m->agent_bytes, cudaMemcpyDeviceToHost, b->st));
+    CK(cudaStreamSynchronize(b->st));
+    return TGPU_OK;
+}
+
+}  // extern "C"

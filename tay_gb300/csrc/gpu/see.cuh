@@ -1,0 +1,293 @@
+// See-pass and act-pass kernel templates.
+//
+// See pass (replaces tay/cpu_z_grid.c:232-321 + tay/space.c:106-148, and the generated
+// OpenCL see kernel, tay/ocl_grid.c:376-417 + tay/ocl_generics.c:13-114):
+//   * one CTA = 128 consecutive seers in cell order (never crossing a segment);
+//   * each seer's neighbour cells are the cells overlapping its box p +- r (padded by a
+//     fraction of a cell against rounding), clamped to the grid;
+//   * the CTA stages every cell of the union of its seers' cell boxes into shared
+//     memory, cells in row-major order, so each (y, z) row of cells is one contiguous
+//     run of staged agents;
+//   * each warp walks the rows of the union of its 32 seers' boxes; all 32 lanes read
+//     the same staged agent (a shared-memory broadcast), apply the reference's inclusive
+//     per-axis box test (space.c:62-68: skip when d < -r || d > r, d = seer - seen) and,
+//     when it passes, call the model's see function on registers: no atomics on agent
+//     state, the seer writes only its own accumulators;
+//   * when the halo does not fit the staging buffer, the same walk reads the cells from
+//     global memory through the dense cell table.
+// Act pass (replaces tay/space.c:250-263): one thread per agent.
+#pragma once
+
+#include <climits>
+
+#include "tgpu_internal.cuh"
+#include "tgpu_kernels.cuh"
+
+namespace tgpu {
+
+namespace see_detail {
+
+TGPU_D int warp_min_i(int v) {
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+TGPU_D int warp_max_i(int v) {
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+TGPU_D uint32_t warp_sum_u(uint32_t v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Cell range along one axis for the interval [p - r, p + r], widened by `pad` cells on
+// each side so that rounding in the key computation can never put a neighbour that
+// passes the box test outside the range.
+TGPU_D void axis_range(float p, float r, float origin, float inv_cs, int dim, float pad, int &lo, int &hi) {
+    float a = ((p - r) - origin) * inv_cs - pad;
+    float b = ((p + r) - origin) * inv_cs + pad;
+    int l = (int)floorf(a), h = (int)floorf(b);
+    lo = l < 0 ? 0 : (l >= dim ? dim - 1 : l);
+    hi = h < 0 ? 0 : (h >= dim ? dim - 1 : h);
+}
+
+// Inclusive per-axis box test of the reference: a pair is skipped when any
+// d = seer - seen satisfies d < -r || d > r, i.e. |d| > r (NaN compares false both ways).
+TGPU_D bool box_hit(const float4 &a, const float4 &b, const float4 &r) {
+    return !(fabsf(a.x - b.x) > r.x) && !(fabsf(a.y - b.y) > r.y) && !(fabsf(a.z - b.z) > r.z);
+}
+
+struct SmemSeen {
+    const float4 *base;
+    uint32_t cap;
+    TGPU_D float4 f4(int k, uint32_t j) const { return base[(uint32_t)k * cap + j]; }
+};
+
+template <int N>
+struct GlobalSeen {
+    const float4 *s[N];
+    TGPU_D float4 f4(int k, uint32_t j) const { return __ldg(s[k] + j); }
+};
+
+// Largest rounding error, in cells, of a cell coordinate computed as
+// floor((p - origin) * inv_cs): a few ulps of the largest coordinate magnitude plus the
+// relative error of the multiply on coordinates up to 1024 cells.
+TGPU_D float grid_pad(const Grid &g, const SegmentSpec &s, const BoxAcc &b) {
+    float m = 0.0f, csmin = g.cs[0];
+    for (int a = 0; a < 3; ++a) {
+        float lo = s.fixed_box ? s.box_min[a] : ordered_to_float(b.lo[a]);
+        float hi = s.fixed_box ? s.box_max[a] : ordered_to_float(b.hi[a]);
+        m = fmaxf(m, fmaxf(fabsf(lo), fabsf(hi)));
+        csmin = fminf(csmin, g.cs[a]);
+    }
+    float ulp = m * 1.1920929e-7f;  // 2^-23
+    return fmaxf(1.0f / 512.0f, 16.0f * ulp / csmin + 1024.0f * 4.0f * 1.1920929e-7f);
+}
+
+}  // namespace see_detail
+
+template <class P>
+__global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
+    using namespace see_detail;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4 *stage = reinterpret_cast<float4 *>(smem_raw);
+    uint32_t *cell_off = reinterpret_cast<uint32_t *>(stage + (size_t)P::kSeenF4 * L.stage_cap);
+    uint32_t *cell_first = cell_off + L.stage_cells + 1;
+    __shared__ int hbox[6];
+    __shared__ uint32_t warp_sums[kSeeThreads / 32];
+    __shared__ uint32_t s_total;
+
+    const uint2 cta = L.cta_table[blockIdx.x];
+    const uint32_t seg = cta.x;
+    const SegmentSpec S = L.specs[seg];
+    const BoxAcc B = L.box[seg];
+    const Grid g = segment_grid(S, B);
+    const float pad = grid_pad(g, S, B);
+    const float4 r4 = L.radii[seg];
+    const typename P::SeeCtx &sctx = *reinterpret_cast<const typename P::SeeCtx *>(L.ctx + (size_t)seg * L.ctx_stride);
+    const typename P::ActCtx &actx =
+        *reinterpret_cast<const typename P::ActCtx *>(L.act_ctx + (size_t)seg * L.act_ctx_stride);
+    const uint32_t seg_end = S.begin + S.count;
+    const uint32_t i = cta.y + threadIdx.x;
+    const bool active = i < seg_end;
+    const uint32_t lane = threadIdx.x & 31u;
+
+    float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
+    typename P::Seer s;
+    int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
+    if (active) {
+        sp = L.io.in_f4[0][i];
+        P::load(s, L.io, i, sctx, actx);
+        axis_range(sp.x, r4.x, g.origin[0], g.inv_cs[0], g.dims[0], pad, lo[0], hi[0]);
+        axis_range(sp.y, r4.y, g.origin[1], g.inv_cs[1], g.dims[1], pad, lo[1], hi[1]);
+        axis_range(sp.z, r4.z, g.origin[2], g.inv_cs[2], g.dims[2], pad, lo[2], hi[2]);
+    }
+
+    // CTA halo box = union of the seers' cell boxes
+    if (threadIdx.x < 6) hbox[threadIdx.x] = threadIdx.x < 3 ? INT_MAX : INT_MIN;
+    __syncthreads();
+    {
+        int l0 = warp_min_i(lo[0]), l1 = warp_min_i(lo[1]), l2 = warp_min_i(lo[2]);
+        int h0 = warp_max_i(hi[0]), h1 = warp_max_i(hi[1]), h2 = warp_max_i(hi[2]);
+        if (lane == 0 && l0 <= h0) {
+            atomicMin(&hbox[0], l0);
+            atomicMin(&hbox[1], l1);
+            atomicMin(&hbox[2], l2);
+            atomicMax(&hbox[3], h0);
+            atomicMax(&hbox[4], h1);
+            atomicMax(&hbox[5], h2);
+        }
+    }
+    __syncthreads();
+    const int H0x = hbox[0], H0y = hbox[1], H0z = hbox[2];
+    const int hx = hbox[3] - H0x + 1, hy = hbox[4] - H0y + 1, hz = hbox[5] - H0z + 1;
+    const long long V = (hx > 0 && hy > 0 && hz > 0) ? (long long)hx * hy * hz : 0;
+    bool staged = V > 0 && V <= (long long)L.stage_cells;
+    const uint2 *table = L.table + S.table_base;
+    const uint32_t dx0 = (uint32_t)g.dims[0], dy0 = (uint32_t)g.dims[1];
+
+    uint32_t total = 0;
+    if (staged) {
+        const uint32_t nv = (uint32_t)V;
+        for (uint32_t c = threadIdx.x; c < nv; c += kSeeThreads) {
+            uint32_t x = c % (uint32_t)hx, yz = c / (uint32_t)hx;
+            uint32_t y = yz % (uint32_t)hy, z = yz / (uint32_t)hy;
+            uint2 e = table[((uint32_t)(H0z + (int)z) * dy0 + (uint32_t)(H0y + (int)y)) * dx0 + (uint32_t)(H0x + (int)x)];
+            cell_first[c] = e.x;
+            cell_off[c] = e.y - e.x;
+        }
+        __syncthreads();
+        // exclusive scan of the cell counts: each thread scans a contiguous chunk
+        const uint32_t per = (nv + kSeeThreads - 1) / kSeeThreads;
+        const uint32_t c0 = threadIdx.x * per;
+        const uint32_t c1 = min(c0 + per, nv);
+        uint32_t sum = 0;
+        for (uint32_t c = c0; c < c1; ++c) sum += cell_off[c];
+        uint32_t incl = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t w = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int)lane >= o) incl += w;
+        }
+        if (lane == 31) warp_sums[threadIdx.x >> 5] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t run = 0;
+            for (int w = 0; w < kSeeThreads / 32; ++w) {
+                uint32_t t = warp_sums[w];
+                warp_sums[w] = run;
+                run += t;
+            }
+            s_total = run;
+        }
+        __syncthreads();
+        uint32_t run = warp_sums[threadIdx.x >> 5] + incl - sum;
+        for (uint32_t c = c0; c < c1; ++c) {
+            uint32_t t = cell_off[c];
+            cell_off[c] = run;
+            run += t;
+        }
+        if (threadIdx.x == 0) cell_off[nv] = s_total;
+        total = s_total;
+        staged = total <= L.stage_cap;
+        __syncthreads();
+        if (staged) {
+            for (uint32_t j = threadIdx.x; j < total; j += kSeeThreads) {
+                // last cell whose offset is <= j
+                uint32_t a = 0, b = nv;
+                while (b - a > 1) {
+                    uint32_t m = (a + b) >> 1;
+                    if (cell_off[m] <= j) a = m; else b = m;
+                }
+                const uint32_t src = cell_first[a] + (j - cell_off[a]);
+#pragma unroll
+                for (int k = 0; k < P::kSeenF4; ++k) stage[(uint32_t)k * L.stage_cap + j] = __ldg(L.io.in_f4[P::seen_stream(k)] + src);
+            }
+            __syncthreads();
+        }
+    }
+
+    // per-warp union of the seers' cell boxes
+    const int wl0 = warp_min_i(lo[0]), wl1 = warp_min_i(lo[1]), wl2 = warp_min_i(lo[2]);
+    const int wh0 = warp_max_i(hi[0]), wh1 = warp_max_i(hi[1]), wh2 = warp_max_i(hi[2]);
+    uint32_t pairs = 0;
+    if (wl0 <= wh0) {
+        if (staged) {
+            uint32_t self_slot = 0xFFFFFFFFu;
+            if (active && L.skip_self) {
+                int cx = cell_coord(sp.x, g.origin[0], g.inv_cs[0], g.dims[0]) - H0x;
+                int cy = cell_coord(sp.y, g.origin[1], g.inv_cs[1], g.dims[1]) - H0y;
+                int cz = cell_coord(sp.z, g.origin[2], g.inv_cs[2], g.dims[2]) - H0z;
+                if (cx >= 0 && cx < hx && cy >= 0 && cy < hy && cz >= 0 && cz < hz) {
+                    uint32_t c = ((uint32_t)cz * (uint32_t)hy + (uint32_t)cy) * (uint32_t)hx + (uint32_t)cx;
+                    self_slot = cell_off[c] + (i - cell_first[c]);
+                }
+            }
+            const SmemSeen acc{stage, L.stage_cap};
+            for (int z = wl2; z <= wh2; ++z)
+                for (int y = wl1; y <= wh1; ++y) {
+                    const uint32_t row = ((uint32_t)(z - H0z) * (uint32_t)hy + (uint32_t)(y - H0y)) * (uint32_t)hx;
+                    const uint32_t j0 = cell_off[row + (uint32_t)(wl0 - H0x)];
+                    const uint32_t j1 = cell_off[row + (uint32_t)(wh0 - H0x) + 1];
+#pragma unroll 4
+                    for (uint32_t j = j0; j < j1; ++j) {
+                        const float4 bp = stage[j];
+                        if (active && j != self_slot && box_hit(sp, bp, r4)) {
+                            ++pairs;
+                            P::see(s, sp, bp, acc, j, sctx);
+                        }
+                    }
+                }
+        } else {
+            GlobalSeen<P::kSeenF4> acc;
+#pragma unroll
+            for (int k = 0; k < P::kSeenF4; ++k) acc.s[k] = L.io.in_f4[P::seen_stream(k)];
+            const float4 *pos = L.io.in_f4[0];
+            const uint32_t self = (active && L.skip_self) ? i : 0xFFFFFFFFu;
+            for (int z = wl2; z <= wh2; ++z)
+                for (int y = wl1; y <= wh1; ++y)
+                    for (int x = wl0; x <= wh0; ++x) {
+                        const uint2 e = table[((uint32_t)z * dy0 + (uint32_t)y) * dx0 + (uint32_t)x];
+                        for (uint32_t b = e.x; b < e.y; ++b) {
+                            const float4 bp = __ldg(pos + b);
+                            if (active && b != self && box_hit(sp, bp, r4)) {
+                                ++pairs;
+                                P::see(s, sp, bp, acc, b, sctx);
+                            }
+                        }
+                    }
+        }
+    }
+    if (active) P::finish(s, sp, L.io, i, sctx, actx);
+    if (L.pairs) {
+        uint32_t w = warp_sum_u(pairs);
+        if (lane == 0 && w) atomicAdd(L.pairs, (unsigned long long)w);
+    }
+}
+
+template <class A>
+__global__ void __launch_bounds__(kSortThreads) act_kernel(ActLaunch L) {
+    const uint32_t seg = L.tile_seg[blockIdx.x];
+    const SegmentSpec S = L.specs[seg];
+    const typename A::ActCtx &actx = *reinterpret_cast<const typename A::ActCtx *>(L.ctx + (size_t)seg * L.ctx_stride);
+    const uint32_t t = blockIdx.x - S.tile_begin;
+    const uint32_t beg = S.begin + t * kSortTile;
+    const uint32_t end = min(beg + (uint32_t)kSortTile, S.begin + S.count);
+    for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads) A::act(L.io, i, actx);
+}
+
+// AoS <-> SoA conversion for push and fetch (replaces the OpenCL path's whole-buffer
+// copies, tay/ocl.c:238-272).  `aos` is the record array in device memory.
+template <class M>
+__global__ void __launch_bounds__(256) pack_kernel(const uint32_t *__restrict__ aos, uint32_t n, PassIO io) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) M::pack(aos + (size_t)i * (M::kAgentBytes / 4), io, i);
+}
+
+template <class M>
+__global__ void __launch_bounds__(256) unpack_kernel(uint32_t *__restrict__ aos, uint32_t n, PassIO io,
+                                                     uint32_t program) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) M::unpack(aos + (size_t)i * (M::kAgentBytes / 4), io, i, program);
+}
+
+}  // namespace tgpu

@@ -1,0 +1,407 @@
+// Z-grid sort for a batch of segments: bounding box, Morton cell keys, a stable LSD radix
+// sort of the keys (8-bit digits), the dense cell table, and the reorder of the
+// structure-of-arrays streams into cell order.
+//
+// Replaces, for the GPU Z-grid, the reference's serial counting sort
+// (tay/cpu_z_grid.c:156-221: count per cell, exclusive scan over every cell, memcpy of
+// each AoS agent) and its OpenCL twin (tay/ocl_grid.c:43-209, whose order within a cell
+// is not deterministic).  Here the order is deterministic and stable: agents in the
+// same cell keep their previous relative order, as the reference's CPU sort does.
+#include "tgpu_internal.cuh"
+#include "tgpu_kernels.cuh"
+
+namespace tgpu {
+
+namespace {
+
+TGPU_D uint32_t lane_id() { return threadIdx.x & 31u; }
+
+template <typename T>
+TGPU_D T warp_min(T v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        T w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w < v ? w : v;
+    }
+    return v;
+}
+template <typename T>
+TGPU_D T warp_max(T v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        T w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+TGPU_D uint32_t warp_incl_scan(uint32_t v) {
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t w = __shfl_up_sync(0xffffffffu, v, o);
+        if ((int)lane_id() >= o) v += w;
+    }
+    return v;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ bounding box
+
+__global__ void __launch_bounds__(kSortThreads) bbox_kernel(const SegmentSpec *__restrict__ specs,
+                                                            const uint32_t *__restrict__ tile_seg,
+                                                            const float4 *__restrict__ pos, BoxAcc *box) {
+    const uint32_t seg = tile_seg[blockIdx.x];
+    const SegmentSpec s = specs[seg];
+    if (s.fixed_box) return;
+    const uint32_t t = blockIdx.x - s.tile_begin;
+    const uint32_t beg = s.begin + t * kSortTile;
+    const uint32_t end = min(beg + (uint32_t)kSortTile, s.begin + s.count);
+    uint32_t lo[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+    uint32_t hi[3] = {0u, 0u, 0u};
+    for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads) {
+        float4 p = pos[i];
+        float c[3] = {p.x, p.y, p.z};
+        for (int a = 0; a < 3; ++a) {
+            uint32_t o = float_to_ordered(c[a]);
+            lo[a] = min(lo[a], o);
+            hi[a] = max(hi[a], o);
+        }
+    }
+    __shared__ uint32_t red[6][kSortThreads / 32];
+    for (int a = 0; a < 3; ++a) {
+        uint32_t l = warp_min(lo[a]);
+        uint32_t h = warp_max(hi[a]);
+        if (lane_id() == 0) {
+            red[a][threadIdx.x >> 5] = l;
+            red[3 + a][threadIdx.x >> 5] = h;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        for (int a = 0; a < 3; ++a) {
+            uint32_t l = threadIdx.x < kSortThreads / 32 ? red[a][threadIdx.x] : 0xFFFFFFFFu;
+            uint32_t h = threadIdx.x < kSortThreads / 32 ? red[3 + a][threadIdx.x] : 0u;
+            l = warp_min(l);
+            h = warp_max(h);
+            if (threadIdx.x == 0) {
+                atomicMin(&box[seg].lo[a], l);
+                atomicMax(&box[seg].hi[a], h);
+            }
+        }
+    }
+}
+
+__global__ void box_reset_kernel(BoxAcc *box, uint32_t segments) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= segments) return;
+    for (int a = 0; a < 3; ++a) {
+        box[s].lo[a] = 0xFFFFFFFFu;
+        box[s].hi[a] = 0u;
+    }
+}
+
+// ------------------------------------------------------------------ keys + first histogram
+
+// counts layout: segment-major, then digit, then tile within the segment, so that one
+// exclusive scan over the whole array yields absolute output positions
+// (segments are packed: begin(s) = sum of the counts before s).
+TGPU_D uint32_t count_index(const SegmentSpec &s, uint32_t digit, uint32_t local_tile) {
+    return 256u * s.tile_begin + digit * s.tile_count + local_tile;
+}
+
+__global__ void __launch_bounds__(kSortThreads) key_histogram_kernel(const SegmentSpec *__restrict__ specs,
+                                                                     const uint32_t *__restrict__ tile_seg,
+                                                                     const BoxAcc *__restrict__ box,
+                                                                     const float4 *__restrict__ pos,
+                                                                     uint32_t *__restrict__ keys,
+                                                                     uint32_t *__restrict__ counts, uint32_t mask) {
+    __shared__ uint32_t hist[256];
+    const uint32_t seg = tile_seg[blockIdx.x];
+    const SegmentSpec s = specs[seg];
+    const Grid g = segment_grid(s, box[seg]);
+    const uint32_t t = blockIdx.x - s.tile_begin;
+    const uint32_t beg = s.begin + t * kSortTile;
+    const uint32_t end = min(beg + (uint32_t)kSortTile, s.begin + s.count);
+    hist[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads) {
+        float4 p = pos[i];
+        uint32_t cx = (uint32_t)cell_coord(p.x, g.origin[0], g.inv_cs[0], g.dims[0]);
+        uint32_t cy = (uint32_t)cell_coord(p.y, g.origin[1], g.inv_cs[1], g.dims[1]);
+        uint32_t cz = (uint32_t)cell_coord(p.z, g.origin[2], g.inv_cs[2], g.dims[2]);
+        uint32_t k = morton3(cx, cy, cz);
+        keys[i] = k;
+        atomicAdd(&hist[k & mask], 1u);
+    }
+    __syncthreads();
+    counts[count_index(s, threadIdx.x, t)] = hist[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kSortThreads) digit_histogram_kernel(const SegmentSpec *__restrict__ specs,
+                                                                       const uint32_t *__restrict__ tile_seg,
+                                                                       const uint32_t *__restrict__ keys,
+                                                                       uint32_t *__restrict__ counts, int shift,
+                                                                       uint32_t mask) {
+    __shared__ uint32_t hist[256];
+    const uint32_t seg = tile_seg[blockIdx.x];
+    const SegmentSpec s = specs[seg];
+    const uint32_t t = blockIdx.x - s.tile_begin;
+    const uint32_t beg = s.begin + t * kSortTile;
+    const uint32_t end = min(beg + (uint32_t)kSortTile, s.begin + s.count);
+    hist[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads)
+        atomicAdd(&hist[(keys[i] >> shift) & mask], 1u);
+    __syncthreads();
+    counts[count_index(s, threadIdx.x, t)] = hist[threadIdx.x];
+}
+
+// ------------------------------------------------------------------ device-wide exclusive scan
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanChunk = kScanThreads * kScanItems;
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive prefix and
+// writes the block total.
+TGPU_D uint32_t block_excl_scan(uint32_t v, uint32_t *warp_sums, uint32_t *total) {
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    const uint32_t nwarps = blockDim.x >> 5;
+    uint32_t incl = warp_incl_scan(v);
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < nwarps ? warp_sums[lane] : 0u;
+        uint32_t wi = warp_incl_scan(w);
+        if (lane < nwarps) warp_sums[lane] = wi - w;
+        if (lane == 31) *total = wi;
+    }
+    __syncthreads();
+    uint32_t r = warp_sums[warp] + incl - v;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const uint32_t *__restrict__ data,
+                                                                   uint32_t *__restrict__ partials, uint32_t n) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t total;
+    const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * kScanItems;
+    uint32_t sum = 0;
+    for (int k = 0; k < kScanItems; ++k)
+        if (base + k < n) sum += data[base + k];
+    block_excl_scan(sum, warp_sums, &total);
+    if (threadIdx.x == 0) partials[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_spine_kernel(uint32_t *__restrict__ partials, uint32_t n) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t total;
+    const uint32_t base = threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t sum = 0;
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = base + k < n ? partials[base + k] : 0u;
+        sum += v[k];
+    }
+    uint32_t run = block_excl_scan(sum, warp_sums, &total);
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) partials[base + k] = run;
+        run += v[k];
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(uint32_t *__restrict__ data,
+                                                                  const uint32_t *__restrict__ partials, uint32_t n) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t total;
+    const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t sum = 0;
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = base + k < n ? data[base + k] : 0u;
+        sum += v[k];
+    }
+    uint32_t run = block_excl_scan(sum, warp_sums, &total) + partials[blockIdx.x];
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) data[base + k] = run;
+        run += v[k];
+    }
+}
+
+// ------------------------------------------------------------------ stable scatter
+
+// One tile per block: 8 warps, each warp owns 256 consecutive items and walks them in 8
+// rounds of 32, so (warp, round, lane) is the item order.  Ranks within a round come
+// from __match_any_sync; per-warp running counts per digit live in shared memory; a
+// per-digit prefix over warps and the scanned global counts give each item its output
+// slot.  Items with equal digits therefore keep their input order (stable).
+__global__ void __launch_bounds__(kSortThreads) scatter_kernel(const SegmentSpec *__restrict__ specs,
+                                                               const uint32_t *__restrict__ tile_seg,
+                                                               const uint32_t *__restrict__ keys_in,
+                                                               const uint32_t *__restrict__ vals_in,
+                                                               uint32_t *__restrict__ keys_out,
+                                                               uint32_t *__restrict__ vals_out,
+                                                               const uint32_t *__restrict__ offsets, int shift,
+                                                               uint32_t mask) {
+    constexpr int kWarps = kSortThreads / 32;
+    constexpr int kRounds = kSortTile / kSortThreads;
+    __shared__ uint32_t warp_hist[kWarps][256];
+    __shared__ uint32_t digit_base[256];
+    const uint32_t seg = tile_seg[blockIdx.x];
+    const SegmentSpec s = specs[seg];
+    const uint32_t t = blockIdx.x - s.tile_begin;
+    const uint32_t beg = s.begin + t * kSortTile;
+    const uint32_t end = min(beg + (uint32_t)kSortTile, s.begin + s.count);
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+
+    for (int i = threadIdx.x; i < kWarps * 256; i += kSortThreads) (&warp_hist[0][0])[i] = 0;
+    digit_base[threadIdx.x] = offsets[count_index(s, threadIdx.x, t)];
+    __syncthreads();
+
+    uint32_t key[kRounds], val[kRounds], rank[kRounds], dig[kRounds];
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+        const uint32_t i = beg + warp * (kSortTile / kWarps) + r * 32 + lane;
+        const bool valid = i < end;
+        const uint32_t k = valid ? keys_in[i] : 0u;
+        const uint32_t d = valid ? ((k >> shift) & mask) : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t below = __popc(peers & ((1u << lane) - 1u));
+        const uint32_t before = valid ? warp_hist[warp][d] : 0u;
+        __syncwarp();
+        if (valid && below == 0) warp_hist[warp][d] = before + __popc(peers);
+        __syncwarp();
+        key[r] = k;
+        val[r] = valid ? (vals_in ? vals_in[i] : i) : 0u;
+        rank[r] = before + below;
+        dig[r] = d;
+    }
+    __syncthreads();
+    {
+        uint32_t run = 0;
+        for (int w = 0; w < kWarps; ++w) {
+            uint32_t c = warp_hist[w][threadIdx.x];
+            warp_hist[w][threadIdx.x] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+        if (dig[r] < 256u) {
+            const uint32_t p = digit_base[dig[r]] + warp_hist[warp][dig[r]] + rank[r];
+            keys_out[p] = key[r];
+            vals_out[p] = val[r];
+        }
+    }
+}
+
+// ------------------------------------------------------------------ cell table
+
+TGPU_D uint32_t table_index(const Grid &g, uint32_t key) {
+    uint32_t x = compact10(key), y = compact10(key >> 1), z = compact10(key >> 2);
+    return (z * (uint32_t)g.dims[1] + y) * (uint32_t)g.dims[0] + x;
+}
+
+// Records {first, end} of every run of equal keys at the run's cell (write_runs = 1), or
+// clears those entries again (write_runs = 0) before the next sort.
+__global__ void __launch_bounds__(kSortThreads) cell_table_kernel(const SegmentSpec *__restrict__ specs,
+                                                                  const uint32_t *__restrict__ tile_seg,
+                                                                  const BoxAcc *__restrict__ box,
+                                                                  const uint32_t *__restrict__ keys,
+                                                                  uint2 *__restrict__ table, int write_runs) {
+    const uint32_t seg = tile_seg[blockIdx.x];
+    const SegmentSpec s = specs[seg];
+    const Grid g = segment_grid(s, box[seg]);
+    const uint32_t t = blockIdx.x - s.tile_begin;
+    const uint32_t beg = s.begin + t * kSortTile;
+    const uint32_t seg_end = s.begin + s.count;
+    const uint32_t end = min(beg + (uint32_t)kSortTile, seg_end);
+    for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads) {
+        const uint32_t k = keys[i];
+        const bool first = (i == s.begin) || keys[i - 1] != k;
+        const bool last = (i + 1 == seg_end) || keys[i + 1] != k;
+        if (!first && !last) continue;
+        uint2 *e = table + s.table_base + table_index(g, k);
+        if (write_runs) {
+            if (first) e->x = i;
+            if (last) e->y = i + 1;
+        } else if (first) {
+            *e = make_uint2(0u, 0u);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ reorder
+
+__global__ void __launch_bounds__(256) gather_kernel(uint32_t n, const uint32_t *__restrict__ perm, GatherSet set) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t src = perm[i];
+#pragma unroll
+    for (int c = 0; c < kMaxF4; ++c)
+        if (c < set.nf4) set.dst_f4[c][i] = __ldg(set.src_f4[c] + src);
+#pragma unroll
+    for (int c = 0; c < kMaxU32; ++c)
+        if (c < set.nu32) set.dst_u32[c][i] = __ldg(set.src_u32[c] + src);
+}
+
+// ------------------------------------------------------------------ host-side launchers
+
+void launch_box(const SortLaunch &L, cudaStream_t st) {
+    box_reset_kernel<<<(L.segments + 127) / 128, 128, 0, st>>>(L.box, L.segments);
+    bbox_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.pos, L.box);
+}
+
+static void launch_scan(const SortLaunch &L, cudaStream_t st) {
+    const uint32_t n = 256u * L.tiles;
+    const uint32_t blocks = (n + kScanChunk - 1) / kScanChunk;
+    scan_reduce_kernel<<<blocks, kScanThreads, 0, st>>>(L.counts, L.partials, n);
+    scan_spine_kernel<<<1, kScanThreads, 0, st>>>(L.partials, blocks);
+    scan_apply_kernel<<<blocks, kScanThreads, 0, st>>>(L.counts, L.partials, n);
+}
+
+// Sorts the keys of every segment; on return *sorted_keys / *perm point at the buffers
+// holding the sorted keys and the permutation (sorted slot -> previous slot).
+void launch_sort(const SortLaunch &L, cudaStream_t st, uint32_t **sorted_keys, uint32_t **perm) {
+    uint32_t *kin = L.keys[0], *kout = L.keys[1];
+    uint32_t *vin = nullptr, *vout = L.vals[1];
+    const int passes = (int)((L.key_bits + 7) / 8);
+    for (int p = 0; p < passes; ++p) {
+        const int shift = 8 * p;
+        const int bits = min(8, (int)L.key_bits - shift);
+        const uint32_t mask = (1u << bits) - 1u;
+        if (p == 0)
+            key_histogram_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.box, L.pos, kin, L.counts,
+                                                                   mask);
+        else
+            digit_histogram_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, kin, L.counts, shift, mask);
+        launch_scan(L, st);
+        scatter_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, kin, vin, kout, vout, L.counts, shift,
+                                                         mask);
+        // ping-pong: the next pass reads what this one wrote
+        uint32_t *tk = kin;
+        kin = kout;
+        kout = tk;
+        if (p == 0) {
+            vin = vout;
+            vout = L.vals[0];
+        } else {
+            uint32_t *tv = vin;
+            vin = vout;
+            vout = tv;
+        }
+    }
+    *sorted_keys = kin;
+    *perm = vin;
+}
+
+void launch_cell_table(const SortLaunch &L, const uint32_t *sorted_keys, int write_runs, cudaStream_t st) {
+    cell_table_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.box, sorted_keys, L.table, write_runs);
+}
+
+void launch_gather(uint32_t n, const uint32_t *perm, const GatherSet &set, cudaStream_t st) {
+    if (n == 0) return;
+    gather_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, perm, set);
+}
+
+}  // namespace tgpu

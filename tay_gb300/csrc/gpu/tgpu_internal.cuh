@@ -1,0 +1,180 @@
+// Internal definitions shared by the GB300 Z-grid kernels.
+//
+// Data layout in HBM (one "arena" per batch of segments; a plain tay_run is a batch of
+// one segment):
+//   * agents of all segments are concatenated; segment s owns [begin, begin + count);
+//   * every agent field lives in a structure-of-arrays stream: float4 streams (16 B per
+//     agent, coalesced 16-byte loads) and u32 streams;
+//   * state streams are double-buffered ("cur" / "alt"): the sort gathers them into
+//     cell order, a fused see+act pass writes the fields it changes into the other copy;
+//   * per-step streams (accumulators, density/pressure) are single-buffered and valid
+//     only inside one step;
+//   * a dense cell table (uint2 {first, end} per cell, row-major over the segment's grid)
+//     per segment, written only at non-empty cells after each sort and cleared the same
+//     way before the next one (the reference clears its table per step too,
+//     tay/cpu_z_grid.c:223-225).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define TGPU_HD __host__ __device__ __forceinline__
+#define TGPU_D __device__ __forceinline__
+
+namespace tgpu {
+
+constexpr int kMaxF4 = 6;   // float4 streams per model
+constexpr int kMaxU32 = 2;  // u32 streams per model
+constexpr int kSortTile = 2048;       // agents per radix tile (256 threads x 8)
+constexpr int kSortThreads = 256;
+constexpr int kSeeThreads = 128;      // seers per see CTA
+
+// Static per-segment description, written by the host once per run.
+struct SegmentSpec {
+    uint32_t begin;          // first agent (index into the concatenated streams)
+    uint32_t count;          // agents in this segment
+    uint32_t table_base;     // first entry of this segment's dense cell table
+    uint32_t table_cap;      // entries available to it
+    uint32_t tile_begin;     // first radix tile of this segment
+    uint32_t tile_count;     // radix tiles of this segment
+    uint32_t axis_cells_max; // power of two, <= 1024: bounds each grid axis (key bits)
+    uint32_t fixed_box;      // 1: use box_min/box_max instead of the agents' bounding box
+    float part[3];           // minimum cell edge per axis
+    float reach[3];          // largest see radius per axis over the segment's see passes
+    float box_min[3];        // fixed space box (tay_fix_space_box)
+    float box_max[3];
+};
+
+// Per-step grid, derived on the device from the bounding box.  Every kernel derives
+// it with the same function from the same inputs, so all kernels agree bit for bit.
+struct Grid {
+    float origin[3];
+    float inv_cs[3];
+    float cs[3];
+    int dims[3];
+};
+
+// Bounding box accumulator: order-preserving u32 encodings so that atomicMin/atomicMax
+// on unsigned integers order floats correctly.
+struct BoxAcc {
+    uint32_t lo[3];
+    uint32_t hi[3];
+};
+
+TGPU_HD uint32_t float_to_ordered(float f) {
+#ifdef __CUDA_ARCH__
+    uint32_t b = __float_as_uint(f);
+#else
+    union { float f; uint32_t u; } cvt;
+    cvt.f = f;
+    uint32_t b = cvt.u;
+#endif
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+TGPU_HD float ordered_to_float(uint32_t o) {
+    uint32_t b = (o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o;
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(b);
+#else
+    union { float f; uint32_t u; } cvt;
+    cvt.u = b;
+    return cvt.f;
+#endif
+}
+
+// Grid rule (GPU Z-grid): cells of edge >= part (the requested minimum part size, as in
+// tay_configure_space), covering [min, max] of the box; each axis at most
+// axis_cells_max cells and the whole grid at most table_cap cells, enlarging the cells
+// when either bound would be exceeded (the reference shrinks its grid to its memory in
+// the same spirit, tay/cpu_z_grid.c:175-176, tay/cpu_grid.c:95-106).
+TGPU_HD int clamp_cells(float cells, uint32_t axis_max) {
+    // NaN and values below 1 give one cell; never more than axis_max
+    if (!(cells >= 1.0f)) return 1;
+    if (cells > (float)axis_max) return (int)axis_max;
+    return (int)cells;
+}
+
+TGPU_HD Grid derive_grid(const SegmentSpec &s, const float *mn, const float *mx) {
+    Grid g;
+    float cs[3], ext[3];
+    int d[3];
+    for (int i = 0; i < 3; ++i) {
+        ext[i] = mx[i] - mn[i];
+        if (!(ext[i] >= 0.0f) || ext[i] > 3.0e38f) ext[i] = 0.0f;
+        cs[i] = s.part[i] > 0.0f ? s.part[i] : 1.0f;
+        float cells = floorf(ext[i] / cs[i]) + 1.0f;
+        if (cells > (float)s.axis_cells_max) cs[i] = ext[i] / ((float)s.axis_cells_max - 0.5f);
+        d[i] = clamp_cells(floorf(ext[i] / cs[i]) + 1.0f, s.axis_cells_max);
+    }
+    for (int iter = 0; iter < 64; ++iter) {
+        unsigned long long total = (unsigned long long)d[0] * (unsigned long long)d[1] * (unsigned long long)d[2];
+        if (total <= s.table_cap) break;
+        for (int i = 0; i < 3; ++i) {
+            cs[i] *= 1.25f;
+            d[i] = clamp_cells(floorf(ext[i] / cs[i]) + 1.0f, s.axis_cells_max);
+        }
+    }
+    if ((unsigned long long)d[0] * (unsigned long long)d[1] * (unsigned long long)d[2] > s.table_cap) {
+        for (int i = 0; i < 3; ++i) {
+            d[i] = 1;
+            cs[i] = ext[i] > cs[i] ? ext[i] : cs[i];
+        }
+    }
+    for (int i = 0; i < 3; ++i) {
+        g.origin[i] = mn[i];
+        g.cs[i] = cs[i];
+        g.inv_cs[i] = 1.0f / cs[i];
+        g.dims[i] = d[i];
+    }
+    return g;
+}
+
+TGPU_HD int cell_coord(float p, float origin, float inv_cs, int dim) {
+    int c = (int)floorf((p - origin) * inv_cs);
+    return c < 0 ? 0 : (c >= dim ? dim - 1 : c);
+}
+
+// 3-D Morton code, 10 bits per axis, x at bit 0 (the reference's key layout,
+// tay/cpu_z_grid.c:57-77, written here with the usual magic-number spread).
+TGPU_HD uint32_t spread10(uint32_t v) {
+    v &= 0x3FFu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+TGPU_HD uint32_t compact10(uint32_t v) {
+    v &= 0x09249249u;
+    v = (v | (v >> 2)) & 0x030C30C3u;
+    v = (v | (v >> 4)) & 0x0300F00Fu;
+    v = (v | (v >> 8)) & 0xFF0000FFu;
+    v = (v | (v >> 16)) & 0x000003FFu;
+    return v;
+}
+
+TGPU_HD uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    return spread10(x) | (spread10(y) << 1) | (spread10(z) << 2);
+}
+
+// The step's grid of a segment: from its fixed box, or from the bounding box of its
+// positions accumulated by the box kernel.
+TGPU_HD Grid segment_grid(const SegmentSpec &s, const BoxAcc &b) {
+    float mn[3], mx[3];
+    for (int i = 0; i < 3; ++i) {
+        mn[i] = s.fixed_box ? s.box_min[i] : ordered_to_float(b.lo[i]);
+        mx[i] = s.fixed_box ? s.box_max[i] : ordered_to_float(b.hi[i]);
+    }
+    return derive_grid(s, mn, mx);
+}
+
+// Device-side error word: kernels never trap; they record the first failure here and
+// the host turns it into TAY_ERROR_CUDA.
+enum DeviceError : uint32_t {
+    kErrNone = 0,
+    kErrTableOverflow = 1,
+};
+
+}  // namespace tgpu

@@ -1,0 +1,74 @@
+// Launch descriptions shared between the sort, see/act kernels and the runtime.
+#pragma once
+
+#include "tgpu_internal.cuh"
+
+namespace tgpu {
+
+// Everything the sort needs for one batch of segments.
+struct SortLaunch {
+    const SegmentSpec *specs;  // [segments]
+    const uint32_t *tile_seg;  // [tiles] segment of each radix tile
+    BoxAcc *box;               // [segments]
+    const float4 *pos;         // positions, current order
+    uint32_t *keys[2];         // [n] ping-pong key buffers
+    uint32_t *vals[2];         // [n] ping-pong permutation buffers
+    uint32_t *counts;          // [256 * tiles]
+    uint32_t *partials;        // [ceil(256 * tiles / 4096)]
+    uint2 *table;              // dense cell tables of all segments
+    uint32_t segments;
+    uint32_t tiles;
+    uint32_t key_bits;
+};
+
+struct GatherSet {
+    const float4 *src_f4[kMaxF4];
+    float4 *dst_f4[kMaxF4];
+    const uint32_t *src_u32[kMaxU32];
+    uint32_t *dst_u32[kMaxU32];
+    int nf4;
+    int nu32;
+};
+
+// Streams seen by a pass kernel.  Index meaning is model-specific; float4 stream 0 is
+// always the position.
+struct PassIO {
+    const float4 *in_f4[kMaxF4];
+    float4 *out_f4[kMaxF4];
+    const uint32_t *in_u32[kMaxU32];
+    uint32_t *out_u32[kMaxU32];
+};
+
+struct SeeLaunch {
+    const SegmentSpec *specs;
+    const BoxAcc *box;
+    const uint2 *table;
+    const uint2 *cta_table;   // per CTA {segment, first seer}
+    const float4 *radii;      // per segment see radii of this pass
+    const char *ctx;          // per segment see context, stride ctx_stride
+    uint32_t ctx_stride;
+    const char *act_ctx;      // per segment context of a fused act pass (or = ctx)
+    uint32_t act_ctx_stride;
+    uint32_t ctas;
+    int skip_self;            // same group and !self_see: a seer never sees itself
+    uint32_t stage_cap;       // staged agents per CTA
+    uint32_t stage_cells;     // halo cells per CTA
+    unsigned long long *pairs;  // box-test passes, summed over the launch
+    PassIO io;
+};
+
+struct ActLaunch {
+    const SegmentSpec *specs;
+    const uint32_t *tile_seg;
+    const char *ctx;
+    uint32_t ctx_stride;
+    uint32_t tiles;
+    PassIO io;
+};
+
+void launch_box(const SortLaunch &L, cudaStream_t st);
+void launch_sort(const SortLaunch &L, cudaStream_t st, uint32_t **sorted_keys, uint32_t **perm);
+void launch_cell_table(const SortLaunch &L, const uint32_t *sorted_keys, int write_runs, cudaStream_t st);
+void launch_gather(uint32_t n, const uint32_t *perm, const GatherSet &set, cudaStream_t st);
+
+}  // namespace tgpu

@@ -1,0 +1,138 @@
+"""Host-side descriptions of the device models: AoS record layouts, contexts, pass lists.
+
+Each model is registered in the library under the func names listed here; a host uses
+them through the plain Tay API (tay_add_see / tay_add_act with these names), exactly as a
+reference host registers its functions for the OpenCL path.
+
+  test_basic  the reference's test agent (test/agent.h:2-19, test/agent.c:2-55):
+              passes agent_see (self_see FALSE), agent_act
+  boids       separation / alignment / cohesion: boids_see (self_see FALSE), boids_act
+  sph         weakly compressible SPH: sph_density (self_see TRUE), sph_pressure,
+              sph_force (self_see FALSE), sph_integrate
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import api
+
+F4 = ("<f4", 4)
+
+TEST_RECORD = np.dtype([("tag", "<u4", 2), ("p",) + F4, ("v",) + F4, ("b_buffer",) + F4, ("b_buffer_count", "<i4"),
+                        ("f_buffer",) + F4, ("id", "<i4")])
+BOIDS_RECORD = np.dtype([("tag", "<u4", 2), ("p",) + F4, ("v",) + F4, ("coh",) + F4, ("ali",) + F4,
+                         ("sep",) + F4, ("count", "<i4"), ("id", "<i4")])
+SPH_RECORD = np.dtype([("tag", "<u4", 2), ("p",) + F4, ("v",) + F4, ("a",) + F4, ("rho", "<f4"), ("P", "<f4"),
+                       ("id", "<i4"), ("pad", "<i4")])
+assert TEST_RECORD.itemsize == 80 and BOIDS_RECORD.itemsize == 96 and SPH_RECORD.itemsize == 72
+
+
+def records(dtype, p, v):
+    n = p.shape[0]
+    rec = np.zeros(n, dtype)
+    rec["p"] = p
+    rec["v"] = v
+    rec["id"] = np.arange(n, dtype=np.int32)
+    return rec
+
+
+def by_id(rec):
+    """Records reordered by their id field (the reference's result_index idiom)."""
+    out = np.empty_like(rec)
+    out[rec["id"]] = rec
+    return out
+
+
+def test_contexts(radius=50.0, lo=0.0, hi=1000.0):
+    see = np.array([radius, radius, radius, 0.0], np.float32)           # SeeContext {float4 radii}
+    act = np.array([lo, lo, lo, 0.0, hi, hi, hi, 0.0], np.float32)      # ActContext {float4 min, max}
+    return see, act
+
+
+def boids_context(r=10.0, w_sep=1.5, w_ali=1.0, w_coh=1.0, max_speed=2.0, dt=1.0):
+    r = np.float32(r)
+    return np.array([r, r * r, w_sep, w_ali, w_coh, max_speed, dt, 0.0], np.float32)
+
+
+def sph_context(h=0.02, dx=0.01, rho0=1000.0, c0=20.0, alpha=0.05, dt=1e-4, g=(0.0, 0.0, -9.81),
+                tank_min=(0.0, 0.0, 0.0), tank_max=(2.0, 1.5, 0.8)):
+    """Context values computed in float64 and rounded once to float32."""
+    m = rho0 * dx ** 3
+    vals = [h, 1.0 / h, (2.0 * h) ** 2, 1.0 / (np.pi * h ** 3), m, rho0, c0 * c0 * rho0 / 7.0, c0, alpha,
+            0.01 * h * h, dt, *g, *tank_min, *tank_max]
+    return np.array(vals, np.float32)
+
+
+@dataclass
+class Pass:
+    name: str
+    see: bool
+    ctx: np.ndarray
+    radius: float = 0.0
+    self_see: bool = False
+
+
+@dataclass
+class Setup:
+    """A one-group state: record dtype, passes, space parameters."""
+
+    dtype: np.dtype
+    passes: list
+    part: float
+    mb: int = 250
+    fixed_box: tuple | None = None
+    extra: dict = field(default_factory=dict)
+
+
+def test_setup(radius=50.0, part=50.0, passes=("agent_see", "agent_act"), mb=250):
+    see, act = test_contexts(radius)
+    lst = []
+    for p in passes:
+        if p == "agent_see":
+            lst.append(Pass("agent_see", True, see, radius, False))
+        else:
+            lst.append(Pass("agent_act", False, act))
+    return Setup(TEST_RECORD, lst, part, mb)
+
+
+def boids_setup(r=10.0, part=10.0, passes=("boids_see", "boids_act"), mb=250):
+    ctx = boids_context(r)
+    lst = [Pass(p, p == "boids_see", ctx, r, False) for p in passes]
+    return Setup(BOIDS_RECORD, lst, part, mb)
+
+
+def sph_setup(h=0.02, part=None, passes=("sph_density", "sph_pressure", "sph_force", "sph_integrate"), mb=250,
+              **ctx_kw):
+    ctx = sph_context(h=h, **ctx_kw)
+    r = 2.0 * h
+    lst = [Pass(p, p in ("sph_density", "sph_force"), ctx, r, p == "sph_density") for p in passes]
+    return Setup(SPH_RECORD, lst, part if part is not None else r, mb)
+
+
+def make_state(setup: Setup, recs: np.ndarray):
+    """Creates a state with one TAY_GPU_Z_GRID group holding `recs`, passes registered."""
+    st = api.State()
+    g = st.add_group(setup.dtype.itemsize, max(1, recs.shape[0]), True)
+    st.configure_space(g, api.TAY_GPU_Z_GRID, 3, api.f4(setup.part), setup.mb)
+    if setup.fixed_box is not None:
+        st.fix_space_box(g, api.f4(*setup.fixed_box[0]), api.f4(*setup.fixed_box[1]))
+    for p in setup.passes:
+        if p.see:
+            st.add_see(g, g, p.name, api.f4(p.radius, p.radius, p.radius, p.radius), p.self_see, p.ctx)
+        else:
+            st.add_act(g, p.name, p.ctx)
+    st.commit(g, recs)
+    return st, g
+
+
+def run(setup: Setup, recs: np.ndarray, steps: int):
+    """Runs `steps` steps through the C API; returns the records ordered by id."""
+    st, g = make_state(setup, recs)
+    st.start()
+    st.run(steps)
+    out = by_id(st.agents(g, setup.dtype))
+    st.end()
+    st.close()
+    return out

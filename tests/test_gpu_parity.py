@@ -1,0 +1,107 @@
+"""GPU parity: the CUDA Z-grid path (through the Tay C API) against the oracle, on the same
+seeded records.  Counts are compared bit for bit; floats with a normwise relative error
+bound (max |gpu - oracle| / max |oracle|): 1e-5 after one step, 1e-3 after many."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from tay_gb300 import api
+from tay_gb300 import models as M
+from tay_gb300 import workloads as W
+
+from parity import normwise, oracle_run
+
+pytestmark = pytest.mark.gpu
+
+TOL_1STEP = 1e-5
+TOL_MANY = 1e-3
+
+
+def _basic(n, seed=11):
+    ps = W.basic_points(n, seed=seed)
+    return M.records(M.TEST_RECORD, ps.p, ps.v)
+
+
+def test_basic_counts_bit_exact_one_step(gpu, port):
+    recs = _basic(20000)
+    setup = M.test_setup(passes=("agent_see",))
+    g = M.run(setup, recs, 1)
+    o = oracle_run(port, O.MODEL_TEST, setup, recs, 1)
+    assert g["b_buffer_count"].sum() > 0
+    assert np.array_equal(g["b_buffer_count"], o["b_buffer_count"])
+    assert normwise(g["b_buffer"][:, :3], o["b_buffer"][:, :3]) < TOL_1STEP
+    assert np.array_equal(g["p"], o["p"]) and np.array_equal(g["v"], o["v"])
+
+
+def test_basic_counts_match_cpu_simple(gpu, port):
+    recs = _basic(4000, seed=3)
+    setup = M.test_setup(passes=("agent_see",))
+    g = M.run(setup, recs, 1)
+    o = oracle_run(port, O.MODEL_TEST, setup, recs, 1, space="simple")
+    assert np.array_equal(g["b_buffer_count"], o["b_buffer_count"])
+
+
+def test_basic_steps(gpu, port):
+    recs = _basic(20000, seed=5)
+    setup = M.test_setup()
+    g = M.run(setup, recs, 20)
+    o = oracle_run(port, O.MODEL_TEST, setup, recs, 20)
+    # positions and velocities do not depend on the see pass: bit-exact
+    assert np.array_equal(g["p"][:, :3], o["p"][:, :3])
+    assert np.array_equal(g["v"][:, :3], o["v"][:, :3])
+    assert np.array_equal(g["b_buffer_count"], o["b_buffer_count"])
+    assert normwise(g["f_buffer"][:, :3], o["f_buffer"][:, :3]) < TOL_MANY
+
+
+def test_boids_one_step(gpu, port):
+    ps = W.boids_points(30000, seed=7, clusters=8, side=400.0)
+    recs = M.records(M.BOIDS_RECORD, ps.p, ps.v)
+    setup = M.boids_setup(passes=("boids_see",))
+    g = M.run(setup, recs, 1)
+    o = oracle_run(port, O.MODEL_BOIDS, setup, recs, 1)
+    assert g["count"].sum() > 0
+    assert np.array_equal(g["count"], o["count"])
+    for f in ("coh", "ali", "sep"):
+        assert normwise(g[f][:, :3], o[f][:, :3]) < TOL_1STEP, f
+    full = M.boids_setup()
+    g = M.run(full, recs, 1)
+    o = oracle_run(port, O.MODEL_BOIDS, full, recs, 1)
+    assert normwise(g["p"][:, :3], o["p"][:, :3]) < TOL_1STEP
+    assert normwise(g["v"][:, :3], o["v"][:, :3]) < TOL_1STEP
+    assert np.all(g["count"] == 0)
+
+
+def test_sph_one_step(gpu, port):
+    sph = W.sph_dam(16, 24, 16)
+    recs = M.records(M.SPH_RECORD, sph.points.p, sph.points.v)
+    for passes in (("sph_density",), ("sph_density", "sph_pressure", "sph_force")):
+        setup = M.sph_setup(passes=passes)
+        g = M.run(setup, recs, 1)
+        o = oracle_run(port, O.MODEL_SPH, setup, recs, 1)
+        assert normwise(g["rho"], o["rho"]) < TOL_1STEP
+        if "sph_force" in passes:
+            assert normwise(g["P"], o["P"]) < 1e-4
+            assert normwise(g["a"][:, :3], o["a"][:, :3]) < 1e-3
+    setup = M.sph_setup()
+    g = M.run(setup, recs, 5)
+    o = oracle_run(port, O.MODEL_SPH, setup, recs, 5)
+    assert normwise(g["p"][:, :3], o["p"][:, :3]) < TOL_1STEP
+    assert normwise(g["v"][:, :3], o["v"][:, :3]) < TOL_MANY
+
+
+def test_batch_matches_individual_runs(gpu):
+    setups, recs_list = [], []
+    for i, n in enumerate((1500, 4000, 2500)):
+        ps = W.boids_points(n, seed=20 + i, clusters=2, side=100.0)
+        recs_list.append(M.records(M.BOIDS_RECORD, ps.p, ps.v))
+        setups.append(M.boids_setup(r=5.0 + 3 * i, part=5.0 + 3 * i, mb=4))
+    singles = [M.run(s, r, 3) for s, r in zip(setups, recs_list)]
+    states = [M.make_state(s, r) for s, r in zip(setups, recs_list)]
+    for st, _ in states:
+        st.start()
+    api.run_batch([st for st, _ in states], 3)
+    for (st, g), single in zip(states, singles):
+        out = M.by_id(st.agents(g, M.BOIDS_RECORD))
+        assert np.array_equal(out["p"], single["p"])
+        assert np.array_equal(out["v"], single["v"])
+        st.end()
