@@ -1,0 +1,324 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Z-grid step on the 1M-boid workload.
+
+Workload: 1,048,576 FP32 boids, 64 Gaussian clusters (sigma 40) with centres uniform in a
+cube of side 2000, velocity = unit random direction x speed U[1, 2]; see radius 10,
+separation/alignment/cohesion weights 1.5/1.0/1.0, max speed 2, dt 1; Z-grid with minimum
+cell size 10 (seeded synthetic data: SplitMix64, seed 2).
+
+One step = sort (keys, radix passes, cell table, reorder) + the fused see+act pass.
+  value   pair-interactions/s with the agents resident in HBM: pairs that passed the box
+          test (device counter) / device time of the timed steps (CUDA events on the
+          engine's stream), L2 flushed between steps;
+  e2e     the same metric through the Tay C API with host buffers: each step is
+          tay_run(state, 1), which copies the AoS records host->device, runs the step and
+          copies them back (the OpenCL path's push/fetch per run, tay/state.c:208-315);
+  roofline  of the dominant kernel (the fused see+act pass), from a profiled leg with
+          CUDA events around every kernel class on the engine's stream.
+--impl reference times the CPU implementation of the same step (the oracle restatement
+of the reference's CpuZGrid, all host threads) on the same workload.
+
+Multi-GPU: the step does not shard (one state = one GPU); N ranks run N independent
+replicas ("replicas only"), and value = pairs of all ranks / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_BOIDS = 1 << 20
+RADIUS = 10.0
+CELL = 10.0
+SEED = 2
+BOIDS_RECORD_BYTES = 104
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=3, help="steps of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        import torch
+
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if self.world == 1:
+            return x
+        import torch
+
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-f", self.path], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 7:
+                    continue
+                try:
+                    sm.append(float(parts[0]))
+                    mx.append(float(parts[1]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[3:7]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload():
+    from tay_gb300 import models as M
+    from tay_gb300 import workloads as W
+
+    ps = W.boids_points(N_BOIDS, seed=SEED)
+    recs = M.records(M.BOIDS_RECORD, ps.p, ps.v)
+    setup = M.boids_setup(r=RADIUS, part=CELL, mb=256)
+    return setup, recs
+
+
+CONFIG = {"workload": "boids_1M_zgrid", "agents": N_BOIDS, "radius": RADIUS, "cell": CELL,
+          "clusters": 64, "sigma": 40.0, "side": 2000.0, "weights": [1.5, 1.0, 1.0], "max_speed": 2.0, "dt": 1.0,
+          "passes": ["boids_see", "boids_act"], "seed": SEED}
+
+
+def cpu_baseline(setup, recs, steps):
+    """Oracle restatement of the reference CpuZGrid step, all host threads, `steps` steps."""
+    from oracle import pyoracle as O
+
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    r = O.port().run(O.MODEL_BOIDS, "z_grid", recs, setup.passes[0].ctx, setup.passes[0].ctx, RADIUS, CELL, steps,
+                     O.PASS_SEE0 | O.PASS_ACT0, threads=threads, mb=setup.mb)
+    wall = time.perf_counter() - t0
+    secs = r.ms_per_step * steps / 1000.0
+    return {"value": r.pairs / secs, "unit": "pair-interactions/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} full steps of the 1M-boid workload on CpuZGrid (oracle restatement, {threads} threads)",
+            "ms_per_step": r.ms_per_step, "pairs_per_step": r.pairs / steps, "wall_s": round(wall, 2)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    setup, recs = workload()
+    for _ in range(min(args.warmup, 1)):
+        cpu_baseline(setup, recs, 1)
+    cb = cpu_baseline(setup, recs, max(1, args.steps if args.steps <= 10 else 10))
+    line = {"metric": "pair-interactions/s", "value": cb["value"], "unit": "pair-interactions/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": CONFIG,
+            "impl": "reference", "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": "pair-interactions/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference's own build (oracle/_ref) needs its source tree, absent on the GPU box; "
+                    "the oracle restatement, bit-exact with it in tests, is timed instead"}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, rank, world, D):
+    from tay_gb300 import api
+    from tay_gb300 import models as M
+
+    gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(rank)).split(",")[0] or 0) if world == 1 else rank
+    setup, recs = workload()
+    api.set_tuning(use_graphs=True)
+    B = api.Batch([(setup, recs)])
+    B.push()
+    for _ in range(args.warmup):
+        B.flush_l2()
+        B.run(1)
+
+    clocks = Clocks(gpu_index)
+    clocks.start()
+    D.barrier()
+    dev_ms, pairs = 0.0, 0
+    for _ in range(args.steps):
+        B.flush_l2()
+        ms, p = B.run(1)
+        dev_ms += ms
+        pairs += p
+    D.barrier()
+    # profiled leg: per-kernel-class device time, same flush protocol, no graphs
+    prof_steps = min(args.steps, 20)
+    prof = [0.0] * 8
+    for _ in range(prof_steps):
+        B.flush_l2()
+        part = B.profile(1)
+        prof = [a + b for a, b in zip(prof + [0.0] * (len(part) - len(prof)), part)]
+    launches = B.launches_per_step() * args.steps
+    B.close()
+
+    # e2e through the C API with host buffers (push + step + fetch per tay_run)
+    st, g = M.make_state(setup, recs)
+    st.start()
+    for _ in range(max(1, args.warmup // 2)):
+        st.run(1)
+    e2e_steps = min(args.steps, 50)
+    D.barrier()
+    t0 = time.perf_counter()
+    e2e_pairs = 0
+    for _ in range(e2e_steps):
+        st.run(1)
+        e2e_pairs += st.pairs()
+    e2e_s = time.perf_counter() - t0
+    D.barrier()
+    st.end()
+    st.close()
+    clk = clocks.stop()
+
+    secs = D.max(dev_ms / 1000.0)
+    all_pairs = D.sum(pairs)
+    e2e_s = D.max(e2e_s)
+    e2e_pairs = D.sum(e2e_pairs)
+
+    peak, peak_kind = peaks()
+    see_ms = prof[4] / prof_steps
+    # algorithmic bytes of one fused see+act launch: every agent's seen fields (position
+    # and velocity, 32 B) read once and its new position and velocity (32 B) written once
+    see_bytes = N_BOIDS * 64
+    achieved = see_bytes / (see_ms / 1000.0) / 1e9
+    step_ms = sum(prof) / prof_steps
+    # whole-step algorithmic bytes (key from position 16 B, key+index write 8 B, reorder of
+    # the 36 B state read+write, see+act 64 B)
+    step_bytes = N_BOIDS * (16 + 8 + 2 * 36 + 64)
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "see_boids_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+    if rank == 0:
+        line = {
+            "metric": "pair-interactions/s", "value": all_pairs / secs, "unit": "pair-interactions/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded SplitMix64, BASELINE boids shape)",
+            "config": dict(CONFIG, l2="flushed between timed steps", parallelism=f"replicas{world}"),
+            "steps_per_s": args.steps / secs,
+            "pairs_per_step": all_pairs / world / args.steps,
+            "e2e": {"value": e2e_pairs / e2e_s, "unit": "pair-interactions/s",
+                    "h2d_bytes_per_step": N_BOIDS * BOIDS_RECORD_BYTES,
+                    "d2h_bytes_per_step": N_BOIDS * BOIDS_RECORD_BYTES, "steps": e2e_steps,
+                    "ms_per_step": 1000.0 * e2e_s / e2e_steps},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": "see_kernel<boids::SeeAct>", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": see_bytes, "launch_ms": see_ms},
+            "step_roofline": {"achieved": step_bytes / (step_ms / 1000.0) / 1e9, "unit": "GB/s",
+                              "frac": step_bytes / (step_ms / 1000.0) / 1e9 / peak,
+                              "algorithmic_bytes_per_step": step_bytes, "profiled_step_ms": step_ms},
+            "kernel_ms": {"box": prof[0] / prof_steps, "sort": prof[1] / prof_steps,
+                          "cell_table": prof[2] / prof_steps, "reorder": prof[3] / prof_steps,
+                          "see_act": prof[4] / prof_steps},
+            "clocks": clk,
+        }
+        if not args.no_cpu_baseline and world == 1:
+            line["cpu_baseline"] = cpu_baseline(setup, recs, args.cpu_steps)
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    D = Dist(world)
+    try:
+        run_gb300(args, rank, world, D)
+    finally:
+        D.close()
+
+
+if __name__ == "__main__":
+    main()

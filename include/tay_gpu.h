@@ -84,6 +84,24 @@ int tgpu_batch_fetch(TgpuBatch *batch, int group, void *host_records);
 double tgpu_batch_last_device_ms(const TgpuBatch *batch);
 unsigned long long tgpu_batch_last_pairs(const TgpuBatch *batch);
 
+/* Profiled run: enqueues `steps` steps without graphs, with CUDA events on the batch's
+ * stream around each kernel class, waits, and adds the device ms of each class to
+ * ms[0..n): 0 bounding box, 1 keys + radix sort, 2 cell table write + clear, 3 reorder,
+ * 4.. the model's pass kernels in program order. Returns TGPU_OK or an error. */
+int tgpu_batch_profile(TgpuBatch *batch, int steps, double *ms, int n);
+
+/* Number of kernel classes tgpu_batch_profile reports (4 + pass kernels). */
+int tgpu_batch_kernel_classes(const TgpuBatch *batch);
+
+/* Evicts the L2 cache by writing a scratch buffer larger than it on the batch's stream
+ * (for timing without warm-cache carry-over between steps). */
+int tgpu_batch_flush_l2(TgpuBatch *batch);
+
+/* Page-locked host memory for AoS storage (faster push/fetch); falls back to ordinary
+ * zeroed memory when no CUDA device is usable.  Free with tgpu_host_free. */
+void *tgpu_host_alloc(unsigned long long bytes);
+void tgpu_host_free(void *ptr);
+
 /* Number of kernel launches one step enqueues. */
 int tgpu_batch_launches_per_step(const TgpuBatch *batch);
 

@@ -88,14 +88,18 @@ static inline void o_test_act(void *va, void *vc) {
 }
 
 /* ---------------------------------------------------------------------------------
- * Boids: separation / alignment / cohesion inside a sphere of radius r.
+ * Boids (Reynolds' rules in the steering form of Shiffman's "Nature of Code" flocking,
+ * with its weights 1.5 / 1.0 / 1.0 and max speed 2): neighbours within radius r,
+ * separation from neighbours within sep_r.
  *   see(a, b): d = b.p - a.p, d2 = (dx*dx + dy*dy) + dz*dz
- *              if 0 < d2 < r2: count++, coh += d, ali += b.v, sep -= d * (1 / d2)
- *   act(a):    if count > 0:
- *                 acc = w_sep * sep/n + w_ali * (ali/n - v) + w_coh * (coh/n) / r
- *                 v += dt * acc
- *              speed = |v|; if speed > max_speed: v *= max_speed / speed
- *              p += dt * v; accumulators reset
+ *              if 0 < d2 < r2:   count++, coh += d, ali += b.v
+ *                 if d2 < sep_r2: sep_count++, sep -= d * (1 / d2)
+ *   act(a):    for (vec, n, w) in (sep, sep_count, w_sep), (ali, count, w_ali), (coh, count, w_coh):
+ *                 if n > 0 and |vec| > 0:
+ *                    s = vec * (max_speed / |vec|) - v;  if |s| > max_force: s *= max_force / |s|
+ *                    acc += w * s
+ *              v += dt * acc; if |v| > max_speed: v *= max_speed / |v|; p += dt * v
+ *              accumulators reset
  * --------------------------------------------------------------------------------- */
 typedef struct {
     OTag tag;
@@ -105,18 +109,22 @@ typedef struct {
     REAL ali[4];
     REAL sep[4];
     int count;
+    int sep_count;
     int id;
+    int pad;
 } OBoid;
 
 typedef struct {
     REAL r;
     REAL r2;
+    REAL sep_r2;
     REAL w_sep;
     REAL w_ali;
     REAL w_coh;
     REAL max_speed;
+    REAL max_force;
     REAL dt;
-    REAL pad;
+    REAL pad[3];
 } OBoidsContext;
 
 static inline void o_boids_see(void *va, void *vb, void *vc) {
@@ -130,7 +138,6 @@ static inline void o_boids_see(void *va, void *vb, void *vc) {
     d2 = d2 + dy * dy;
     d2 = d2 + dz * dz;
     if (d2 < c->r2 && d2 > (REAL)0) {
-        REAL inv = (REAL)1 / d2;
         a->count++;
         a->coh[0] = a->coh[0] + dx;
         a->coh[1] = a->coh[1] + dy;
@@ -138,30 +145,53 @@ static inline void o_boids_see(void *va, void *vb, void *vc) {
         a->ali[0] = a->ali[0] + b->v[0];
         a->ali[1] = a->ali[1] + b->v[1];
         a->ali[2] = a->ali[2] + b->v[2];
-        a->sep[0] = a->sep[0] - dx * inv;
-        a->sep[1] = a->sep[1] - dy * inv;
-        a->sep[2] = a->sep[2] - dz * inv;
+        if (d2 < c->sep_r2) {
+            REAL inv = (REAL)1 / d2;
+            a->sep_count++;
+            a->sep[0] = a->sep[0] - dx * inv;
+            a->sep[1] = a->sep[1] - dy * inv;
+            a->sep[2] = a->sep[2] - dz * inv;
+        }
     }
+}
+
+static inline REAL o_len3(const REAL *x) {
+    REAL s = x[0] * x[0];
+    s = s + x[1] * x[1];
+    s = s + x[2] * x[2];
+    return O_SQRT(s);
+}
+
+static inline void o_boids_steer(const REAL *vec, int n, REAL w, const REAL *v, const OBoidsContext *c, REAL *acc) {
+    if (n <= 0)
+        return;
+    REAL len = o_len3(vec);
+    if (!(len > (REAL)0))
+        return;
+    REAL k = c->max_speed / len;
+    REAL s[3];
+    for (int i = 0; i < 3; ++i)
+        s[i] = vec[i] * k - v[i];
+    REAL sl = o_len3(s);
+    if (sl > c->max_force) {
+        REAL f = c->max_force / sl;
+        for (int i = 0; i < 3; ++i)
+            s[i] = s[i] * f;
+    }
+    for (int i = 0; i < 3; ++i)
+        acc[i] = acc[i] + w * s[i];
 }
 
 static inline void o_boids_act(void *va, void *vc) {
     OBoid *a = (OBoid *)va;
     const OBoidsContext *c = (const OBoidsContext *)vc;
-    if (a->count > 0) {
-        REAL inv_n = (REAL)1 / (REAL)a->count;
-        REAL inv_r = (REAL)1 / c->r;
-        for (int i = 0; i < 3; ++i) {
-            REAL s = c->w_sep * (a->sep[i] * inv_n);
-            REAL al = c->w_ali * (a->ali[i] * inv_n - a->v[i]);
-            REAL co = c->w_coh * ((a->coh[i] * inv_n) * inv_r);
-            REAL acc = (s + al) + co;
-            a->v[i] = a->v[i] + c->dt * acc;
-        }
-    }
-    REAL s2 = a->v[0] * a->v[0];
-    s2 = s2 + a->v[1] * a->v[1];
-    s2 = s2 + a->v[2] * a->v[2];
-    REAL speed = O_SQRT(s2);
+    REAL acc[3] = {0, 0, 0};
+    o_boids_steer(a->sep, a->sep_count, c->w_sep, a->v, c, acc);
+    o_boids_steer(a->ali, a->count, c->w_ali, a->v, c, acc);
+    o_boids_steer(a->coh, a->count, c->w_coh, a->v, c, acc);
+    for (int i = 0; i < 3; ++i)
+        a->v[i] = a->v[i] + c->dt * acc[i];
+    REAL speed = o_len3(a->v);
     if (speed > c->max_speed) {
         REAL k = c->max_speed / speed;
         for (int i = 0; i < 3; ++i)
@@ -174,6 +204,7 @@ static inline void o_boids_act(void *va, void *vc) {
         a->sep[i] = 0;
     }
     a->count = 0;
+    a->sep_count = 0;
 }
 
 /* ---------------------------------------------------------------------------------

@@ -34,7 +34,7 @@ def _rec(real):
     test = np.dtype([("tag", "<u4", 2), ("p", f, 4), ("v", f, 4), ("b_buffer", f, 4), ("b_buffer_count", "<i4"),
                      ("f_buffer", f, 4), ("id", "<i4")])
     boid = np.dtype([("tag", "<u4", 2), ("p", f, 4), ("v", f, 4), ("coh", f, 4), ("ali", f, 4), ("sep", f, 4),
-                     ("count", "<i4"), ("id", "<i4")])
+                     ("count", "<i4"), ("sep_count", "<i4"), ("id", "<i4"), ("pad", "<i4")])
     sph = np.dtype([("tag", "<u4", 2), ("p", f, 4), ("v", f, 4), ("a", f, 4), ("rho", f), ("P", f), ("id", "<i4"),
                     ("pad", "<i4")])
     return {MODEL_TEST: test, MODEL_BOIDS: boid, MODEL_SPH: sph}
@@ -42,13 +42,14 @@ def _rec(real):
 
 RECORDS = {np.float32: _rec(np.float32), np.float64: _rec(np.float64)}
 assert RECORDS[np.float32][MODEL_TEST].itemsize == 80
-assert RECORDS[np.float32][MODEL_BOIDS].itemsize == 96
+assert RECORDS[np.float32][MODEL_BOIDS].itemsize == 104
 assert RECORDS[np.float32][MODEL_SPH].itemsize == 72
 
 
-def boids_context(real, r=10.0, w_sep=1.5, w_ali=1.0, w_coh=1.0, max_speed=2.0, dt=1.0):
+def boids_context(real, r=10.0, sep_r=5.0, w_sep=1.5, w_ali=1.0, w_coh=1.0, max_speed=2.0, max_force=0.03, dt=1.0):
     r = real(r)
-    return np.array([r, r * r, w_sep, w_ali, w_coh, max_speed, dt, 0.0], dtype=real)
+    sep_r = real(sep_r)
+    return np.array([r, r * r, sep_r * sep_r, w_sep, w_ali, w_coh, max_speed, max_force, dt, 0, 0, 0], dtype=real)
 
 
 def sph_context(real, h=0.02, dx=0.01, rho0=1000.0, c0=20.0, alpha=0.05, dt=1e-4, g=(0.0, 0.0, -9.81),
@@ -98,14 +99,21 @@ def _bind(lib, name, real_c):
 class RunResult:
     records: np.ndarray
     ms_per_step: float
+    pairs: int = -1  # box-test passes over the run (port only)
 
 
 class _Impl:
-    def __init__(self, so, names):
+    def __init__(self, so, names, pair_fns=None):
         if not os.path.exists(so):
             raise FileNotFoundError(so)
         self.lib = ctypes.CDLL(so)
         self.fns = {real: _bind(self.lib, nm, c) for real, (nm, c) in names.items()}
+        self.pair_fns = {}
+        for real, nm in (pair_fns or {}).items():
+            f = getattr(self.lib, nm)
+            f.restype = ctypes.c_ulonglong
+            f.argtypes = []
+            self.pair_fns[real] = f
 
     def run(self, model, space, records, see_ctx, act_ctx, radius, part_size, steps, pass_mask, threads=0, mb=250,
             real=np.float32):
@@ -119,7 +127,8 @@ class _Impl:
                  real(part_size), mb, steps, pass_mask, threads, ctypes.byref(ms))
         if ran != steps:
             raise RuntimeError(f"oracle run failed ({ran} of {steps} steps)")
-        return RunResult(rec, ms.value)
+        pairs = int(self.pair_fns[real]()) if real in self.pair_fns else -1
+        return RunResult(rec, ms.value, pairs)
 
 
 _port = None
@@ -132,7 +141,8 @@ def port():
         if not os.path.exists(PORT_SO):
             build_port()
         _port = _Impl(PORT_SO, {np.float32: ("oracle_run_f32", ctypes.c_float),
-                                np.float64: ("oracle_run_f64", ctypes.c_double)})
+                                np.float64: ("oracle_run_f64", ctypes.c_double)},
+                      {np.float32: "oracle_last_pairs_f32", np.float64: "oracle_last_pairs_f64"})
     return _port
 
 

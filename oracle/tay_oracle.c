@@ -359,8 +359,11 @@ static void o_unsort(OGroup *g) {
 
 /* tay/space.c:106-148; `skip_self` selects space_see_point_point (same group, no
  * self-see) over space_see_point_point_self_see */
-static void o_pair(const OGroup *g, const OPass *pass, unsigned seer_beg, unsigned seer_end, unsigned seen_beg,
+static unsigned long long O_NAME(pairs_by_thread)[64];
+
+static unsigned long long o_pair(const OGroup *g, const OPass *pass, unsigned seer_beg, unsigned seer_end, unsigned seen_beg,
                    unsigned seen_end, int skip_self) {
+    unsigned long long pairs = 0;
     for (unsigned s = seer_beg; s < seer_end; ++s) {
         char *seer = g->storage + (size_t)g->agent_size * s;
         const REAL *sp = o_pos(g, s);
@@ -378,9 +381,11 @@ static void o_pair(const OGroup *g, const OPass *pass, unsigned seer_beg, unsign
             }
             if (skip)
                 continue;
+            ++pairs; /* the reference's narrow-phase counter, tay/space.c:56-60 */
             pass->see(seer, g->storage + (size_t)g->agent_size * b, pass->ctx);
         }
     }
+    return pairs;
 }
 
 /* neighbour cell index box for a seer box (tay/cpu_z_grid.c:232-247, tay/cpu_grid.c:158-174) */
@@ -408,8 +413,9 @@ static void o_see_task(OTask *task, int thread_i, int threads) {
     unsigned beg, end;
     o_range(g->count, thread_i, threads, &beg, &end);
 
+    unsigned long long pairs = 0;
     if (g->space == O_SPACE_SIMPLE) { /* tay/cpu_simple.c:6-38 */
-        o_pair(g, pass, beg, end, 0, g->count, skip_self);
+        O_NAME(pairs_by_thread)[thread_i] += o_pair(g, pass, beg, end, 0, g->count, skip_self);
         return;
     }
 
@@ -457,10 +463,11 @@ static void o_see_task(OTask *task, int thread_i, int threads) {
                         first = c->first;
                         count = c->count;
                     }
-                    o_pair(g, pass, s, run_end, first, first + count, skip_self);
+                    pairs += o_pair(g, pass, s, run_end, first, first + count, skip_self);
                 }
         s = run_end;
     }
+    O_NAME(pairs_by_thread)[thread_i] += pairs;
 }
 
 static void o_act_task(OTask *task, int thread_i, int threads) {
@@ -488,6 +495,14 @@ static int o_agent_id(int model, const char *a) {
         case O_MODEL_BOIDS: return ((const OBoid *)a)->id;
         default: return ((const OSphParticle *)a)->id;
     }
+}
+
+/* Box-test passes summed over the passes and steps of the last oracle_run. */
+unsigned long long O_NAME(oracle_last_pairs)(void) {
+    unsigned long long s = 0;
+    for (int i = 0; i < 64; ++i)
+        s += O_NAME(pairs_by_thread)[i];
+    return s;
 }
 
 unsigned O_NAME(oracle_agent_size)(int model) {
@@ -560,6 +575,7 @@ int O_NAME(oracle_run)(int model, int space, int n, void *agents, const void *se
             passes[passes_count++] = (OPass){0, 0, o_sph_integrate, {0, 0, 0}, 0, &sph};
     }
 
+    memset(O_NAME(pairs_by_thread), 0, sizeof(O_NAME(pairs_by_thread)));
     struct timespec t0, t1;
     clock_gettime(CLOCK_MONOTONIC, &t0);
     for (int step = 0; step < steps; ++step) {

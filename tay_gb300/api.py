@@ -86,6 +86,11 @@ TGPU_SYMBOLS = [
     ("tgpu_batch_program", ctypes.c_int, [_VP]),
     ("tgpu_set_tuning", None, [ctypes.c_uint, ctypes.c_uint, ctypes.c_float, ctypes.c_int]),
     ("tgpu_model_of", ctypes.c_char_p, [ctypes.c_char_p]),
+    ("tgpu_batch_profile", ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
+    ("tgpu_batch_kernel_classes", ctypes.c_int, [_VP]),
+    ("tgpu_batch_flush_l2", ctypes.c_int, [_VP]),
+    ("tgpu_host_alloc", _VP, [ctypes.c_ulonglong]),
+    ("tgpu_host_free", None, [_VP]),
     ("tgpu_device_count", ctypes.c_int, []),
     ("tgpu_last_error", ctypes.c_char_p, []),
 ]
@@ -205,6 +210,96 @@ class State:
 
     def pairs(self):
         return self.L.tay_get_pairs_for_last_run(self.ptr)
+
+
+class TgpuPass(ctypes.Structure):
+    _fields_ = [("func_name", ctypes.c_char_p), ("is_see", ctypes.c_int), ("radii", ctypes.c_float * 4),
+                ("self_see", ctypes.c_int), ("context", ctypes.c_void_p), ("context_size", ctypes.c_uint)]
+
+
+class TgpuGroup(ctypes.Structure):
+    _fields_ = [("agent_size", ctypes.c_uint), ("count", ctypes.c_uint), ("min_part_sizes", ctypes.c_float * 4),
+                ("shared_megabytes", ctypes.c_int), ("box_fixed", ctypes.c_int), ("box_min", ctypes.c_float * 4),
+                ("box_max", ctypes.c_float * 4), ("pass_count", ctypes.c_int),
+                ("passes", ctypes.POINTER(TgpuPass))]
+
+
+class Batch:
+    """Direct use of the engine ABI (include/tay_gpu.h): one device batch of groups that
+    share a model and pass sequence.  `groups` is a list of (setup, records) pairs with
+    setup a tay_gb300.models.Setup."""
+
+    def __init__(self, groups):
+        self.L = lib()
+        self._keep = []
+        descs = (TgpuGroup * len(groups))()
+        for i, (setup, recs) in enumerate(groups):
+            passes = (TgpuPass * len(setup.passes))()
+            for k, p in enumerate(setup.passes):
+                ctx = np.ascontiguousarray(p.ctx)
+                name = p.name.encode()
+                self._keep += [ctx, name]
+                passes[k].func_name = name
+                passes[k].is_see = 1 if p.see else 0
+                passes[k].radii[:] = [p.radius] * 4
+                passes[k].self_see = 1 if p.self_see else 0
+                passes[k].context = ctx.ctypes.data
+                passes[k].context_size = ctx.nbytes
+            self._keep.append(passes)
+            d = descs[i]
+            d.agent_size = setup.dtype.itemsize
+            d.count = recs.shape[0]
+            d.min_part_sizes[:] = [setup.part] * 4
+            d.shared_megabytes = setup.mb
+            d.box_fixed = 0
+            d.pass_count = len(setup.passes)
+            d.passes = passes
+        self._descs = descs
+        self.ptr = ctypes.c_void_p()
+        self._check(self.L.tgpu_batch_create(descs, len(groups), ctypes.byref(self.ptr)), "tgpu_batch_create")
+        self.groups = groups
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise TayError(f"{what}: {self.L.tgpu_last_error().decode()}")
+
+    def push(self):
+        for i, (_, recs) in enumerate(self.groups):
+            r = np.ascontiguousarray(recs)
+            self._check(self.L.tgpu_batch_push(self.ptr, i, r.ctypes.data), "tgpu_batch_push")
+
+    def run(self, steps):
+        self._check(self.L.tgpu_batch_run(self.ptr, steps), "tgpu_batch_run")
+        return self.L.tgpu_batch_last_device_ms(self.ptr), self.L.tgpu_batch_last_pairs(self.ptr)
+
+    def fetch(self, i):
+        setup, recs = self.groups[i]
+        out = np.zeros(recs.shape[0], setup.dtype)
+        self._check(self.L.tgpu_batch_fetch(self.ptr, i, out.ctypes.data), "tgpu_batch_fetch")
+        return out
+
+    def profile(self, steps):
+        n = self.L.tgpu_batch_kernel_classes(self.ptr)
+        ms = (ctypes.c_double * n)()
+        self._check(self.L.tgpu_batch_profile(self.ptr, steps, ms, n), "tgpu_batch_profile")
+        return list(ms)
+
+    def flush_l2(self):
+        self._check(self.L.tgpu_batch_flush_l2(self.ptr), "tgpu_batch_flush_l2")
+
+    def launches_per_step(self):
+        return self.L.tgpu_batch_launches_per_step(self.ptr)
+
+    def close(self):
+        if self.ptr:
+            self.L.tgpu_batch_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def run_batch(states, steps):

@@ -1,19 +1,25 @@
 // Boids on the GPU, registered as "boids_see" / "boids_act".
 //
-// Model (separation / alignment / cohesion inside a sphere of radius r):
+// Model: Reynolds' rules in the steering form of Shiffman's "Nature of Code" flocking
+// (weights 1.5 / 1.0 / 1.0, max speed 2, max force 0.03): neighbours inside radius r,
+// separation from neighbours inside sep_r.
 //   see(a, b):  d = b.p - a.p, d2 = (dx*dx + dy*dy) + dz*dz, each product and sum rounded
-//               separately (no FMA), so the neighbour decision 0 < d2 < r2 is bit-identical
-//               to an IEEE evaluation of the same expression on the CPU;
-//               count++, coh += d, ali += b.v, sep -= d * (1 / d2)
-//   act(a):     if count > 0: acc = w_sep*sep/n + w_ali*(ali/n - v) + w_coh*(coh/n)/r,
+//               separately (no FMA), so the neighbour decisions are bit-identical to an
+//               IEEE evaluation of the same expression on the CPU;
+//               if 0 < d2 < r2:   count++, coh += d, ali += b.v
+//                  if d2 < sep_r2: sep_count++, sep -= d * (1 / d2)
+//   act(a):     for (vec, n, w) in (sep, sep_count, w_sep), (ali, count, w_ali),
+//               (coh, count, w_coh): if n > 0 and |vec| > 0:
+//                  s = vec * (max_speed / |vec|) - v, limited to |s| <= max_force;
+//                  acc += w * s
 //               v += dt*acc; clamp |v| to max_speed; p += dt*v
 // Accumulators are per-step outputs: every see pass starts them from zero and the act
 // pass consumes them, so after a see+act step they read back as zero.
 //
-// AoS record (96 bytes): tag u32[2] @0, p float4 @8, v float4 @24, coh float4 @40,
-// ali float4 @56, sep float4 @72, count int @88, id int @92.
+// AoS record (104 bytes): tag u32[2] @0, p float4 @8, v float4 @24, coh float4 @40,
+// ali float4 @56, sep float4 @72, count int @88, sep_count int @92, id int @96, pad @100.
 // Streams: f4[0] POS, f4[1] VEL, u32[0] ID (state); f4[2] ACC0 = coh.xyz + count,
-// f4[3] ACC1 = ali.xyz, f4[4] ACC2 = sep.xyz (per-step).
+// f4[3] ACC1 = ali.xyz + sep_count, f4[4] ACC2 = sep.xyz (per-step).
 #include "model.cuh"
 
 namespace tgpu {
@@ -23,12 +29,12 @@ enum { POS = 0, VEL = 1, ACC0 = 2, ACC1 = 3, ACC2 = 4 };
 enum { ID = 0 };
 
 struct Ctx {
-    float r, r2, w_sep, w_ali, w_coh, max_speed, dt, pad;
+    float r, r2, sep_r2, w_sep, w_ali, w_coh, max_speed, max_force, dt, pad[3];
 };
 
 struct Seer {
     float cx, cy, cz, ax, ay, az, sx, sy, sz;
-    int count;
+    int count, sep_count;
     float4 v;
 };
 
@@ -37,6 +43,7 @@ TGPU_D void zero(Seer &s) {
     s.ax = s.ay = s.az = 0.0f;
     s.sx = s.sy = s.sz = 0.0f;
     s.count = 0;
+    s.sep_count = 0;
 }
 
 template <class Acc>
@@ -46,7 +53,6 @@ TGPU_D void see_fn(Seer &s, const float4 &a, const float4 &b, const Acc &acc, ui
     d2 = __fadd_rn(d2, __fmul_rn(dy, dy));
     d2 = __fadd_rn(d2, __fmul_rn(dz, dz));
     if (d2 < c.r2 && d2 > 0.0f) {
-        const float inv = __frcp_rn(d2);
         const float4 bv = acc.f4(1, j);
         s.count += 1;
         s.cx += dx;
@@ -55,27 +61,51 @@ TGPU_D void see_fn(Seer &s, const float4 &a, const float4 &b, const Acc &acc, ui
         s.ax += bv.x;
         s.ay += bv.y;
         s.az += bv.z;
-        s.sx -= dx * inv;
-        s.sy -= dy * inv;
-        s.sz -= dz * inv;
+        if (d2 < c.sep_r2) {
+            const float inv = __frcp_rn(d2);
+            s.sep_count += 1;
+            s.sx -= dx * inv;
+            s.sy -= dy * inv;
+            s.sz -= dz * inv;
+        }
     }
 }
 
-TGPU_D void act_fn(float4 &p, float4 &v, const Seer &s, const Ctx &c) {
-    if (s.count > 0) {
-        const float inv_n = 1.0f / (float)s.count;
-        const float inv_r = 1.0f / c.r;
-        const float accx = (c.w_sep * (s.sx * inv_n) + c.w_ali * (s.ax * inv_n - v.x)) + c.w_coh * ((s.cx * inv_n) * inv_r);
-        const float accy = (c.w_sep * (s.sy * inv_n) + c.w_ali * (s.ay * inv_n - v.y)) + c.w_coh * ((s.cy * inv_n) * inv_r);
-        const float accz = (c.w_sep * (s.sz * inv_n) + c.w_ali * (s.az * inv_n - v.z)) + c.w_coh * ((s.cz * inv_n) * inv_r);
-        v.x = v.x + c.dt * accx;
-        v.y = v.y + c.dt * accy;
-        v.z = v.z + c.dt * accz;
+TGPU_D float len3(float x, float y, float z) {
+    float s = x * x;
+    s = s + y * y;
+    s = s + z * z;
+    return sqrtf(s);
+}
+
+TGPU_D void steer(float vx, float vy, float vz, int n, float w, const float4 &v, const Ctx &c, float &ax, float &ay,
+                  float &az) {
+    if (n <= 0) return;
+    const float len = len3(vx, vy, vz);
+    if (!(len > 0.0f)) return;
+    const float k = c.max_speed / len;
+    float sx = vx * k - v.x, sy = vy * k - v.y, sz = vz * k - v.z;
+    const float sl = len3(sx, sy, sz);
+    if (sl > c.max_force) {
+        const float f = c.max_force / sl;
+        sx *= f;
+        sy *= f;
+        sz *= f;
     }
-    float s2 = v.x * v.x;
-    s2 = s2 + v.y * v.y;
-    s2 = s2 + v.z * v.z;
-    const float speed = sqrtf(s2);
+    ax += w * sx;
+    ay += w * sy;
+    az += w * sz;
+}
+
+TGPU_D void act_fn(float4 &p, float4 &v, const Seer &s, const Ctx &c) {
+    float ax = 0.0f, ay = 0.0f, az = 0.0f;
+    steer(s.sx, s.sy, s.sz, s.sep_count, c.w_sep, v, c, ax, ay, az);
+    steer(s.ax, s.ay, s.az, s.count, c.w_ali, v, c, ax, ay, az);
+    steer(s.cx, s.cy, s.cz, s.count, c.w_coh, v, c, ax, ay, az);
+    v.x = v.x + c.dt * ax;
+    v.y = v.y + c.dt * ay;
+    v.z = v.z + c.dt * az;
+    const float speed = len3(v.x, v.y, v.z);
     if (speed > c.max_speed) {
         const float k = c.max_speed / speed;
         v.x *= k;
@@ -100,7 +130,7 @@ struct SeeOnly {
     }
     TGPU_D static void finish(Seer &s, const float4 &, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {
         io.out_f4[ACC0][i] = make_float4(s.cx, s.cy, s.cz, __int_as_float(s.count));
-        io.out_f4[ACC1][i] = make_float4(s.ax, s.ay, s.az, 0.0f);
+        io.out_f4[ACC1][i] = make_float4(s.ax, s.ay, s.az, __int_as_float(s.sep_count));
         io.out_f4[ACC2][i] = make_float4(s.sx, s.sy, s.sz, 0.0f);
     }
 };
@@ -128,11 +158,11 @@ struct SeeAct {
 };
 
 struct Codec {
-    static constexpr uint32_t kAgentBytes = 96;
+    static constexpr uint32_t kAgentBytes = 104;
     TGPU_D static void pack(const uint32_t *w, const PassIO &io, uint32_t i) {
         io.out_f4[POS][i] = ld_words4(w + 2);
         io.out_f4[VEL][i] = ld_words4(w + 6);
-        io.out_u32[ID][i] = w[23];
+        io.out_u32[ID][i] = w[24];
     }
     // program 0: see only (accumulators visible); program 1: see + act (consumed)
     TGPU_D static void unpack(uint32_t *w, const PassIO &io, uint32_t i, uint32_t program) {
@@ -147,10 +177,12 @@ struct Codec {
             a2 = io.in_f4[ACC2][i];
         }
         st_words4(w + 10, make_float4(a0.x, a0.y, a0.z, 0.f));
-        st_words4(w + 14, a1);
-        st_words4(w + 18, a2);
+        st_words4(w + 14, make_float4(a1.x, a1.y, a1.z, 0.f));
+        st_words4(w + 18, make_float4(a2.x, a2.y, a2.z, 0.f));
         w[22] = __float_as_uint(a0.w);
-        w[23] = io.in_u32[ID][i];
+        w[23] = __float_as_uint(a1.w);
+        w[24] = io.in_u32[ID][i];
+        w[25] = 0u;
     }
 };
 
@@ -169,7 +201,7 @@ const ProgramDesc kPrograms[] = {
 };
 
 const ModelDesc kModel = {
-    "boids", 96, 5, 1, {kState, kState, kStep, kStep, kStep}, {kState}, (uint32_t)sizeof(Ctx), (uint32_t)sizeof(Ctx),
+    "boids", 104, 5, 1, {kState, kState, kStep, kStep, kStep}, {kState}, (uint32_t)sizeof(Ctx), (uint32_t)sizeof(Ctx),
     kKernels, 2, kPrograms, 2, pack_t<Codec>, unpack_t<Codec>,
 };
 

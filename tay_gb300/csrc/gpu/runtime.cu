@@ -317,14 +317,32 @@ SortLaunch sort_launch(TgpuBatch *b) {
     return L;
 }
 
-void enqueue_step(TgpuBatch *b) {
+// Optional per-class timing: when `ev` is given, an event is recorded before and after
+// each kernel class (ev[2k], ev[2k+1] for classes 0..3, then one pair per pass kernel;
+// the clear at the end is class 2's second half: ev2[0..1]).
+struct StepEvents {
+    cudaEvent_t *ev;   // 2 * classes
+    cudaEvent_t *ev2;  // 2 (table clear)
+};
+
+void mark(const StepEvents *e, int k, cudaStream_t st) {
+    if (e) cudaEventRecord(e->ev[k], st);
+}
+
+void enqueue_step(TgpuBatch *b, const StepEvents *E = nullptr) {
     if (b->total == 0 || b->tiles == 0) return;
     cudaStream_t st = b->st;
     SortLaunch L = sort_launch(b);
+    mark(E, 0, st);
     launch_box(L, st);
+    mark(E, 1, st);
     uint32_t *skeys = nullptr, *perm = nullptr;
+    mark(E, 2, st);
     launch_sort(L, st, &skeys, &perm);
+    mark(E, 3, st);
+    mark(E, 4, st);
     launch_cell_table(L, skeys, 1, st);
+    mark(E, 5, st);
 
     GatherSet g{};
     for (int c = 0; c < b->m->nf4; ++c) {
@@ -341,9 +359,13 @@ void enqueue_step(TgpuBatch *b) {
         b->cur_u32[c] ^= 1;
         ++g.nu32;
     }
+    mark(E, 6, st);
     launch_gather(b->total, perm, g, st);
+    mark(E, 7, st);
 
+    int kidx = 0;
     for (auto &r : b->runs) {
+        mark(E, 8 + 2 * kidx, st);
         const bool see = r.k->see != nullptr;
         PassIO io = make_io(b, r.k, see, 0);
         if (see) {
@@ -377,8 +399,12 @@ void enqueue_step(TgpuBatch *b) {
             A.io = io;
             r.k->launch_act(A, st);
         }
+        mark(E, 9 + 2 * kidx, st);
+        ++kidx;
     }
+    if (E) cudaEventRecord(E->ev2[0], st);
     launch_cell_table(L, skeys, 0, st);
+    if (E) cudaEventRecord(E->ev2[1], st);
 }
 
 uint64_t parity_signature(const TgpuBatch *b) {
@@ -409,6 +435,80 @@ void advance_parity(TgpuBatch *b) {
 extern "C" {
 
 const char *tgpu_last_error(void) { return g_err.c_str(); }
+
+int tgpu_batch_kernel_classes(const TgpuBatch *b) { return b ? 4 + (int)b->runs.size() : 0; }
+
+int tgpu_batch_profile(TgpuBatch *b, int steps, double *ms, int n) {
+    if (!b || steps < 0 || !ms) return fail(TGPU_ERR_ARG, "bad profile");
+    int rc = prepare_specs(b);
+    if (rc) return rc;
+    const int classes = 4 + (int)b->runs.size();
+    std::vector<cudaEvent_t> ev(2 * classes), ev2(2);
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    for (auto &e : ev2) CK(cudaEventCreate(&e));
+    StepEvents E{ev.data(), ev2.data()};
+    for (int s = 0; s < steps; ++s) {
+        enqueue_step(b, &E);
+        CK(cudaStreamSynchronize(b->st));
+        for (int k = 0; k < classes && k < n; ++k) {
+            float t = 0.0f;
+            CK(cudaEventElapsedTime(&t, ev[2 * k], ev[2 * k + 1]));
+            ms[k] += t;
+        }
+        float t = 0.0f;
+        CK(cudaEventElapsedTime(&t, ev2[0], ev2[1]));
+        if (n > 2) ms[2] += t;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    for (auto &e : ev2) cudaEventDestroy(e);
+    CK(cudaGetLastError());
+    return TGPU_OK;
+}
+
+int tgpu_batch_flush_l2(TgpuBatch *b) {
+    if (!b) return fail(TGPU_ERR_ARG, "null batch");
+    static void *scratch = nullptr;
+    static size_t scratch_bytes = 0;
+    int dev = 0, l2 = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
+    const size_t want = std::max<size_t>(2 * (size_t)l2, 256u << 20);
+    if (scratch_bytes < want) {
+        cudaFree(scratch);
+        scratch = nullptr;
+        scratch_bytes = 0;
+        CK(cudaMalloc(&scratch, want));
+        scratch_bytes = want;
+    }
+    CK(cudaMemsetAsync(scratch, (int)(b->total & 0xFF), scratch_bytes, b->st));
+    return TGPU_OK;
+}
+
+void *tgpu_host_alloc(unsigned long long bytes) {
+    void *p = nullptr;
+    if (bytes == 0) bytes = 1;
+    if (cudaHostAlloc(&p, (size_t)bytes, cudaHostAllocDefault) == cudaSuccess) {
+        memset(p, 0, (size_t)bytes);
+        return p;
+    }
+    cudaGetLastError();
+    // no usable device: ordinary memory, tagged so tgpu_host_free can tell them apart
+    unsigned char *q = (unsigned char *)calloc(1, (size_t)bytes + 64);
+    if (!q) return nullptr;
+    q[0] = 0xA5;
+    return q + 64;
+}
+
+void tgpu_host_free(void *ptr) {
+    if (!ptr) return;
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, ptr) == cudaSuccess && attr.type == cudaMemoryTypeHost) {
+        cudaFreeHost(ptr);
+        return;
+    }
+    cudaGetLastError();
+    free((unsigned char *)ptr - 64);
+}
 
 int tgpu_device_count(void) {
     int n = 0;

@@ -211,6 +211,12 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
     const int wh0 = warp_max_i(hi[0]), wh1 = warp_max_i(hi[1]), wh2 = warp_max_i(hi[2]);
     uint32_t pairs = 0;
     if (wl0 <= wh0) {
+        // A warp walks the union of its lanes' cell boxes (one broadcast read serves all
+        // 32 lanes) when the union is compact; when its seers are spread out, as in sparse
+        // regions, each lane walks its own box instead.
+        const int lane_vol = active ? max(0, hi[0] - lo[0] + 1) * max(0, hi[1] - lo[1] + 1) * max(0, hi[2] - lo[2] + 1) : 0;
+        const long long union_vol = (long long)(wh0 - wl0 + 1) * (wh1 - wl1 + 1) * (wh2 - wl2 + 1);
+        const bool union_mode = union_vol <= 2LL * warp_max_i(lane_vol);
         if (staged) {
             uint32_t self_slot = 0xFFFFFFFFu;
             if (active && L.skip_self) {
@@ -223,33 +229,39 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
                 }
             }
             const SmemSeen acc{stage, L.stage_cap};
-            for (int z = wl2; z <= wh2; ++z)
-                for (int y = wl1; y <= wh1; ++y) {
-                    const uint32_t row = ((uint32_t)(z - H0z) * (uint32_t)hy + (uint32_t)(y - H0y)) * (uint32_t)hx;
-                    const uint32_t j0 = cell_off[row + (uint32_t)(wl0 - H0x)];
-                    const uint32_t j1 = cell_off[row + (uint32_t)(wh0 - H0x) + 1];
+            // the rows this lane walks: the warp's union box, or the lane's own box
+            const int z0 = union_mode ? wl2 : lo[2], z1 = union_mode ? wh2 : hi[2];
+            const int y0 = union_mode ? wl1 : lo[1], y1 = union_mode ? wh1 : hi[1];
+            const int x0 = union_mode ? wl0 : lo[0], x1 = union_mode ? wh0 : hi[0];
+            if (union_mode || active) {
+                for (int z = z0; z <= z1; ++z)
+                    for (int y = y0; y <= y1; ++y) {
+                        const uint32_t row = ((uint32_t)(z - H0z) * (uint32_t)hy + (uint32_t)(y - H0y)) * (uint32_t)hx;
+                        const uint32_t j0 = cell_off[row + (uint32_t)(x0 - H0x)];
+                        const uint32_t j1 = cell_off[row + (uint32_t)(x1 - H0x) + 1];
 #pragma unroll 4
-                    for (uint32_t j = j0; j < j1; ++j) {
-                        const float4 bp = stage[j];
-                        if (active && j != self_slot && box_hit(sp, bp, r4)) {
-                            ++pairs;
-                            P::see(s, sp, bp, acc, j, sctx);
+                        for (uint32_t j = j0; j < j1; ++j) {
+                            const float4 bp = stage[j];
+                            if (active && j != self_slot && box_hit(sp, bp, r4)) {
+                                ++pairs;
+                                P::see(s, sp, bp, acc, j, sctx);
+                            }
                         }
                     }
-                }
-        } else {
+            }
+        } else if (active) {
             GlobalSeen<P::kSeenF4> acc;
 #pragma unroll
             for (int k = 0; k < P::kSeenF4; ++k) acc.s[k] = L.io.in_f4[P::seen_stream(k)];
             const float4 *pos = L.io.in_f4[0];
-            const uint32_t self = (active && L.skip_self) ? i : 0xFFFFFFFFu;
-            for (int z = wl2; z <= wh2; ++z)
-                for (int y = wl1; y <= wh1; ++y)
-                    for (int x = wl0; x <= wh0; ++x) {
+            const uint32_t self = L.skip_self ? i : 0xFFFFFFFFu;
+            for (int z = lo[2]; z <= hi[2]; ++z)
+                for (int y = lo[1]; y <= hi[1]; ++y)
+                    for (int x = lo[0]; x <= hi[0]; ++x) {
                         const uint2 e = table[((uint32_t)z * dy0 + (uint32_t)y) * dx0 + (uint32_t)x];
                         for (uint32_t b = e.x; b < e.y; ++b) {
                             const float4 bp = __ldg(pos + b);
-                            if (active && b != self && box_hit(sp, bp, r4)) {
+                            if (b != self && box_hit(sp, bp, r4)) {
                                 ++pairs;
                                 P::see(s, sp, bp, acc, b, sctx);
                             }

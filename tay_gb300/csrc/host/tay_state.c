@@ -101,7 +101,7 @@ void tay_destroy_state(TayState *state) {
     if (!state) return;
     if (cache_refers_to(state)) drop_batch_cache();
     release_batch(state);
-    for (int i = 0; i < TAY_MAX_GROUPS; ++i) free(state->groups[i].storage);
+    for (int i = 0; i < TAY_MAX_GROUPS; ++i) tgpu_host_free(state->groups[i].storage);
     free(state);
 }
 
@@ -131,7 +131,7 @@ TayGroup *tay_add_group(TayState *state, unsigned agent_size, unsigned agent_cap
     }
     TayGroup *g = state->groups + i;
     memset(g, 0, sizeof(*g));
-    g->storage = (char *)calloc(agent_capacity ? agent_capacity : 1, agent_size ? agent_size : 1);
+    g->storage = (char *)tgpu_host_alloc((unsigned long long)(agent_capacity ? agent_capacity : 1) * (agent_size ? agent_size : 1));
     if (!g->storage) {
         set_error(state, TAY_ERROR_GROUP_INDEX_OUT_OF_RANGE, "out of host memory");
         return 0;

@@ -6,7 +6,8 @@ reference host registers its functions for the OpenCL path.
 
   test_basic  the reference's test agent (test/agent.h:2-19, test/agent.c:2-55):
               passes agent_see (self_see FALSE), agent_act
-  boids       separation / alignment / cohesion: boids_see (self_see FALSE), boids_act
+  boids       separation / alignment / cohesion in steering form: boids_see (self_see
+              FALSE), boids_act
   sph         weakly compressible SPH: sph_density (self_see TRUE), sph_pressure,
               sph_force (self_see FALSE), sph_integrate
 """
@@ -23,10 +24,10 @@ F4 = ("<f4", 4)
 TEST_RECORD = np.dtype([("tag", "<u4", 2), ("p",) + F4, ("v",) + F4, ("b_buffer",) + F4, ("b_buffer_count", "<i4"),
                         ("f_buffer",) + F4, ("id", "<i4")])
 BOIDS_RECORD = np.dtype([("tag", "<u4", 2), ("p",) + F4, ("v",) + F4, ("coh",) + F4, ("ali",) + F4,
-                         ("sep",) + F4, ("count", "<i4"), ("id", "<i4")])
+                         ("sep",) + F4, ("count", "<i4"), ("sep_count", "<i4"), ("id", "<i4"), ("pad", "<i4")])
 SPH_RECORD = np.dtype([("tag", "<u4", 2), ("p",) + F4, ("v",) + F4, ("a",) + F4, ("rho", "<f4"), ("P", "<f4"),
                        ("id", "<i4"), ("pad", "<i4")])
-assert TEST_RECORD.itemsize == 80 and BOIDS_RECORD.itemsize == 96 and SPH_RECORD.itemsize == 72
+assert TEST_RECORD.itemsize == 80 and BOIDS_RECORD.itemsize == 104 and SPH_RECORD.itemsize == 72
 
 
 def records(dtype, p, v):
@@ -51,9 +52,12 @@ def test_contexts(radius=50.0, lo=0.0, hi=1000.0):
     return see, act
 
 
-def boids_context(r=10.0, w_sep=1.5, w_ali=1.0, w_coh=1.0, max_speed=2.0, dt=1.0):
+def boids_context(r=10.0, sep_r=None, w_sep=1.5, w_ali=1.0, w_coh=1.0, max_speed=2.0, max_force=0.03, dt=1.0):
+    """Context of the boids model: neighbour radius r, separation radius sep_r (r / 2 by
+    default), weights, max speed and max steering force, time step."""
     r = np.float32(r)
-    return np.array([r, r * r, w_sep, w_ali, w_coh, max_speed, dt, 0.0], np.float32)
+    sep_r = np.float32(r / 2 if sep_r is None else sep_r)
+    return np.array([r, r * r, sep_r * sep_r, w_sep, w_ali, w_coh, max_speed, max_force, dt, 0, 0, 0], np.float32)
 
 
 def sph_context(h=0.02, dx=0.01, rho0=1000.0, c0=20.0, alpha=0.05, dt=1e-4, g=(0.0, 0.0, -9.81),
