@@ -210,7 +210,7 @@ def run_gb300(args, rank, world, D):
 
     gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(rank)).split(",")[0] or 0) if world == 1 else rank
     setup, recs = workload()
-    api.set_tuning(use_graphs=True)
+    api.set_tuning()  # library defaults
     B = api.Batch([(setup, recs)])
     B.push()
     for _ in range(args.warmup):
@@ -227,6 +227,8 @@ def run_gb300(args, rank, world, D):
         dev_ms += ms
         pairs += p
     D.barrier()
+    B.run(1)
+    tel = B.telemetry()
     # profiled leg: per-kernel-class device time, same flush protocol, no graphs
     prof_steps = min(args.steps, 20)
     prof = [0.0] * 8
@@ -299,6 +301,8 @@ def run_gb300(args, rank, world, D):
                           "cell_table": prof[2] / prof_steps, "reorder": prof[3] / prof_steps,
                           "see_act": prof[4] / prof_steps},
             "clocks": clk,
+            "tuning": api.get_tuning(),
+            "telemetry": tel,
         }
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(setup, recs, args.cpu_steps)

@@ -90,6 +90,14 @@ unsigned long long tgpu_batch_last_pairs(const TgpuBatch *batch);
  * 4.. the model's pass kernels in program order. Returns TGPU_OK or an error. */
 int tgpu_batch_profile(TgpuBatch *batch, int steps, double *ms, int n);
 
+/* Telemetry of the last run, summed over its steps and see passes (the GPU counterpart
+ * of the reference's TAY_TELEMETRY counters, tay/space.c:50-60, tay/thread.c:137-242):
+ * out[0] candidates box-tested (broad phase; out[0] vs pairs gives the neighbour-finding
+ * efficiency), out[1] see CTAs that staged their halo in shared memory, out[2] see CTAs
+ * that read it from global memory, out[3] warps that walked their union box, out[4]
+ * warps whose lanes walked their own boxes. */
+int tgpu_batch_telemetry(const TgpuBatch *batch, unsigned long long *out, int n);
+
 /* Number of kernel classes tgpu_batch_profile reports (4 + pass kernels). */
 int tgpu_batch_kernel_classes(const TgpuBatch *batch);
 
@@ -110,10 +118,27 @@ int tgpu_batch_launches_per_step(const TgpuBatch *batch);
 const char *tgpu_batch_model(const TgpuBatch *batch);
 int tgpu_batch_program(const TgpuBatch *batch);
 
-/* Tuning knobs (0 = default): agents staged per see CTA, halo cells per see CTA,
- * cell-size multiple applied to min_part_sizes, and CUDA-graph use. Apply to batches
- * created afterwards. */
-void tgpu_set_tuning(unsigned stage_cap, unsigned stage_cells, float cell_multiple, int use_graphs);
+/* Tuning of the see kernel and the grid; applies to batches created afterwards.
+ *   stage          1: each see CTA stages its halo cells in shared memory; 0: candidates
+ *                  are read through the L1 cache (more CTAs per SM)
+ *   stage_cap      agents staged per CTA (0 = default)
+ *   stage_cells    halo cells per CTA (0 = default)
+ *   cell_multiple  grid cell edge = cell_multiple x min_part_sizes (0 = 1)
+ *   union_factor   a warp walks the union of its seers' cell boxes (one read serves all
+ *                  32 lanes) when that union is at most union_factor times the largest
+ *                  single box; otherwise each lane walks its own box (0 = default)
+ *   use_graphs     capture each step in a CUDA graph and replay it */
+typedef struct TgpuTuning {
+    int stage;
+    unsigned stage_cap;
+    unsigned stage_cells;
+    float cell_multiple;
+    unsigned union_factor;
+    int use_graphs;
+} TgpuTuning;
+
+void tgpu_set_tuning(const TgpuTuning *tuning);  /* NULL restores the defaults */
+void tgpu_get_tuning(TgpuTuning *tuning);
 
 /* Resolves a func_name to its model; returns the model name or NULL. */
 const char *tgpu_model_of(const char *func_name);

@@ -84,10 +84,12 @@ TGPU_SYMBOLS = [
     ("tgpu_batch_launches_per_step", ctypes.c_int, [_VP]),
     ("tgpu_batch_model", ctypes.c_char_p, [_VP]),
     ("tgpu_batch_program", ctypes.c_int, [_VP]),
-    ("tgpu_set_tuning", None, [ctypes.c_uint, ctypes.c_uint, ctypes.c_float, ctypes.c_int]),
+    ("tgpu_set_tuning", None, [_VP]),
+    ("tgpu_get_tuning", None, [_VP]),
     ("tgpu_model_of", ctypes.c_char_p, [ctypes.c_char_p]),
     ("tgpu_batch_profile", ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
     ("tgpu_batch_kernel_classes", ctypes.c_int, [_VP]),
+    ("tgpu_batch_telemetry", ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]),
     ("tgpu_batch_flush_l2", ctypes.c_int, [_VP]),
     ("tgpu_host_alloc", _VP, [ctypes.c_ulonglong]),
     ("tgpu_host_free", None, [_VP]),
@@ -284,6 +286,14 @@ class Batch:
         self._check(self.L.tgpu_batch_profile(self.ptr, steps, ms, n), "tgpu_batch_profile")
         return list(ms)
 
+    def telemetry(self):
+        """Counters of the last run: candidates tested, pairs, staged / global CTAs,
+        union / per-lane warps."""
+        out = (ctypes.c_ulonglong * 8)()
+        self._check(self.L.tgpu_batch_telemetry(self.ptr, out, 8), "tgpu_batch_telemetry")
+        return {"candidates": out[0], "pairs": self.L.tgpu_batch_last_pairs(self.ptr), "staged_ctas": out[1],
+                "global_ctas": out[2], "union_warps": out[3], "lane_warps": out[4]}
+
     def flush_l2(self):
         self._check(self.L.tgpu_batch_flush_l2(self.ptr), "tgpu_batch_flush_l2")
 
@@ -312,5 +322,24 @@ def run_batch(states, steps):
     return r
 
 
-def set_tuning(stage_cap=0, stage_cells=0, cell_multiple=1.0, use_graphs=True):
-    lib().tgpu_set_tuning(stage_cap, stage_cells, cell_multiple, 1 if use_graphs else 0)
+class TgpuTuning(ctypes.Structure):
+    _fields_ = [("stage", ctypes.c_int), ("stage_cap", ctypes.c_uint), ("stage_cells", ctypes.c_uint),
+                ("cell_multiple", ctypes.c_float), ("union_factor", ctypes.c_uint), ("use_graphs", ctypes.c_int)]
+
+
+def get_tuning() -> dict:
+    t = TgpuTuning()
+    lib().tgpu_get_tuning(ctypes.byref(t))
+    return {f: getattr(t, f) for f, _ in TgpuTuning._fields_}
+
+
+def set_tuning(**kw):
+    """Sets tuning fields (stage, stage_cap, stage_cells, cell_multiple, union_factor,
+    use_graphs) for batches created afterwards; no arguments restores the defaults."""
+    if not kw:
+        lib().tgpu_set_tuning(None)
+        return
+    cur = get_tuning()
+    cur.update(kw)
+    t = TgpuTuning(**{k: (int(v) if k != "cell_multiple" else float(v)) for k, v in cur.items()})
+    lib().tgpu_set_tuning(ctypes.byref(t))

@@ -41,13 +41,17 @@ int fail(int code, const char *fmt, ...) {
             return fail(TGPU_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
     } while (0)
 
-struct Tuning {
-    unsigned stage_cap = 0;
-    unsigned stage_cells = 0;
-    float cell_multiple = 1.0f;
-    int use_graphs = 1;
-};
-Tuning g_tuning;
+TgpuTuning default_tuning() {
+    TgpuTuning t;
+    t.stage = 0;
+    t.stage_cap = 0;
+    t.stage_cells = 0;
+    t.cell_multiple = 1.0f;
+    t.union_factor = 1;
+    t.use_graphs = 1;
+    return t;
+}
+TgpuTuning g_tuning = default_tuning();
 
 const ModelDesc *model_list(int i) {
     switch (i) {
@@ -92,7 +96,7 @@ struct KernelRun {
     char *d_see_ctx = nullptr;  // [segments * ctx_stride]
     char *d_act_ctx = nullptr;
     size_t smem = 0;
-    uint32_t stage_cap = 0, stage_cells = 0;
+    uint32_t stage_cap = 0, stage_cells = 0, union_factor = 2;
     int skip_self = 0;
 };
 
@@ -130,6 +134,8 @@ struct TgpuBatch {
     size_t table_entries = 0;
     uint32_t *d_aos = nullptr;
     unsigned long long *d_pairs = nullptr;
+    unsigned long long *d_telemetry = nullptr;  // kTelemetry counters, summed over a run
+    unsigned long long last_telemetry[8] = {};
     size_t ctx_stride = 0;
     std::vector<KernelRun> runs;
     int launches_per_step = 0;
@@ -164,6 +170,7 @@ void free_batch(TgpuBatch *b) {
     cudaFree(b->table);
     cudaFree(b->d_aos);
     cudaFree(b->d_pairs);
+    cudaFree(b->d_telemetry);
     for (auto &r : b->runs) {
         cudaFree(r.d_radii);
         cudaFree(r.d_see_ctx);
@@ -383,7 +390,9 @@ void enqueue_step(TgpuBatch *b, const StepEvents *E = nullptr) {
             S.skip_self = r.skip_self;
             S.stage_cap = r.stage_cap;
             S.stage_cells = r.stage_cells;
+            S.union_factor = r.union_factor;
             S.pairs = b->d_pairs;
+            S.telemetry = b->d_telemetry;
             S.io = io;
             r.k->launch_see(S, r.smem, st);
             for (int c = 0; c < b->m->nf4; ++c)
@@ -435,6 +444,12 @@ void advance_parity(TgpuBatch *b) {
 extern "C" {
 
 const char *tgpu_last_error(void) { return g_err.c_str(); }
+
+int tgpu_batch_telemetry(const TgpuBatch *b, unsigned long long *out, int n) {
+    if (!b || !out) return fail(TGPU_ERR_ARG, "bad telemetry");
+    for (int k = 0; k < n && k < 8; ++k) out[k] = b->last_telemetry[k];
+    return TGPU_OK;
+}
 
 int tgpu_batch_kernel_classes(const TgpuBatch *b) { return b ? 4 + (int)b->runs.size() : 0; }
 
@@ -519,11 +534,14 @@ int tgpu_device_count(void) {
     return n;
 }
 
-void tgpu_set_tuning(unsigned stage_cap, unsigned stage_cells, float cell_multiple, int use_graphs) {
-    g_tuning.stage_cap = stage_cap;
-    g_tuning.stage_cells = stage_cells;
-    g_tuning.cell_multiple = cell_multiple > 0.0f ? cell_multiple : 1.0f;
-    g_tuning.use_graphs = use_graphs;
+void tgpu_set_tuning(const TgpuTuning *t) {
+    g_tuning = t ? *t : default_tuning();
+    if (!(g_tuning.cell_multiple > 0.0f)) g_tuning.cell_multiple = 1.0f;
+    if (!g_tuning.union_factor) g_tuning.union_factor = 1;
+}
+
+void tgpu_get_tuning(TgpuTuning *t) {
+    if (t) *t = g_tuning;
 }
 
 const char *tgpu_model_of(const char *func_name) {
@@ -652,6 +670,7 @@ int tgpu_batch_create(const TgpuGroup *groups, int group_count, TgpuBatch **out)
     }
     CKB(cudaMalloc(&b->d_aos, (size_t)m->agent_bytes * n));
     CKB(cudaMalloc(&b->d_pairs, sizeof(unsigned long long)));
+    CKB(cudaMalloc(&b->d_telemetry, sizeof(unsigned long long) * 8));
 
     b->ctx_stride = (std::max(m->see_ctx_bytes, m->act_ctx_bytes) + 15u) & ~15u;
     const ProgramDesc &pd = m->programs[program];
@@ -667,10 +686,18 @@ int tgpu_batch_create(const TgpuGroup *groups, int group_count, TgpuBatch **out)
             r.skip_self = tp.self_see ? 0 : 1;
             CKB(cudaMalloc(&r.d_radii, sizeof(float4) * b->nseg));
             CKB(cudaMalloc(&r.d_see_ctx, b->ctx_stride * b->nseg));
-            const uint32_t cap_default = r.k->staged_f4 <= 1 ? 2048u : 1536u;
-            r.stage_cap = g_tuning.stage_cap ? g_tuning.stage_cap : cap_default;
-            r.stage_cells = g_tuning.stage_cells ? g_tuning.stage_cells : 1024u;
-            r.smem = (size_t)r.k->staged_f4 * r.stage_cap * sizeof(float4) + (2ull * r.stage_cells + 1) * sizeof(uint32_t);
+            const uint32_t cap_default = r.k->staged_f4 <= 1 ? 1024u : 768u;
+            r.union_factor = g_tuning.union_factor;
+            if (g_tuning.stage) {
+                r.stage_cap = g_tuning.stage_cap ? g_tuning.stage_cap : cap_default;
+                r.stage_cells = g_tuning.stage_cells ? g_tuning.stage_cells : 512u;
+                r.smem = (size_t)r.k->staged_f4 * r.stage_cap * sizeof(float4) +
+                         (2ull * r.stage_cells + 1) * sizeof(uint32_t);
+            } else {
+                r.stage_cap = 0;
+                r.stage_cells = 0;
+                r.smem = 0;
+            }
             if (r.smem > 220 * 1024) {
                 fail(TGPU_ERR_ARG, "staging buffer of %zu bytes exceeds shared memory", r.smem);
                 return bail(TGPU_ERR_ARG);
@@ -747,6 +774,7 @@ int tgpu_batch_enqueue(TgpuBatch *b, int steps) {
     int rc = prepare_specs(b);
     if (rc) return rc;
     CK(cudaMemsetAsync(b->d_pairs, 0, sizeof(unsigned long long), b->st));
+    CK(cudaMemsetAsync(b->d_telemetry, 0, sizeof(unsigned long long) * 8, b->st));
     CK(cudaEventRecord(b->e0, b->st));
     for (int i = 0; i < steps; ++i) {
         if (!b->use_graphs) {
@@ -783,6 +811,7 @@ int tgpu_batch_sync(TgpuBatch *b) {
     CK(cudaEventElapsedTime(&ms, b->e0, b->e1));
     b->last_ms = ms;
     CK(cudaMemcpy(&b->last_pairs, b->d_pairs, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(b->last_telemetry, b->d_telemetry, sizeof(b->last_telemetry), cudaMemcpyDeviceToHost));
     return TGPU_OK;
 }
 

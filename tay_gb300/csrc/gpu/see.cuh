@@ -58,6 +58,7 @@ TGPU_D bool box_hit(const float4 &a, const float4 &b, const float4 &r) {
 }
 
 struct SmemSeen {
+    static constexpr bool kGlobal = false;
     const float4 *base;
     uint32_t cap;
     TGPU_D float4 f4(int k, uint32_t j) const { return base[(uint32_t)k * cap + j]; }
@@ -65,6 +66,7 @@ struct SmemSeen {
 
 template <int N>
 struct GlobalSeen {
+    static constexpr bool kGlobal = true;
     const float4 *s[N];
     TGPU_D float4 f4(int k, uint32_t j) const { return __ldg(s[k] + j); }
 };
@@ -82,6 +84,70 @@ TGPU_D float grid_pad(const Grid &g, const SegmentSpec &s, const BoxAcc &b) {
     }
     float ulp = m * 1.1920929e-7f;  // 2^-23
     return fmaxf(1.0f / 512.0f, 16.0f * ulp / csmin + 1024.0f * 4.0f * 1.1920929e-7f);
+}
+
+// Loads a candidate position from shared memory (staged) or through the read-only cache.
+TGPU_D float4 load_pos(const float4 *src, uint32_t j, bool global) {
+    return global ? __ldg(src + j) : src[j];
+}
+
+// Union walk over candidates [j0, j1) of `src`: batches of up to 32, a box-test phase
+// into per-lane hit masks (all lanes read the same candidate), then a see phase in which
+// every lane with hits runs the see function on its next hit.
+template <class P, class Acc>
+TGPU_D void union_batches(typename P::Seer &s, const float4 &sp, const float4 &r4, bool active, uint32_t j0,
+                          uint32_t j1, uint32_t self, const float4 *src, const Acc &acc,
+                          const typename P::SeeCtx &sctx, uint32_t &pairs, uint32_t &tested) {
+    constexpr bool kGlobal = Acc::kGlobal;
+    for (uint32_t jb = j0; jb < j1; jb += 32) {
+        const uint32_t nb = min(32u, j1 - jb);
+        if (active) tested += nb;
+        uint32_t hits = 0;
+#pragma unroll 8
+        for (uint32_t k = 0; k < nb; ++k) {
+            const float4 bp = load_pos(src, jb + k, kGlobal);
+            hits |= (uint32_t)(box_hit(sp, bp, r4) && jb + k != self) << k;
+        }
+        if (!active) hits = 0;
+        pairs += __popc(hits);
+        while (__any_sync(0xffffffffu, hits != 0)) {
+            if (hits) {
+                const uint32_t j = jb + (uint32_t)(__ffs(hits) - 1);
+                hits &= hits - 1u;
+                P::see(s, sp, load_pos(src, j, kGlobal), acc, j, sctx);
+            }
+        }
+    }
+}
+
+// Per-lane walk over candidates [j0, j1): two candidates per iteration for independent
+// loads in flight.
+template <class P, class Acc>
+TGPU_D void lane_run(typename P::Seer &s, const float4 &sp, const float4 &r4, uint32_t j0, uint32_t j1, uint32_t self,
+                     const float4 *src, const Acc &acc, const typename P::SeeCtx &sctx, uint32_t &pairs,
+                     uint32_t &tested) {
+    constexpr bool kGlobal = Acc::kGlobal;
+    tested += j1 - j0;
+    uint32_t j = j0;
+    for (; j + 1 < j1; j += 2) {
+        const float4 b0 = load_pos(src, j, kGlobal);
+        const float4 b1 = load_pos(src, j + 1, kGlobal);
+        if (j != self && box_hit(sp, b0, r4)) {
+            ++pairs;
+            P::see(s, sp, b0, acc, j, sctx);
+        }
+        if (j + 1 != self && box_hit(sp, b1, r4)) {
+            ++pairs;
+            P::see(s, sp, b1, acc, j + 1, sctx);
+        }
+    }
+    if (j < j1) {
+        const float4 b0 = load_pos(src, j, kGlobal);
+        if (j != self && box_hit(sp, b0, r4)) {
+            ++pairs;
+            P::see(s, sp, b0, acc, j, sctx);
+        }
+    }
 }
 
 }  // namespace see_detail
@@ -142,7 +208,7 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
     const int H0x = hbox[0], H0y = hbox[1], H0z = hbox[2];
     const int hx = hbox[3] - H0x + 1, hy = hbox[4] - H0y + 1, hz = hbox[5] - H0z + 1;
     const long long V = (hx > 0 && hy > 0 && hz > 0) ? (long long)hx * hy * hz : 0;
-    bool staged = V > 0 && V <= (long long)L.stage_cells;
+    bool staged = L.stage_cap > 0 && V > 0 && V <= (long long)L.stage_cells;
     const uint2 *table = L.table + S.table_base;
     const uint32_t dx0 = (uint32_t)g.dims[0], dy0 = (uint32_t)g.dims[1];
 
@@ -210,13 +276,16 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
     const int wl0 = warp_min_i(lo[0]), wl1 = warp_min_i(lo[1]), wl2 = warp_min_i(lo[2]);
     const int wh0 = warp_max_i(hi[0]), wh1 = warp_max_i(hi[1]), wh2 = warp_max_i(hi[2]);
     uint32_t pairs = 0;
+    uint32_t tested = 0;
+    if (L.telemetry && threadIdx.x == 0) atomicAdd(L.telemetry + (staged ? 1 : 2), 1ull);
     if (wl0 <= wh0) {
         // A warp walks the union of its lanes' cell boxes (one broadcast read serves all
         // 32 lanes) when the union is compact; when its seers are spread out, as in sparse
         // regions, each lane walks its own box instead.
         const int lane_vol = active ? max(0, hi[0] - lo[0] + 1) * max(0, hi[1] - lo[1] + 1) * max(0, hi[2] - lo[2] + 1) : 0;
         const long long union_vol = (long long)(wh0 - wl0 + 1) * (wh1 - wl1 + 1) * (wh2 - wl2 + 1);
-        const bool union_mode = union_vol <= 2LL * warp_max_i(lane_vol);
+        const bool union_mode = union_vol <= (long long)L.union_factor * warp_max_i(lane_vol);
+        if (L.telemetry && lane == 0) atomicAdd(L.telemetry + (union_mode ? 3 : 4), 1ull);
         if (staged) {
             uint32_t self_slot = 0xFFFFFFFFu;
             if (active && L.skip_self) {
@@ -229,50 +298,59 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
                 }
             }
             const SmemSeen acc{stage, L.stage_cap};
-            // the rows this lane walks: the warp's union box, or the lane's own box
-            const int z0 = union_mode ? wl2 : lo[2], z1 = union_mode ? wh2 : hi[2];
-            const int y0 = union_mode ? wl1 : lo[1], y1 = union_mode ? wh1 : hi[1];
-            const int x0 = union_mode ? wl0 : lo[0], x1 = union_mode ? wh0 : hi[0];
-            if (union_mode || active) {
-                for (int z = z0; z <= z1; ++z)
-                    for (int y = y0; y <= y1; ++y) {
+            if (union_mode) {
+                // Two phases per batch of up to 32 staged agents: every lane box-tests
+                // its seer against the batch (broadcast reads) into a hit mask, then the
+                // lanes run the see function over their own hits together.
+                for (int z = wl2; z <= wh2; ++z)
+                    for (int y = wl1; y <= wh1; ++y) {
                         const uint32_t row = ((uint32_t)(z - H0z) * (uint32_t)hy + (uint32_t)(y - H0y)) * (uint32_t)hx;
-                        const uint32_t j0 = cell_off[row + (uint32_t)(x0 - H0x)];
-                        const uint32_t j1 = cell_off[row + (uint32_t)(x1 - H0x) + 1];
-#pragma unroll 4
-                        for (uint32_t j = j0; j < j1; ++j) {
-                            const float4 bp = stage[j];
-                            if (active && j != self_slot && box_hit(sp, bp, r4)) {
-                                ++pairs;
-                                P::see(s, sp, bp, acc, j, sctx);
-                            }
-                        }
+                        const uint32_t j0 = cell_off[row + (uint32_t)(wl0 - H0x)];
+                        const uint32_t j1 = cell_off[row + (uint32_t)(wh0 - H0x) + 1];
+                        union_batches<P>(s, sp, r4, active, j0, j1, self_slot, stage, acc, sctx, pairs, tested);
+                    }
+            } else if (active) {
+                for (int z = lo[2]; z <= hi[2]; ++z)
+                    for (int y = lo[1]; y <= hi[1]; ++y) {
+                        const uint32_t row = ((uint32_t)(z - H0z) * (uint32_t)hy + (uint32_t)(y - H0y)) * (uint32_t)hx;
+                        const uint32_t j0 = cell_off[row + (uint32_t)(lo[0] - H0x)];
+                        const uint32_t j1 = cell_off[row + (uint32_t)(hi[0] - H0x) + 1];
+                        lane_run<P>(s, sp, r4, j0, j1, self_slot, stage, acc, sctx, pairs, tested);
                     }
             }
-        } else if (active) {
+        } else {
             GlobalSeen<P::kSeenF4> acc;
 #pragma unroll
             for (int k = 0; k < P::kSeenF4; ++k) acc.s[k] = L.io.in_f4[P::seen_stream(k)];
             const float4 *pos = L.io.in_f4[0];
-            const uint32_t self = L.skip_self ? i : 0xFFFFFFFFu;
-            for (int z = lo[2]; z <= hi[2]; ++z)
-                for (int y = lo[1]; y <= hi[1]; ++y)
-                    for (int x = lo[0]; x <= hi[0]; ++x) {
-                        const uint2 e = table[((uint32_t)z * dy0 + (uint32_t)y) * dx0 + (uint32_t)x];
-                        for (uint32_t b = e.x; b < e.y; ++b) {
-                            const float4 bp = __ldg(pos + b);
-                            if (b != self && box_hit(sp, bp, r4)) {
-                                ++pairs;
-                                P::see(s, sp, bp, acc, b, sctx);
-                            }
+            const uint32_t self = (active && L.skip_self) ? i : 0xFFFFFFFFu;
+            if (union_mode) {
+                // same two-phase walk over the union box, cell by cell from the table:
+                // every lane reads the same address, which L1 serves once for the warp
+                for (int z = wl2; z <= wh2; ++z)
+                    for (int y = wl1; y <= wh1; ++y)
+                        for (int x = wl0; x <= wh0; ++x) {
+                            const uint2 e = table[((uint32_t)z * dy0 + (uint32_t)y) * dx0 + (uint32_t)x];
+                            union_batches<P>(s, sp, r4, active, e.x, e.y, self, pos, acc, sctx, pairs, tested);
                         }
-                    }
+            } else if (active) {
+                for (int z = lo[2]; z <= hi[2]; ++z)
+                    for (int y = lo[1]; y <= hi[1]; ++y)
+                        for (int x = lo[0]; x <= hi[0]; ++x) {
+                            const uint2 e = table[((uint32_t)z * dy0 + (uint32_t)y) * dx0 + (uint32_t)x];
+                            lane_run<P>(s, sp, r4, e.x, e.y, self, pos, acc, sctx, pairs, tested);
+                        }
+            }
         }
     }
     if (active) P::finish(s, sp, L.io, i, sctx, actx);
     if (L.pairs) {
         uint32_t w = warp_sum_u(pairs);
         if (lane == 0 && w) atomicAdd(L.pairs, (unsigned long long)w);
+    }
+    if (L.telemetry) {
+        uint32_t w = warp_sum_u(tested);
+        if (lane == 0 && w) atomicAdd(L.telemetry, (unsigned long long)w);
     }
 }
 

@@ -51,9 +51,15 @@ struct SeeLaunch {
     uint32_t act_ctx_stride;
     uint32_t ctas;
     int skip_self;            // same group and !self_see: a seer never sees itself
-    uint32_t stage_cap;       // staged agents per CTA
+    uint32_t stage_cap;       // staged agents per CTA (0: no staging, read through L1)
     uint32_t stage_cells;     // halo cells per CTA
+    uint32_t union_factor;    // a warp walks its union box when union <= factor x lane box
     unsigned long long *pairs;  // box-test passes, summed over the launch
+    // telemetry (the reference's TAY_TELEMETRY counters, tay/space.c:50-60, plus the
+    // kernel's own paths): [0] candidates box-tested (broad phase), [1] staged CTAs,
+    // [2] CTAs that read the halo from global memory, [3] warps that walked the union
+    // box, [4] warps whose lanes walked their own boxes
+    unsigned long long *telemetry;
     PassIO io;
 };
 
