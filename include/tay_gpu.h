@@ -140,6 +140,32 @@ typedef struct TgpuTuning {
 void tgpu_set_tuning(const TgpuTuning *tuning);  /* NULL restores the defaults */
 void tgpu_get_tuning(TgpuTuning *tuning);
 
+/* Allocation-free neighbour pass.  No counterpart in the reference: it exists for callers
+ * that cannot call cudaMalloc when they need the pass - hosts whose memory manager owns
+ * the whole device heap (a framework's caching allocator, a fixed per-process budget),
+ * plugins that may not allocate after initialisation, and latency-sensitive loops that
+ * cannot afford cudaMalloc's implicit synchronisation.
+ *
+ * Runs the test model's see pass ("agent_see": per agent, the sum of b.p - a.p over the
+ * other agents inside the per-axis radii, and their count) on `n` float4 positions that
+ * are already in device memory, and writes one float4 per agent to the device buffer
+ * `out`, in the input order: x, y, z = the sum, w = the count as int bits.  radii and
+ * min_part_sizes are 4 host floats each.  All intermediate buffers live in one fixed
+ * array (about 5 MB) of the library's own device memory, which every GPU that loads the
+ * library holds until the process exits; no device memory is allocated.
+ *   - n must not exceed tgpu_noalloc_max_agents() (65536); larger calls fail with
+ *     TGPU_ERR_ARG and a message from tgpu_noalloc_last_error();
+ *   - the array is shared by every call and keeps the last call's contents (each call
+ *     clears what must start at zero); calls whose work overlaps on the GPU race;
+ *   - the first call on a device looks up the array's device address with that device
+ *     current; make that first call before any stream capture;
+ *   - work is enqueued on `stream` (a cudaStream_t, NULL for the default stream) and the
+ *     call returns once it has finished. */
+int tgpu_see_noalloc(const float *positions, unsigned n, const float *radii, const float *min_part_sizes,
+                     float *out, void *stream);
+unsigned tgpu_noalloc_max_agents(void);
+const char *tgpu_noalloc_last_error(void);
+
 /* Resolves a func_name to its model; returns the model name or NULL. */
 const char *tgpu_model_of(const char *func_name);
 

@@ -28,6 +28,7 @@ CU_SOURCES = [
     "gpu/model_test_basic.cu",
     "gpu/model_boids.cu",
     "gpu/model_sph.cu",
+    "gpu/noalloc.cu",
 ]
 C_SOURCES = [
     "host/tay_state.c",

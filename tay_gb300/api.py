@@ -93,6 +93,10 @@ TGPU_SYMBOLS = [
     ("tgpu_batch_flush_l2", ctypes.c_int, [_VP]),
     ("tgpu_host_alloc", _VP, [ctypes.c_ulonglong]),
     ("tgpu_host_free", None, [_VP]),
+    ("tgpu_see_noalloc", ctypes.c_int, [_VP, ctypes.c_uint, ctypes.POINTER(ctypes.c_float),
+                                         ctypes.POINTER(ctypes.c_float), _VP, _VP]),
+    ("tgpu_noalloc_max_agents", ctypes.c_uint, []),
+    ("tgpu_noalloc_last_error", ctypes.c_char_p, []),
     ("tgpu_device_count", ctypes.c_int, []),
     ("tgpu_last_error", ctypes.c_char_p, []),
 ]
