@@ -22,9 +22,16 @@
 
 #ifndef REAL
 #define REAL float
+#pragma pack(pop)
+
 #endif
 
 #define O_SQRT(x) ((REAL)sqrt((double)(x)))
+
+/* Records are packed, like the reference's agents (test/agent.h:2, __attribute__((packed))),
+ * so the FP64 build has no alignment padding either and Python can describe every record
+ * with a packed dtype. */
+#pragma pack(push, 1)
 
 typedef struct {
     unsigned part_i;
@@ -356,5 +363,7 @@ static inline void o_sph_integrate(void *va, void *vc) {
     a->a[1] = 0;
     a->a[2] = 0;
 }
+
+#pragma pack(pop)
 
 #endif

@@ -28,6 +28,7 @@ TayRunner runner;
 typedef struct {
     pthread_t handle;
     int index;
+    unsigned long long start_generation; /* generation current when the worker was created */
 } RefWorker;
 
 static RefWorker workers[TAY_MAX_THREADS];
@@ -40,7 +41,7 @@ static int pool_remaining = 0;
 static void *worker_main(void *arg) {
     RefWorker *w = (RefWorker *)arg;
     TayThread *t = runner.threads + w->index;
-    unsigned long long seen = 0;
+    unsigned long long seen = w->start_generation;
     for (;;) {
         pthread_mutex_lock(&pool_lock);
         while (pool_generation == seen)
@@ -91,6 +92,7 @@ void tay_threads_start(unsigned threads_count, unsigned thread_storage_size) {
         t->context.storage = calloc(1, thread_storage_size ? thread_storage_size : 1);
         t->context.storage_size = thread_storage_size;
         workers[i].index = (int)i;
+        workers[i].start_generation = pool_generation;
         pthread_create(&workers[i].handle, 0, worker_main, workers + i);
     }
     runner.state = TAY_RUNNER_WAITING;

@@ -75,12 +75,13 @@ static struct {
 
 typedef struct {
     int index;
+    unsigned long long start_generation; /* generation current when the worker was created */
 } OWorkerArg;
 static OWorkerArg O_NAME(worker_args)[64];
 
 static void *O_NAME(worker)(void *varg) {
     int index = ((OWorkerArg *)varg)->index;
-    unsigned long long seen = 0;
+    unsigned long long seen = ((OWorkerArg *)varg)->start_generation;
     for (;;) {
         pthread_mutex_lock(&POOL.lock);
         while (POOL.generation == seen)
@@ -136,6 +137,7 @@ static void O_NAME(pool_start)(int threads) {
     POOL.count = threads;
     for (int i = 0; i < threads; ++i) {
         O_NAME(worker_args)[i].index = i;
+        O_NAME(worker_args)[i].start_generation = POOL.generation;
         pthread_create(&POOL.handles[i], 0, O_NAME(worker), &O_NAME(worker_args)[i]);
     }
 }
@@ -250,7 +252,8 @@ static void o_z_grid_sort(OGroup *g) {
         REAL size = g->box_max[i] - g->box_min[i] + cs * (REAL)0.001;
         unsigned cells = (unsigned)O_FLOOR(size / cs);
         unsigned side_n = 0;
-        while ((1u << (side_n + 1u)) <= cells)
+        /* bounded at 30: the reference's loop never ends for extents of 2^31 cells or more */
+        while (side_n < 30u && (1u << (side_n + 1u)) <= cells)
             ++side_n;
         if (side_n > n)
             n = side_n;

@@ -1,0 +1,76 @@
+"""Generates the golden vectors in this folder by running the reference Tay library itself.
+
+    python tests/golden/make_golden.py [/path/to/reference/tay/tree]
+
+Builds the reference's own CPU path from its source tree (oracle/ref/Makefile, outputs in
+oracle/_ref/) and runs each case below through the reference's public API
+(tay_create_state ... tay_run ... tay_get_agent) on seeded inputs from
+tay_gb300.workloads.  The outputs (AoS records in id order) are stored in golden.npz with
+the inputs they came from, so the oracle restatement can be pinned against the reference
+on machines where the reference source tree is absent.
+
+Cases (small enough for CpuSimple):
+  test_see_*     test model, 1500 agents in [0,1000]^3, r = 50, see pass only, 1 step,
+                 CpuSimple / CpuGrid / CpuZGrid
+  test_full_*    same agents, see + act, 10 steps, CpuGrid / CpuZGrid
+  boids_see      2000 boids in 4 clusters, r = 10, see only, 1 step, CpuZGrid
+  boids_full     same, see + act, 5 steps, CpuZGrid
+  sph_density    6x6x6 lattice, density pass only, 1 step, CpuZGrid
+  sph_full       8x8x8 lattice, all four passes, 5 steps, CpuZGrid
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import pyoracle as O  # noqa: E402
+from tay_gb300 import workloads as W  # noqa: E402
+
+
+def cases():
+    ps = W.basic_points(1500, seed=101)
+    see, act = np.array([50, 50, 50, 0], np.float32), O.test_act_context(np.float32)
+    rec = O.make_records(O.MODEL_TEST, ps.p, ps.v)
+    for space in ("simple", "grid", "z_grid"):
+        yield f"test_see_{space}", O.MODEL_TEST, space, rec, see, act, 50.0, 50.0, 1, O.PASS_SEE0
+    for space in ("grid", "z_grid"):
+        yield f"test_full_{space}", O.MODEL_TEST, space, rec, see, act, 50.0, 50.0, 10, O.PASS_SEE0 | O.PASS_ACT0
+    bp = W.boids_points(2000, seed=102, clusters=4, side=200.0)
+    brec = O.make_records(O.MODEL_BOIDS, bp.p, bp.v)
+    bctx = O.boids_context(np.float32)
+    yield "boids_see", O.MODEL_BOIDS, "z_grid", brec, bctx, bctx, 10.0, 10.0, 1, O.PASS_SEE0
+    yield "boids_full", O.MODEL_BOIDS, "z_grid", brec, bctx, bctx, 10.0, 10.0, 5, O.PASS_SEE0 | O.PASS_ACT0
+    s6 = W.sph_dam(6, 6, 6)
+    srec6 = O.make_records(O.MODEL_SPH, s6.points.p, s6.points.v)
+    sctx = O.sph_context(np.float32)
+    yield "sph_density", O.MODEL_SPH, "z_grid", srec6, sctx, sctx, 0.04, 0.04, 1, O.PASS_SEE0
+    s8 = W.sph_dam(8, 8, 8)
+    srec8 = O.make_records(O.MODEL_SPH, s8.points.p, s8.points.v)
+    yield "sph_full", O.MODEL_SPH, "z_grid", srec8, sctx, sctx, 0.04, 0.04, 5, 15
+
+
+def main():
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    O.build_reference(ref_root)
+    ref = O.reference()
+    if ref is None:
+        raise SystemExit("the reference library did not build")
+    out = {}
+    for name, model, space, rec, see, act, radius, part, steps, mask in cases():
+        r = ref.run(model, space, rec, see, act, radius, part, steps, mask, threads=4)
+        out[f"{name}__in"] = rec
+        out[f"{name}__out"] = r.records
+        out[f"{name}__meta"] = np.array([model, O.SPACE[space], steps, mask], np.int64)
+        out[f"{name}__params"] = np.array([radius, part], np.float64)
+        out[f"{name}__see"] = see
+        out[f"{name}__act"] = act
+        print(f"{name}: {rec.shape[0]} agents, {steps} steps")
+    np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
+
+
+if __name__ == "__main__":
+    main()
