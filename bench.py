@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=3, help="steps of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--stage", type=int, default=None, help="see kernel: 1 = stage halos in shared memory")
+    ap.add_argument("--union-factor", type=int, default=None, help="see kernel: union walk threshold")
+    ap.add_argument("--cell-multiple", type=float, default=None, help="grid cell edge / min part size")
     return ap.parse_args()
 
 
@@ -210,7 +213,11 @@ def run_gb300(args, rank, world, D):
 
     gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(rank)).split(",")[0] or 0) if world == 1 else rank
     setup, recs = workload()
-    api.set_tuning()  # library defaults
+    api.set_tuning()  # library defaults, then any overrides from the command line
+    over = {k: v for k, v in (("stage", args.stage), ("union_factor", args.union_factor),
+                              ("cell_multiple", args.cell_multiple)) if v is not None}
+    if over:
+        api.set_tuning(**over)
     B = api.Batch([(setup, recs)])
     B.push()
     for _ in range(args.warmup):
