@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=3, help="steps of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batched-states", type=int, default=512, help="states of the batched leg (0 = skip)")
     ap.add_argument("--stage", type=int, default=None, help="see kernel: 1 = stage halos in shared memory")
     ap.add_argument("--union-factor", type=int, default=None, help="see kernel: union walk threshold")
     ap.add_argument("--cell-multiple", type=float, default=None, help="grid cell edge / min part size")
@@ -172,6 +173,61 @@ def workload():
 CONFIG = {"workload": "boids_1M_zgrid", "agents": N_BOIDS, "radius": RADIUS, "cell": CELL,
           "clusters": 64, "sigma": 40.0, "side": 2000.0, "weights": [1.5, 1.0, 1.0], "max_speed": 2.0, "dt": 1.0,
           "passes": ["boids_see", "boids_act"], "seed": SEED}
+
+
+def batched_workload(states):
+    """BASELINE batched boids: `states` states, N log-uniform in [1000, 65536], box side
+    (125 N)^(1/3), radius U[5, 20] (cell = radius), same boids rules."""
+    from tay_gb300 import models as M
+    from tay_gb300 import workloads as W
+
+    bb = W.batched_boids(states=states, seed=4)
+    groups = []
+    for ps, r, side in bb.states:
+        recs = M.records(M.BOIDS_RECORD, ps.p, ps.v)
+        groups.append((M.boids_setup(r=r, part=r, mb=4), recs))
+    return groups
+
+
+def batched_vs_plain(states, steps):
+    """Device-resident comparison on the same GPU: one batch of all states (one launch per
+    kernel per step) against the states run one by one (each its own batch and step)."""
+    from tay_gb300 import api
+
+    groups = batched_workload(states)
+    agents = sum(r.shape[0] for _, r in groups)
+    B = api.Batch(groups)
+    B.push()
+    B.run(2)
+    dev_ms, pairs = 0.0, 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ms, p = B.run(1)
+        dev_ms += ms
+        pairs += p
+    wall_b = (time.perf_counter() - t0) / steps
+    B.close()
+    singles = [api.Batch([g]) for g in groups]
+    for s in singles:
+        s.push()
+        s.run(1)
+    plain_steps = max(1, min(steps, 3))
+    dev_p, pairs_p = 0.0, 0
+    t0 = time.perf_counter()
+    for _ in range(plain_steps):
+        for s in singles:
+            ms, p = s.run(1)
+            dev_p += ms
+            pairs_p += p
+    wall_p = (time.perf_counter() - t0) / plain_steps
+    for s in singles:
+        s.close()
+    return {"states": states, "agents": agents, "steps": steps,
+            "batched_ms_per_step": wall_b * 1000.0, "batched_device_ms_per_step": dev_ms / steps,
+            "batched_pairs_per_s": pairs / (wall_b * steps),
+            "plain_ms_per_step": wall_p * 1000.0, "plain_device_ms_per_step": dev_p / plain_steps,
+            "plain_pairs_per_s": pairs_p / (wall_p * plain_steps),
+            "speedup": wall_p / wall_b}
 
 
 def cpu_baseline(setup, recs, steps):
@@ -311,6 +367,8 @@ def run_gb300(args, rank, world, D):
             "tuning": api.get_tuning(),
             "telemetry": tel,
         }
+        if args.batched_states > 0:
+            line["batched"] = batched_vs_plain(args.batched_states, min(args.steps, 20))
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(setup, recs, args.cpu_steps)
         print(json.dumps(line), flush=True)
