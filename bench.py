@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=3, help="steps of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batched-states", type=int, default=512, help="states of the batched leg (0 = skip)")
+    ap.add_argument("--sph", type=int, default=1, help="1 = add the 524,288-particle SPH leg")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--stage", type=int, default=None, help="see kernel: 1 = stage halos in shared memory")
     ap.add_argument("--union-factor", type=int, default=None, help="see kernel: union walk threshold")
     ap.add_argument("--cell-multiple", type=float, default=None, help="grid cell edge / min part size")
@@ -189,12 +191,14 @@ def batched_workload(states):
     return groups
 
 
-def batched_vs_plain(states, steps):
+def batched_vs_plain(states, steps, tune=True):
     """Device-resident comparison on the same GPU: one batch of all states (one launch per
     kernel per step) against the states run one by one (each its own batch and step)."""
-    from tay_gb300 import api
+    from tay_gb300 import api, autotune
 
     groups = batched_workload(states)
+    if tune:
+        autotune.autotune(groups, use_cache=False)
     agents = sum(r.shape[0] for _, r in groups)
     B = api.Batch(groups)
     B.push()
@@ -222,12 +226,43 @@ def batched_vs_plain(states, steps):
     wall_p = (time.perf_counter() - t0) / plain_steps
     for s in singles:
         s.close()
-    return {"states": states, "agents": agents, "steps": steps,
+    tuning = api.get_tuning()
+    api.set_tuning()
+    return {"tuning": tuning, "states": states, "agents": agents, "steps": steps,
             "batched_ms_per_step": wall_b * 1000.0, "batched_device_ms_per_step": dev_ms / steps,
             "batched_pairs_per_s": pairs / (wall_b * steps),
             "plain_ms_per_step": wall_p * 1000.0, "plain_device_ms_per_step": dev_p / plain_steps,
             "plain_pairs_per_s": pairs_p / (wall_p * plain_steps),
             "speedup": wall_p / wall_b}
+
+
+def sph_leg(steps, tune=True):
+    """BASELINE SPH dam break: 64x128x64 = 524,288 particles on a 0.01 lattice in a
+    2.0 x 1.5 x 0.8 tank, h 0.02 (see radius 2h), four passes per step."""
+    from tay_gb300 import api, autotune
+    from tay_gb300 import models as M
+    from tay_gb300 import workloads as W
+
+    s = W.sph_dam(64, 128, 64)
+    recs = M.records(M.SPH_RECORD, s.points.p, s.points.v)
+    setup = M.sph_setup(mb=512)
+    if tune:
+        autotune.autotune([(setup, recs)], use_cache=False)
+    B = api.Batch([(setup, recs)])
+    B.push()
+    B.run(2)
+    dev_ms, pairs = 0.0, 0
+    for _ in range(steps):
+        B.flush_l2()
+        ms, p = B.run(1)
+        dev_ms += ms
+        pairs += p
+    B.close()
+    tuning = api.get_tuning()
+    api.set_tuning()
+    return {"particles": int(recs.shape[0]), "steps": steps, "ms_per_step": dev_ms / steps,
+            "pair_interactions_per_s": pairs / (dev_ms / 1000.0), "pairs_per_step": pairs / steps,
+            "tuning": tuning}
 
 
 def cpu_baseline(setup, recs, steps):
@@ -269,11 +304,16 @@ def run_gb300(args, rank, world, D):
 
     gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(rank)).split(",")[0] or 0) if world == 1 else rank
     setup, recs = workload()
-    api.set_tuning()  # library defaults, then any overrides from the command line
+    from tay_gb300 import autotune
+
+    api.set_tuning()  # library defaults, then the autotuner's choice or command-line overrides
     over = {k: v for k, v in (("stage", args.stage), ("union_factor", args.union_factor),
                               ("cell_multiple", args.cell_multiple)) if v is not None}
+    tuned = None
     if over:
         api.set_tuning(**over)
+    elif not args.no_autotune:
+        tuned = autotune.autotune([(setup, recs)], use_cache=False)
     B = api.Batch([(setup, recs)])
     B.push()
     for _ in range(args.warmup):
@@ -365,10 +405,13 @@ def run_gb300(args, rank, world, D):
                           "see_act": prof[4] / prof_steps},
             "clocks": clk,
             "tuning": api.get_tuning(),
+            "autotune": None if tuned is None else {"trials": tuned["trials"], "ms_per_step": tuned["ms_per_step"]},
             "telemetry": tel,
         }
         if args.batched_states > 0:
-            line["batched"] = batched_vs_plain(args.batched_states, min(args.steps, 20))
+            line["batched"] = batched_vs_plain(args.batched_states, min(args.steps, 20), not args.no_autotune)
+        if args.sph:
+            line["sph"] = sph_leg(min(args.steps, 20), not args.no_autotune)
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(setup, recs, args.cpu_steps)
         print(json.dumps(line), flush=True)

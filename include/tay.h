@@ -164,6 +164,27 @@ unsigned tay_commit_agents(TayState *state, TayGroup *group, const void *records
 /* NEW: number of committed agents of a group. */
 unsigned tay_get_agent_count(TayState *state, TayGroup *group);
 
+/* NEW: differentiable SPH rollouts (the benchmark spec's hand-written adjoint; no
+ * counterpart in the reference).  tay_run_recorded advances `count` states (each one
+ * TAY_GPU_Z_GRID group running sph_density, sph_pressure, sph_force, sph_integrate) by
+ * `steps` steps like tay_run_batch, recording what the adjoint needs: with
+ * checkpoint_every = k > 0 the state of every k-th step (segments are recomputed during
+ * the backward sweep), with 0 every step.  tay_run_backward then takes dL/d(final
+ * positions) and dL/d(final velocities) and returns dL/d(initial positions), dL/d(initial
+ * velocities) and dL/d(alpha, c0) of each state's SPH context.  Per-agent arrays hold 4
+ * floats per agent, the agents of state s at rows offset(s) + id (offset(s) = the agent
+ * counts of the states before s, id = the agent's id field); dloss_dparams holds 2
+ * doubles per state.  Neighbour sets are held fixed within each step.  Returns 1 on
+ * success, 0 with the error set. */
+int tay_run_recorded(TayState **states, int count, int steps, int checkpoint_every);
+int tay_run_backward(TayState **states, int count, const float *dloss_dp, const float *dloss_dv, float *dloss_dp0,
+                     float *dloss_dv0, double *dloss_dparams);
+/* NEW: device ms of the last recorded forward and of the last backward sweep, and the
+ * device memory they held (bytes). */
+double tay_get_recorded_forward_ms(void);
+double tay_get_backward_ms(void);
+unsigned long long tay_get_adjoint_device_bytes(void);
+
 /* NEW: last error message (CUDA or device model) of this state. */
 const char *tay_get_error_message(TayState *state);
 

@@ -140,6 +140,33 @@ typedef struct TgpuTuning {
 void tgpu_set_tuning(const TgpuTuning *tuning);  /* NULL restores the defaults */
 void tgpu_get_tuning(TgpuTuning *tuning);
 
+/* Adjoint of SPH rollouts (spec: hand-written adjoint; no counterpart in the
+ * reference).  For a batch running the full SPH sequence (sph_density, sph_pressure,
+ * sph_force, sph_integrate):
+ *   tgpu_adjoint_create   prepares a rollout of `steps` steps; checkpoint_every = k > 0
+ *                         keeps the state of every k-th step and recomputes each k-step
+ *                         segment during the backward sweep; 0 records every step in
+ *                         the forward run (no recomputation, more memory);
+ *   tgpu_adjoint_forward  runs the rollout from the batch's current state;
+ *   tgpu_adjoint_backward given dL/d(final positions) and dL/d(final velocities) (host,
+ *                         float4 per agent, agents of group g at rows begin(g) + id, id =
+ *                         the record's id field), returns dL/d(initial positions),
+ *                         dL/d(initial velocities) in the same layout and dL/d(alpha, c0)
+ *                         per group (2 doubles per group).  Neighbour sets are held fixed
+ *                         within each step.  Any output pointer may be NULL. */
+typedef struct TgpuAdjoint TgpuAdjoint;
+int tgpu_adjoint_create(TgpuBatch *batch, int steps, int checkpoint_every, TgpuAdjoint **out);
+int tgpu_adjoint_forward(TgpuAdjoint *adjoint);
+int tgpu_adjoint_backward(TgpuAdjoint *adjoint, const float *dl_dpos, const float *dl_dvel, float *dpos0,
+                          float *dvel0, double *dparams);
+double tgpu_adjoint_forward_ms(const TgpuAdjoint *adjoint);
+double tgpu_adjoint_backward_ms(const TgpuAdjoint *adjoint);
+unsigned long long tgpu_adjoint_device_bytes(const TgpuAdjoint *adjoint);
+void tgpu_adjoint_destroy(TgpuAdjoint *adjoint);
+
+/* Device memory in bytes held by a batch (streams, tables, sort buffers). */
+unsigned long long tgpu_batch_device_bytes(const TgpuBatch *batch);
+
 /* Allocation-free neighbour pass.  No counterpart in the reference: it exists for callers
  * that cannot call cudaMalloc when they need the pass - hosts whose memory manager owns
  * the whole device heap (a framework's caching allocator, a fixed per-process budget),

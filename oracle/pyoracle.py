@@ -154,3 +154,27 @@ def reference():
             return None
         _ref = _Impl(REF_SO, {np.float32: ("ref_run", ctypes.c_float)})
     return _ref
+
+
+def sph_adjoint_f64(x0, v0, ctx64, steps, dl_dx=None, dl_dv=None):
+    """FP64 CPU adjoint of an SPH rollout (oracle/sph_adjoint.c), all pairs.
+    x0, v0, dl_dx, dl_dv: [n, 3]; ctx64: sph_context(np.float64, ...).  Returns
+    dict(dx0, dv0, dalpha, dc0, x_final, v_final)."""
+    lib = port().lib
+    fn = lib.oracle_sph_adjoint_f64
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 3 + [ctypes.c_int] + [ctypes.c_void_p] * 7
+    n = x0.shape[0]
+    x0 = np.ascontiguousarray(x0[:, :3], np.float64)
+    v0 = np.ascontiguousarray(v0[:, :3], np.float64)
+    gx = np.zeros((n, 3)) if dl_dx is None else np.ascontiguousarray(dl_dx[:, :3], np.float64)
+    gv = np.zeros((n, 3)) if dl_dv is None else np.ascontiguousarray(dl_dv[:, :3], np.float64)
+    c = np.ascontiguousarray(ctx64, np.float64)
+    dx0, dv0 = np.zeros((n, 3)), np.zeros((n, 3))
+    xf, vf = np.zeros((n, 3)), np.zeros((n, 3))
+    th = np.zeros(2)
+    r = fn(n, x0.ctypes.data, v0.ctypes.data, c.ctypes.data, steps, gx.ctypes.data, gv.ctypes.data, dx0.ctypes.data,
+           dv0.ctypes.data, th.ctypes.data, xf.ctypes.data, vf.ctypes.data)
+    if r != steps:
+        raise RuntimeError("oracle_sph_adjoint_f64 failed")
+    return {"dx0": dx0, "dv0": dv0, "dalpha": th[0], "dc0": th[1], "x_final": xf, "v_final": vf}

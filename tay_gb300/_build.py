@@ -29,6 +29,7 @@ CU_SOURCES = [
     "gpu/model_boids.cu",
     "gpu/model_sph.cu",
     "gpu/noalloc.cu",
+    "gpu/adjoint.cu",
 ]
 C_SOURCES = [
     "host/tay_state.c",

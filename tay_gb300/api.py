@@ -69,6 +69,11 @@ TAY_SYMBOLS = [
     ("tay_commit_agents", ctypes.c_uint, [_VP, _VP, _VP, ctypes.c_uint]),
     ("tay_get_agent_count", ctypes.c_uint, [_VP, _VP]),
     ("tay_get_error_message", ctypes.c_char_p, [_VP]),
+    ("tay_run_recorded", ctypes.c_int, [ctypes.POINTER(_VP), ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    ("tay_run_backward", ctypes.c_int, [ctypes.POINTER(_VP), ctypes.c_int, _VP, _VP, _VP, _VP, _VP]),
+    ("tay_get_recorded_forward_ms", ctypes.c_double, []),
+    ("tay_get_backward_ms", ctypes.c_double, []),
+    ("tay_get_adjoint_device_bytes", ctypes.c_ulonglong, []),
 ]
 TGPU_SYMBOLS = [
     ("tgpu_batch_create", ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(_VP)]),
@@ -93,6 +98,14 @@ TGPU_SYMBOLS = [
     ("tgpu_batch_flush_l2", ctypes.c_int, [_VP]),
     ("tgpu_host_alloc", _VP, [ctypes.c_ulonglong]),
     ("tgpu_host_free", None, [_VP]),
+    ("tgpu_adjoint_create", ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_VP)]),
+    ("tgpu_adjoint_forward", ctypes.c_int, [_VP]),
+    ("tgpu_adjoint_backward", ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    ("tgpu_adjoint_forward_ms", ctypes.c_double, [_VP]),
+    ("tgpu_adjoint_backward_ms", ctypes.c_double, [_VP]),
+    ("tgpu_adjoint_device_bytes", ctypes.c_ulonglong, [_VP]),
+    ("tgpu_adjoint_destroy", None, [_VP]),
+    ("tgpu_batch_device_bytes", ctypes.c_ulonglong, [_VP]),
     ("tgpu_see_noalloc", ctypes.c_int, [_VP, ctypes.c_uint, ctypes.POINTER(ctypes.c_float),
                                          ctypes.POINTER(ctypes.c_float), _VP, _VP]),
     ("tgpu_noalloc_max_agents", ctypes.c_uint, []),

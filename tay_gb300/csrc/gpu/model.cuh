@@ -58,6 +58,20 @@ struct ModelDesc {
     void (*unpack)(uint32_t *aos, uint32_t n, const PassIO &io, uint32_t program, cudaStream_t st);
 };
 
+// The SPH model's adjoint kernels (used by adjoint.cu).
+struct SphAdjointKernels {
+    void (*force_record)(const SeeLaunch &L, size_t smem, cudaStream_t st);  // force + integrate, also stores a
+    cudaError_t (*force_record_prepare)(size_t smem);
+    void (*integrate_adj)(const ActLaunch &L, cudaStream_t st);
+    void (*force_adj)(const SeeLaunch &L, size_t smem, cudaStream_t st);
+    cudaError_t (*force_adj_prepare)(size_t smem);
+    void (*density_adj)(const SeeLaunch &L, size_t smem, cudaStream_t st);
+    cudaError_t (*density_adj_prepare)(size_t smem);
+    void (*scatter_adj)(const ActLaunch &L, cudaStream_t st);
+    uint32_t ctx_bytes;
+};
+const SphAdjointKernels *sph_adjoint_kernels();
+
 const ModelDesc *model_test_basic();
 const ModelDesc *model_boids();
 const ModelDesc *model_sph();

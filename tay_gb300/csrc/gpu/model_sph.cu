@@ -59,6 +59,13 @@ TGPU_D float dist2(float dx, float dy, float dz) {
     return __fadd_rn(r2, __fmul_rn(dz, dz));
 }
 
+TGPU_D float kernel_d2w(float q, float sigma, float inv_h) {
+    const float s2 = sigma * inv_h * inv_h;
+    if (q < 1.0f) return s2 * (-3.0f + 4.5f * q);
+    if (q < 2.0f) return s2 * (1.5f * (2.0f - q));
+    return 0.0f;
+}
+
 TGPU_D float pressure(float rho, const Ctx &c) {
     const float x = rho / c.rho0;
     const float x2 = x * x;
@@ -102,7 +109,7 @@ struct ForceSeer {
     float4 v;
 };
 
-template <bool kIntegrate>
+template <bool kIntegrate, bool kStoreAcc = false>
 struct Force {
     using SeeCtx = Ctx;
     using ActCtx = Ctx;
@@ -143,10 +150,8 @@ struct Force {
         }
     }
     TGPU_D static void finish(Seer &s, const float4 &a, const PassIO &io, uint32_t i, const Ctx &, const Ctx &c) {
-        if (!kIntegrate) {
-            io.out_f4[ACC][i] = make_float4(s.ax, s.ay, s.az, 0.0f);
-            return;
-        }
+        if (!kIntegrate || kStoreAcc) io.out_f4[ACC][i] = make_float4(s.ax, s.ay, s.az, 0.0f);
+        if (!kIntegrate) return;
         float p[3] = {a.x, a.y, a.z};
         float v[3] = {s.v.x, s.v.y, s.v.z};
         const float acc[3] = {s.ax, s.ay, s.az};
@@ -215,6 +220,189 @@ const ProgramDesc kPrograms[] = {
     {4, {"sph_density", "sph_pressure", "sph_force", "sph_integrate"}, 2, {1, 3}},
 };
 
+
+// ---------------------------------------------------------------- adjoint passes
+//
+// Reverse mode of one SPH step, with the neighbour sets of the forward step held fixed.
+// Streams of the adjoint (a separate PassIO, sorted order of the step being reversed):
+//   f4 [0] POS, [1] VEL, [2] RP = {rho, P}, [3] ABAR (adjoint of the acceleration),
+//   [4] XBAR, [5] VBAR (adjoints of the step's initial position and velocity),
+//   [6] RHOBAR, [7] THETA = {d/dalpha, d/dc0} per particle; u32 [0] GID (global id).
+// The force is antisymmetric, f_jk = -f_kj (same |x|, s = v.x and rho_bar for both
+// orders), so every term a particle receives from its neighbours' accelerations is a
+// gather with weight (abar_k - abar_j): the adjoint passes are see passes over the same
+// neighbours as the forward ones.
+enum { A_POS = 0, A_VEL = 1, A_RP = 2, A_ABAR = 3, A_XBAR = 4, A_VBAR = 5, A_RHOBAR = 6, A_THETA = 7 };
+enum { A_GID = 0 };
+
+// integrate (v' = v + dt (a + g), x' = x + dt v', walls) reversed; the wall test is
+// re-evaluated from the recorded state, so clamped components pass no gradient through
+// the position and -0.5 through the velocity.
+struct IntegrateAdj {
+    using ActCtx = Ctx;
+    TGPU_D static void act(const PassIO &io, uint32_t i, const Ctx &c) {
+        const uint32_t gid = io.in_u32[A_GID][i];
+        const float4 x = io.in_f4[A_POS][i], v = io.in_f4[A_VEL][i], a = io.in_f4[ACC][i];
+        const float4 xb = io.in_f4[A_XBAR][gid], vb = io.in_f4[A_VBAR][gid];  // id order
+        const float xs[3] = {x.x, x.y, x.z}, vs[3] = {v.x, v.y, v.z}, as[3] = {a.x, a.y, a.z};
+        const float xbs[3] = {xb.x, xb.y, xb.z}, vbs[3] = {vb.x, vb.y, vb.z};
+        float ybar[3], ubar[3], abar[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float u = vs[k] + c.dt * (as[k] + c.g[k]);
+            const float y = xs[k] + c.dt * u;
+            const bool clamped = (y < c.mn[k]) || (y > c.mx[k]);
+            ybar[k] = clamped ? 0.0f : xbs[k];
+            ubar[k] = clamped ? -0.5f * vbs[k] : vbs[k];
+            ubar[k] += c.dt * ybar[k];
+            abar[k] = c.dt * ubar[k];
+        }
+        io.out_f4[A_XBAR][i] = make_float4(ybar[0], ybar[1], ybar[2], 0.0f);
+        io.out_f4[A_VBAR][i] = make_float4(ubar[0], ubar[1], ubar[2], 0.0f);
+        io.out_f4[A_ABAR][i] = make_float4(abar[0], abar[1], abar[2], 0.0f);
+    }
+};
+
+struct ForceAdjSeer {
+    float4 v, ab;
+    float rho, P;
+    float xb[3], vb[3];
+    float rhob, Pb, ta, tc;
+};
+
+// force adjoint: for each neighbour j, with d = x_k - x_j, w = abar_k - abar_j and
+// f_kj = c d, c = -m (A_k + A_j + Pi) D(r), D = W'(r)/r:
+//   xbar_k += c w + (w.d) dc/dx_k,  vbar_k += (w.d) dc/dv_k,
+//   rhobar_k += (w.d) dc/drho_k,    Pbar_k += (w.d) dc/dP_k,
+//   theta += (abar_k.d) dc/d(alpha, c0)
+// then the pressure adjoint: rhobar_k += Pbar_k dP/drho, dL/dc0 += Pbar_k 2 P_k / c0.
+struct ForceAdj {
+    using SeeCtx = Ctx;
+    using ActCtx = Ctx;
+    using Seer = ForceAdjSeer;
+    static constexpr int kSeenF4 = 4;
+    TGPU_D static int seen_stream(int k) { return k == 0 ? A_POS : (k == 1 ? A_VEL : (k == 2 ? A_RP : A_ABAR)); }
+    TGPU_D static void load(Seer &s, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {
+        s.v = io.in_f4[A_VEL][i];
+        s.ab = io.in_f4[A_ABAR][i];
+        const float4 rp = io.in_f4[A_RP][i];
+        s.rho = rp.x;
+        s.P = rp.y;
+        s.xb[0] = s.xb[1] = s.xb[2] = 0.0f;
+        s.vb[0] = s.vb[1] = s.vb[2] = 0.0f;
+        s.rhob = s.Pb = s.ta = s.tc = 0.0f;
+    }
+    template <class Acc>
+    TGPU_D static void see(Seer &s, const float4 &a, const float4 &b, const Acc &acc, uint32_t j, const Ctx &c) {
+        const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+        const float r2 = dist2(dx, dy, dz);
+        if (!(r2 < c.support2 && r2 > 0.0f)) return;
+        const float4 bv = acc.f4(1, j), brp = acc.f4(2, j), bab = acc.f4(3, j);
+        const float r = __fsqrt_rn(r2);
+        const float q = r * c.inv_h;
+        const float dw = kernel_dw(q, c.sigma, c.inv_h);
+        const float d2w = kernel_d2w(q, c.sigma, c.inv_h);
+        const float D = dw / r;
+        const float Dp = (d2w * r - dw) / r2;  // dD/dr
+        const float vx = s.v.x - bv.x, vy = s.v.y - bv.y, vz = s.v.z - bv.z;
+        const float sv = (vx * dx + vy * dy) + vz * dz;
+        const float rho_bar = 0.5f * (s.rho + brp.x);
+        const float den = r2 + c.eta2;
+        float Pi = 0.0f, Pi_s = 0.0f, Pi_r2 = 0.0f, Pi_rb = 0.0f, Pi_al = 0.0f, Pi_c0 = 0.0f;
+        if (sv < 0.0f) {
+            const float k0 = c.h / (den * rho_bar);
+            Pi_al = -c.c0 * k0 * sv;
+            Pi_c0 = -c.alpha * k0 * sv;
+            Pi = c.alpha * Pi_al;
+            Pi_s = -c.alpha * c.c0 * k0;
+            Pi_r2 = -Pi / den;
+            Pi_rb = -Pi / rho_bar;
+        }
+        const float Ak = s.P / (s.rho * s.rho), Aj = brp.y / (brp.x * brp.x);
+        const float T = (Ak + Aj) + Pi;
+        const float cc = -c.m * T * D;
+        const float wx = s.ab.x - bab.x, wy = s.ab.y - bab.y, wz = s.ab.z - bab.z;
+        const float xw = (dx * wx + dy * wy) + dz * wz;
+        const float coef_d = -c.m * (2.0f * Pi_r2 * D + T * Dp / r);
+        const float coef_v = -c.m * D * Pi_s;
+        s.xb[0] += cc * wx + xw * (coef_v * vx + coef_d * dx);
+        s.xb[1] += cc * wy + xw * (coef_v * vy + coef_d * dy);
+        s.xb[2] += cc * wz + xw * (coef_v * vz + coef_d * dz);
+        s.vb[0] += xw * coef_v * dx;
+        s.vb[1] += xw * coef_v * dy;
+        s.vb[2] += xw * coef_v * dz;
+        s.rhob += xw * (-c.m * D) * (-2.0f * s.P / (s.rho * s.rho * s.rho) + 0.5f * Pi_rb);
+        s.Pb += xw * (-c.m * D / (s.rho * s.rho));
+        const float ad = (s.ab.x * dx + s.ab.y * dy) + s.ab.z * dz;
+        s.ta += ad * (-c.m * D * Pi_al);
+        s.tc += ad * (-c.m * D * Pi_c0);
+    }
+    TGPU_D static void finish(Seer &s, const float4 &, const PassIO &io, uint32_t i, const Ctx &c, const Ctx &) {
+        const float x = s.rho / c.rho0;
+        const float x2 = x * x;
+        const float x6 = (x2 * x2) * x2;
+        s.rhob += s.Pb * (c.B * 7.0f * x6 / c.rho0);
+        s.tc += s.Pb * (2.0f * s.P / c.c0);
+        io.out_f4[A_RHOBAR][i] = make_float4(s.rhob, 0.0f, 0.0f, 0.0f);
+        const float4 xb = io.in_f4[A_XBAR][i], vb = io.in_f4[A_VBAR][i];
+        io.out_f4[A_XBAR][i] = make_float4(xb.x + s.xb[0], xb.y + s.xb[1], xb.z + s.xb[2], 0.0f);
+        io.out_f4[A_VBAR][i] = make_float4(vb.x + s.vb[0], vb.y + s.vb[1], vb.z + s.vb[2], 0.0f);
+        io.out_f4[A_THETA][i] = make_float4(s.ta, s.tc, 0.0f, 0.0f);
+    }
+};
+
+struct DensityAdjSeer {
+    float rhob;
+    float xb[3];
+};
+
+// density adjoint: xbar_k += sum_j (rhobar_k + rhobar_j) m W'(r) d / r
+struct DensityAdj {
+    using SeeCtx = Ctx;
+    using ActCtx = Ctx;
+    using Seer = DensityAdjSeer;
+    static constexpr int kSeenF4 = 2;
+    TGPU_D static int seen_stream(int k) { return k == 0 ? A_POS : A_RHOBAR; }
+    TGPU_D static void load(Seer &s, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {
+        s.rhob = io.in_f4[A_RHOBAR][i].x;
+        s.xb[0] = s.xb[1] = s.xb[2] = 0.0f;
+    }
+    template <class Acc>
+    TGPU_D static void see(Seer &s, const float4 &a, const float4 &b, const Acc &acc, uint32_t j, const Ctx &c) {
+        const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+        const float r2 = dist2(dx, dy, dz);
+        if (!(r2 < c.support2 && r2 > 0.0f)) return;
+        const float r = __fsqrt_rn(r2);
+        const float g = (s.rhob + acc.f4(1, j).x) * c.m * kernel_dw(r * c.inv_h, c.sigma, c.inv_h) / r;
+        s.xb[0] += g * dx;
+        s.xb[1] += g * dy;
+        s.xb[2] += g * dz;
+    }
+    TGPU_D static void finish(Seer &s, const float4 &, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {
+        const float4 xb = io.in_f4[A_XBAR][i];
+        io.out_f4[A_XBAR][i] = make_float4(xb.x + s.xb[0], xb.y + s.xb[1], xb.z + s.xb[2], 0.0f);
+    }
+};
+
+// adjoints of the step's initial state back to id order (the order of the step before)
+struct ScatterAdj {
+    using ActCtx = Ctx;
+    TGPU_D static void act(const PassIO &io, uint32_t i, const Ctx &) {
+        const uint32_t gid = io.in_u32[A_GID][i];
+        io.out_f4[A_XBAR][gid] = io.in_f4[A_XBAR][i];
+        io.out_f4[A_VBAR][gid] = io.in_f4[A_VBAR][i];
+    }
+};
+
+const SphAdjointKernels kAdjoint = {
+    launch_see_t<Force<true, true>>, prepare_see_t<Force<true, true>>,
+    launch_act_t<IntegrateAdj>,
+    launch_see_t<ForceAdj>, prepare_see_t<ForceAdj>,
+    launch_see_t<DensityAdj>, prepare_see_t<DensityAdj>,
+    launch_act_t<ScatterAdj>,
+    (uint32_t)sizeof(Ctx),
+};
+
 const ModelDesc kModel = {
     "sph", 72, 4, 1, {kState, kState, kStep, kStep}, {kState}, (uint32_t)sizeof(Ctx), (uint32_t)sizeof(Ctx),
     kKernels, 4, kPrograms, 4, pack_t<Codec>, unpack_t<Codec>,
@@ -223,5 +411,6 @@ const ModelDesc kModel = {
 }  // namespace sph
 
 const ModelDesc *model_sph() { return &sph::kModel; }
+const SphAdjointKernels *sph_adjoint_kernels() { return &sph::kAdjoint; }
 
 }  // namespace tgpu

@@ -15,14 +15,13 @@
 #include <string>
 #include <vector>
 
-#include "model.cuh"
-#include "tay_gpu.h"
-
-using namespace tgpu;
+#include "runtime_internal.cuh"
 
 namespace {
-
 thread_local std::string g_err;
+}  // namespace
+
+namespace tgpu {
 
 int fail(int code, const char *fmt, ...) {
     char buf[512];
@@ -33,6 +32,10 @@ int fail(int code, const char *fmt, ...) {
     g_err = buf;
     return code;
 }
+
+}  // namespace tgpu
+
+namespace {
 
 #define CK(call)                                                                                          \
     do {                                                                                                  \
@@ -88,65 +91,7 @@ uint32_t log2u(uint32_t v) {
     return n;
 }
 
-struct KernelRun {
-    const KernelDesc *k;
-    int see_pass;  // index into the group's pass list, or -1
-    int act_pass;
-    float4 *d_radii = nullptr;  // [segments]
-    char *d_see_ctx = nullptr;  // [segments * ctx_stride]
-    char *d_act_ctx = nullptr;
-    size_t smem = 0;
-    uint32_t stage_cap = 0, stage_cells = 0, union_factor = 2;
-    int skip_self = 0;
-};
-
-struct HostSeg {
-    TgpuGroup g;
-    std::vector<TgpuPass> passes;
-    float host_min[3], host_max[3];
-    bool pushed = false;
-};
-
 }  // namespace
-
-struct TgpuBatch {
-    const ModelDesc *m = nullptr;
-    int program = -1;
-    int nseg = 0;
-    uint32_t total = 0;
-    std::vector<HostSeg> hs;
-    std::vector<SegmentSpec> specs;
-    std::vector<uint32_t> tile_seg;
-    std::vector<uint2> cta;
-    uint32_t tiles = 0, ctas = 0, key_bits = 0;
-    bool specs_dirty = true;
-
-    SegmentSpec *d_specs = nullptr;
-    uint32_t *d_tile_seg = nullptr;
-    uint2 *d_cta = nullptr;
-    BoxAcc *d_box = nullptr;
-    float4 *f4[kMaxF4][2] = {};
-    uint32_t *u32[kMaxU32][2] = {};
-    int cur_f4[kMaxF4] = {};
-    int cur_u32[kMaxU32] = {};
-    uint32_t *keys[2] = {}, *vals[2] = {}, *counts = nullptr, *partials = nullptr;
-    uint2 *table = nullptr;
-    size_t table_entries = 0;
-    uint32_t *d_aos = nullptr;
-    unsigned long long *d_pairs = nullptr;
-    unsigned long long *d_telemetry = nullptr;  // kTelemetry counters, summed over a run
-    unsigned long long last_telemetry[8] = {};
-    size_t ctx_stride = 0;
-    std::vector<KernelRun> runs;
-    int launches_per_step = 0;
-
-    cudaStream_t st = nullptr;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    double last_ms = 0.0;
-    unsigned long long last_pairs = 0;
-    bool use_graphs = true;
-    std::map<uint64_t, cudaGraphExec_t> graphs;
-};
 
 namespace {
 
@@ -228,7 +173,9 @@ int upload_contexts(TgpuBatch *b, int seg) {
 // Per-segment grid bounds from the pushed agents: each axis gets a power-of-two cell
 // budget with 10% headroom over the pushed extent (bounded to 1024, the 10-bit Morton
 // limit); the dense table gets at most shared_megabytes of uint2 entries.
-int prepare_specs(TgpuBatch *b) {
+}  // namespace
+
+int tgpu::prepare_specs(TgpuBatch *b) {
     if (!b->specs_dirty) return TGPU_OK;
     b->specs_dirty = false;
     std::vector<SegmentSpec> next = b->specs;
@@ -282,7 +229,7 @@ int prepare_specs(TgpuBatch *b) {
     return TGPU_OK;
 }
 
-PassIO make_io(TgpuBatch *b, const KernelDesc *k, bool fused_see, uint32_t offset) {
+PassIO tgpu::make_io(TgpuBatch *b, const KernelDesc *k, bool fused_see, uint32_t offset) {
     PassIO io{};
     for (int c = 0; c < b->m->nf4; ++c) {
         if (b->m->role_f4[c] == kState) {
@@ -305,7 +252,7 @@ PassIO make_io(TgpuBatch *b, const KernelDesc *k, bool fused_see, uint32_t offse
     return io;
 }
 
-SortLaunch sort_launch(TgpuBatch *b) {
+SortLaunch tgpu::sort_launch(TgpuBatch *b) {
     SortLaunch L{};
     L.specs = b->d_specs;
     L.tile_seg = b->d_tile_seg;
@@ -324,19 +271,15 @@ SortLaunch sort_launch(TgpuBatch *b) {
     return L;
 }
 
-// Optional per-class timing: when `ev` is given, an event is recorded before and after
-// each kernel class (ev[2k], ev[2k+1] for classes 0..3, then one pair per pass kernel;
-// the clear at the end is class 2's second half: ev2[0..1]).
-struct StepEvents {
-    cudaEvent_t *ev;   // 2 * classes
-    cudaEvent_t *ev2;  // 2 (table clear)
-};
+namespace {
 
 void mark(const StepEvents *e, int k, cudaStream_t st) {
     if (e) cudaEventRecord(e->ev[k], st);
 }
 
-void enqueue_step(TgpuBatch *b, const StepEvents *E = nullptr) {
+}  // namespace
+
+void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E) {
     if (b->total == 0 || b->tiles == 0) return;
     cudaStream_t st = b->st;
     SortLaunch L = sort_launch(b);
@@ -416,6 +359,8 @@ void enqueue_step(TgpuBatch *b, const StepEvents *E = nullptr) {
     if (E) cudaEventRecord(E->ev2[1], st);
 }
 
+namespace {
+
 uint64_t parity_signature(const TgpuBatch *b) {
     uint64_t s = 0;
     for (int c = 0; c < kMaxF4; ++c) s |= (uint64_t)b->cur_f4[c] << c;
@@ -449,6 +394,19 @@ int tgpu_batch_telemetry(const TgpuBatch *b, unsigned long long *out, int n) {
     if (!b || !out) return fail(TGPU_ERR_ARG, "bad telemetry");
     for (int k = 0; k < n && k < 8; ++k) out[k] = b->last_telemetry[k];
     return TGPU_OK;
+}
+
+unsigned long long tgpu_batch_device_bytes(const TgpuBatch *b) {
+    if (!b) return 0ull;
+    const unsigned long long n = b->total ? b->total : 1;
+    unsigned long long bytes = 0;
+    for (int c = 0; c < b->m->nf4; ++c) bytes += n * 16ull * (b->m->role_f4[c] == kState ? 2 : 1);
+    bytes += n * 4ull * 2 * b->m->nu32;
+    bytes += n * 4ull * 4;  // keys, permutation (ping-pong)
+    bytes += 256ull * 4 * (b->tiles ? b->tiles : 1);
+    bytes += b->table_entries * sizeof(uint2);
+    bytes += n * b->m->agent_bytes;
+    return bytes;
 }
 
 int tgpu_batch_kernel_classes(const TgpuBatch *b) { return b ? 4 + (int)b->runs.size() : 0; }

@@ -1,0 +1,92 @@
+// Internal view of a batch, shared by the runtime and the adjoint module.
+#pragma once
+
+#include <map>
+#include <vector>
+
+#include "model.cuh"
+#include "tay_gpu.h"
+
+namespace tgpu {
+
+struct KernelRun {
+    const KernelDesc *k;
+    int see_pass;  // index into the group's pass list, or -1
+    int act_pass;
+    float4 *d_radii = nullptr;  // [segments]
+    char *d_see_ctx = nullptr;  // [segments * ctx_stride]
+    char *d_act_ctx = nullptr;
+    size_t smem = 0;
+    uint32_t stage_cap = 0, stage_cells = 0, union_factor = 2;
+    int skip_self = 0;
+};
+
+struct HostSeg {
+    TgpuGroup g;
+    std::vector<TgpuPass> passes;
+    float host_min[3], host_max[3];
+    bool pushed = false;
+};
+
+// Optional per-class timing of one enqueued step: an event is recorded before and after
+// each kernel class (ev[2k], ev[2k+1] for classes 0..3, then one pair per pass kernel);
+// the table clear at the end is timed by ev2[0..1].
+struct StepEvents {
+    cudaEvent_t *ev;
+    cudaEvent_t *ev2;
+};
+
+}  // namespace tgpu
+
+using namespace tgpu;
+
+struct TgpuBatch {
+    const tgpu::ModelDesc *m = nullptr;
+    int program = -1;
+    int nseg = 0;
+    uint32_t total = 0;
+    std::vector<HostSeg> hs;
+    std::vector<SegmentSpec> specs;
+    std::vector<uint32_t> tile_seg;
+    std::vector<uint2> cta;
+    uint32_t tiles = 0, ctas = 0, key_bits = 0;
+    bool specs_dirty = true;
+
+    SegmentSpec *d_specs = nullptr;
+    uint32_t *d_tile_seg = nullptr;
+    uint2 *d_cta = nullptr;
+    BoxAcc *d_box = nullptr;
+    float4 *f4[kMaxF4][2] = {};
+    uint32_t *u32[kMaxU32][2] = {};
+    int cur_f4[kMaxF4] = {};
+    int cur_u32[kMaxU32] = {};
+    uint32_t *keys[2] = {}, *vals[2] = {}, *counts = nullptr, *partials = nullptr;
+    uint2 *table = nullptr;
+    size_t table_entries = 0;
+    uint32_t *d_aos = nullptr;
+    unsigned long long *d_pairs = nullptr;
+    unsigned long long *d_telemetry = nullptr;  // kTelemetry counters, summed over a run
+    unsigned long long last_telemetry[8] = {};
+    size_t ctx_stride = 0;
+    std::vector<KernelRun> runs;
+    int launches_per_step = 0;
+
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    double last_ms = 0.0;
+    unsigned long long last_pairs = 0;
+    bool use_graphs = true;
+    std::map<uint64_t, cudaGraphExec_t> graphs;
+};
+
+
+namespace tgpu {
+
+// Runtime functions the adjoint module reuses.
+int prepare_specs(TgpuBatch *b);
+void enqueue_step(TgpuBatch *b, const StepEvents *E = nullptr);
+PassIO make_io(TgpuBatch *b, const KernelDesc *k, bool fused_see, uint32_t offset);
+SortLaunch sort_launch(TgpuBatch *b);
+int fail(int code, const char *fmt, ...);
+
+}  // namespace tgpu

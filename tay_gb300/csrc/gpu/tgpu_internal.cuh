@@ -23,7 +23,7 @@
 
 namespace tgpu {
 
-constexpr int kMaxF4 = 6;   // float4 streams per model
+constexpr int kMaxF4 = 8;   // float4 streams per model
 constexpr int kMaxU32 = 2;  // u32 streams per model
 constexpr int kSortTile = 2048;       // agents per radix tile (256 threads x 8)
 constexpr int kSortThreads = 256;

@@ -386,12 +386,14 @@ int tay_run(TayState *state, int steps) {
  * is cached for the last list of states it was built for. */
 static struct {
     TgpuBatch *batch;
+    TgpuAdjoint *adjoint;
     TayState **states;
     unsigned *versions;
     int count;
 } g_batch_cache;
 
 static void drop_batch_cache(void) {
+    if (g_batch_cache.adjoint) tgpu_adjoint_destroy(g_batch_cache.adjoint);
     if (g_batch_cache.batch) tgpu_batch_destroy(g_batch_cache.batch);
     free(g_batch_cache.states);
     free(g_batch_cache.versions);
@@ -413,8 +415,8 @@ static int cache_matches(TayState **states, int count) {
     return 1;
 }
 
-int tay_run_batch(TayState **states, int count, int steps) {
-    if (!states || count <= 0) return 0;
+/* Builds (or reuses) the cached batch of `states`; returns it or NULL with errors set. */
+static TgpuBatch *batch_for(TayState **states, int count) {
     for (int i = 0; i < count; ++i) {
         if (!states[i]->is_running) {
             set_error(states[i], TAY_ERROR_STATE_STATUS, "cannot run simulation steps if simulation is not started");
@@ -443,16 +445,33 @@ int tay_run_batch(TayState **states, int count, int steps) {
             g_batch_cache.versions[i] = states[i]->version;
         }
     }
-    TgpuBatch *b = g_batch_cache.batch;
-    double t0 = now_s();
+    return g_batch_cache.batch;
+}
+
+static int push_all(TgpuBatch *b, TayState **states, int count) {
     int rc = TGPU_OK;
     for (int i = 0; i < count && rc == TGPU_OK; ++i) {
         rc = tgpu_batch_set_contexts(b, i, &states[i]->tgroup);
         if (rc == TGPU_OK) rc = tgpu_batch_push(b, i, states[i]->groups[states[i]->gpu_group].storage);
     }
-    if (rc == TGPU_OK) rc = tgpu_batch_run(b, steps);
+    return rc;
+}
+
+static int fetch_all(TgpuBatch *b, TayState **states, int count) {
+    int rc = TGPU_OK;
     for (int i = 0; i < count && rc == TGPU_OK; ++i)
         rc = tgpu_batch_fetch(b, i, states[i]->groups[states[i]->gpu_group].storage);
+    return rc;
+}
+
+int tay_run_batch(TayState **states, int count, int steps) {
+    if (!states || count <= 0) return 0;
+    TgpuBatch *b = batch_for(states, count);
+    if (!b) return 0;
+    double t0 = now_s();
+    int rc = push_all(b, states, count);
+    if (rc == TGPU_OK) rc = tgpu_batch_run(b, steps);
+    if (rc == TGPU_OK) rc = fetch_all(b, states, count);
     if (rc != TGPU_OK) {
         for (int i = 0; i < count; ++i) device_fail(states[i], rc);
         return 0;
@@ -464,6 +483,62 @@ int tay_run_batch(TayState **states, int count, int steps) {
         states[i]->pairs = tgpu_batch_last_pairs(b);
     }
     return steps;
+}
+
+int tay_run_recorded(TayState **states, int count, int steps, int checkpoint_every) {
+    if (!states || count <= 0 || steps <= 0) return 0;
+    TgpuBatch *b = batch_for(states, count);
+    if (!b) return 0;
+    if (g_batch_cache.adjoint) {
+        tgpu_adjoint_destroy(g_batch_cache.adjoint);
+        g_batch_cache.adjoint = 0;
+    }
+    double t0 = now_s();
+    int rc = push_all(b, states, count);
+    if (rc == TGPU_OK) rc = tgpu_adjoint_create(b, steps, checkpoint_every, &g_batch_cache.adjoint);
+    if (rc == TGPU_OK) rc = tgpu_adjoint_forward(g_batch_cache.adjoint);
+    if (rc == TGPU_OK) rc = fetch_all(b, states, count);
+    if (rc != TGPU_OK) {
+        for (int i = 0; i < count; ++i) device_fail(states[i], rc);
+        return 0;
+    }
+    double t = now_s() - t0;
+    for (int i = 0; i < count; ++i) {
+        states[i]->ms_per_step = t / (double)steps * 1000.0;
+        states[i]->device_ms = tgpu_adjoint_forward_ms(g_batch_cache.adjoint);
+    }
+    return 1;
+}
+
+int tay_run_backward(TayState **states, int count, const float *dloss_dp, const float *dloss_dv, float *dloss_dp0,
+                     float *dloss_dv0, double *dloss_dparams) {
+    if (!states || count <= 0) return 0;
+    if (!g_batch_cache.adjoint || !cache_matches(states, count)) {
+        for (int i = 0; i < count; ++i)
+            set_error(states[i], TAY_ERROR_STATE_STATUS, "tay_run_backward needs a tay_run_recorded of the same states");
+        return 0;
+    }
+    int rc = tgpu_adjoint_backward(g_batch_cache.adjoint, dloss_dp, dloss_dv, dloss_dp0, dloss_dv0, dloss_dparams);
+    if (rc != TGPU_OK) {
+        for (int i = 0; i < count; ++i) device_fail(states[i], rc);
+        return 0;
+    }
+    return 1;
+}
+
+double tay_get_recorded_forward_ms(void) {
+    return g_batch_cache.adjoint ? tgpu_adjoint_forward_ms(g_batch_cache.adjoint) : 0.0;
+}
+
+double tay_get_backward_ms(void) {
+    return g_batch_cache.adjoint ? tgpu_adjoint_backward_ms(g_batch_cache.adjoint) : 0.0;
+}
+
+unsigned long long tay_get_adjoint_device_bytes(void) {
+    unsigned long long bytes = 0;
+    if (g_batch_cache.batch) bytes += tgpu_batch_device_bytes(g_batch_cache.batch);
+    if (g_batch_cache.adjoint) bytes += tgpu_adjoint_device_bytes(g_batch_cache.adjoint);
+    return bytes;
 }
 
 double tay_get_ms_per_step_for_last_run(TayState *state) { return state->ms_per_step; }
