@@ -32,6 +32,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -53,6 +55,7 @@ def parse():
     ap.add_argument("--batched-states", type=int, default=512, help="states of the batched leg (0 = skip)")
     ap.add_argument("--sph", type=int, default=1, help="1 = add the 524,288-particle SPH leg")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--adjoint", type=int, default=1, help="1 = add the differentiable SPH leg")
     ap.add_argument("--stage", type=int, default=None, help="see kernel: 1 = stage halos in shared memory")
     ap.add_argument("--union-factor", type=int, default=None, help="see kernel: union walk threshold")
     ap.add_argument("--cell-multiple", type=float, default=None, help="grid cell edge / min part size")
@@ -265,6 +268,53 @@ def sph_leg(steps, tune=True):
             "tuning": tuning}
 
 
+def adjoint_leg(steps=200, every=20, instances=32, keep=1, tune=True):
+    """BASELINE differentiable SPH calibration: `instances` SPH instances of 20,480
+    particles (32x40x16 lattice, spacing 0.01, h 0.02), a `steps`-step rollout, loss = MSE
+    of final positions against a target rollout (alpha 0.08, c0 22, same initial state);
+    gradients w.r.t. (alpha, c0) and initial velocities from the adjoint with checkpoints
+    every `every` steps.  Reports forward, recorded-forward and backward device time and
+    the device memory held."""
+    from tay_gb300 import api, autotune
+    from tay_gb300 import workloads as W
+    from tay_gb300.adjoint import SphRollout
+
+    tank = (0.64, 0.6, 0.4)
+    s = W.sph_dam(32, 40, 16, tank=tank)
+    inst = [(s.points, 0.05, 20.0, (0.0, 0.0, 0.0), tank) for _ in range(instances)]
+    tgt_roll = SphRollout([(s.points, 0.08, 22.0, (0.0, 0.0, 0.0), tank) for _ in range(instances)], steps, every)
+    target, _ = tgt_roll.forward()
+    tgt_roll.close()
+    groups = SphRollout(inst, steps)._groups(np.zeros((len(inst) * s.points.n, 3), np.float32),
+                                             np.array([[0.05, 20.0]] * instances))
+    if tune:
+        autotune.autotune(groups, use_cache=False)
+    # plain forward (no recording) of the same rollout, one batch, graphs
+    plain = api.Batch(groups)
+    plain.push()
+    fwd_ms, _ = plain.run(steps)
+    plain.close()
+    roll = SphRollout(inst, steps, every, keep_segments=keep)
+    x, _ = roll.forward()
+    n = s.points.n
+    g = np.zeros_like(x)
+    loss = 0.0
+    for k in range(instances):
+        d = x[k * n:(k + 1) * n] - target[k * n:(k + 1) * n]
+        loss += float(np.mean(np.sum(d.astype(np.float64) ** 2, axis=1)))
+        g[k * n:(k + 1) * n] = 2.0 * d / n
+    dx0, dv0, dp = roll.backward(g)
+    rec_ms, bwd_ms, mem = roll.forward_ms(), roll.backward_ms(), roll.device_bytes()
+    roll.close()
+    tuning = api.get_tuning()
+    api.set_tuning()
+    return {"instances": instances, "particles_per_instance": n, "steps": steps, "checkpoint_every": every,
+            "kept_segments": keep if every else None, "tuning": tuning,
+            "forward_ms": fwd_ms, "recorded_forward_ms": rec_ms, "backward_ms": bwd_ms,
+            "fwd_plus_bwd_over_fwd": (rec_ms + bwd_ms) / fwd_ms, "device_bytes": mem, "loss": loss,
+            "dloss_dalpha_mean": float(dp[:, 0].mean()), "dloss_dc0_mean": float(dp[:, 1].mean())}
+
+
 def cpu_baseline(setup, recs, steps):
     """Oracle restatement of the reference CpuZGrid step, all host threads, `steps` steps."""
     from oracle import pyoracle as O
@@ -412,6 +462,11 @@ def run_gb300(args, rank, world, D):
             line["batched"] = batched_vs_plain(args.batched_states, min(args.steps, 20), not args.no_autotune)
         if args.sph:
             line["sph"] = sph_leg(min(args.steps, 20), not args.no_autotune)
+        if args.adjoint:
+            tune = not args.no_autotune
+            line["adjoint"] = adjoint_leg(keep=3, tune=tune)
+            line["adjoint_keep1"] = adjoint_leg(keep=1, tune=tune)
+            line["adjoint_record_all"] = adjoint_leg(every=0, tune=tune)
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(setup, recs, args.cpu_steps)
         print(json.dumps(line), flush=True)

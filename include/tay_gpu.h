@@ -145,8 +145,10 @@ void tgpu_get_tuning(TgpuTuning *tuning);
  * sph_force, sph_integrate):
  *   tgpu_adjoint_create   prepares a rollout of `steps` steps; checkpoint_every = k > 0
  *                         keeps the state of every k-th step and recomputes each k-step
- *                         segment during the backward sweep; 0 records every step in
- *                         the forward run (no recomputation, more memory);
+ *                         segment during the backward sweep, except the last
+ *                         keep_segments segments (>= 1), which the forward run records
+ *                         (k steps of records each); 0 records every step in the forward
+ *                         run (no recomputation, more memory);
  *   tgpu_adjoint_forward  runs the rollout from the batch's current state;
  *   tgpu_adjoint_backward given dL/d(final positions) and dL/d(final velocities) (host,
  *                         float4 per agent, agents of group g at rows begin(g) + id, id =
@@ -155,7 +157,7 @@ void tgpu_get_tuning(TgpuTuning *tuning);
  *                         per group (2 doubles per group).  Neighbour sets are held fixed
  *                         within each step.  Any output pointer may be NULL. */
 typedef struct TgpuAdjoint TgpuAdjoint;
-int tgpu_adjoint_create(TgpuBatch *batch, int steps, int checkpoint_every, TgpuAdjoint **out);
+int tgpu_adjoint_create(TgpuBatch *batch, int steps, int checkpoint_every, int keep_segments, TgpuAdjoint **out);
 int tgpu_adjoint_forward(TgpuAdjoint *adjoint);
 int tgpu_adjoint_backward(TgpuAdjoint *adjoint, const float *dl_dpos, const float *dl_dvel, float *dpos0,
                           float *dvel0, double *dparams);

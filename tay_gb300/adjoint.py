@@ -25,10 +25,11 @@ from . import models as M
 
 class SphRollout:
     def __init__(self, instances, steps: int, checkpoint_every: int = 0, h: float = 0.02, dx: float = 0.01,
-                 mb: int = 64):
+                 mb: int = 64, keep_segments: int = 1):
         self.L = api.lib()
         self.steps = steps
         self.every = checkpoint_every
+        self.keep = keep_segments
         self.instances = instances
         self.h, self.dx, self.mb = h, dx, mb
         self.counts = [ps.n for ps, *_ in instances]
@@ -75,7 +76,8 @@ class SphRollout:
         params = self.params if params is None else np.asarray(params, np.float64)
         self._batch = api.Batch(self._groups(v0, params))
         self._batch.push()
-        self._check(self.L.tgpu_adjoint_create(self._batch.ptr, self.steps, self.every, ctypes.byref(self._adj)),
+        self._check(self.L.tgpu_adjoint_create(self._batch.ptr, self.steps, self.every, self.keep,
+                                               ctypes.byref(self._adj)),
                     "tgpu_adjoint_create")
         self._check(self.L.tgpu_adjoint_forward(self._adj), "tgpu_adjoint_forward")
         x = np.zeros((self.n, 3), np.float32)

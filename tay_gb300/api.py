@@ -98,7 +98,7 @@ TGPU_SYMBOLS = [
     ("tgpu_batch_flush_l2", ctypes.c_int, [_VP]),
     ("tgpu_host_alloc", _VP, [ctypes.c_ulonglong]),
     ("tgpu_host_free", None, [_VP]),
-    ("tgpu_adjoint_create", ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_VP)]),
+    ("tgpu_adjoint_create", ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_VP)]),
     ("tgpu_adjoint_forward", ctypes.c_int, [_VP]),
     ("tgpu_adjoint_backward", ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, _VP]),
     ("tgpu_adjoint_forward_ms", ctypes.c_double, [_VP]),

@@ -82,6 +82,7 @@ __global__ void __launch_bounds__(256) theta_reduce_kernel(const SegmentSpec *__
 struct TgpuAdjoint {
     TgpuBatch *b = nullptr;
     int steps = 0, every = 0;
+    int keep = 1;  // trailing segments recorded during the forward run (checkpoint mode)
     const tgpu::SphAdjointKernels *K = nullptr;
     std::vector<tgpu::Record> rec;
     std::vector<tgpu::Checkpoint> cp;  // cp[k] = state before step k*every; last = final state
@@ -159,7 +160,7 @@ SeeLaunch see_launch(TgpuBatch *b, const KernelRun &r, const PassIO &io) {
     S.skip_self = r.skip_self;
     S.stage_cap = 0;
     S.stage_cells = 0;
-    S.union_factor = 1;
+    S.union_factor = r.union_factor;
     S.pairs = b->d_pairs;
     S.telemetry = nullptr;
     S.io = io;
@@ -285,7 +286,7 @@ void tgpu_adjoint_destroy(TgpuAdjoint *a) {
     delete a;
 }
 
-int tgpu_adjoint_create(TgpuBatch *b, int steps, int checkpoint_every, TgpuAdjoint **out) {
+int tgpu_adjoint_create(TgpuBatch *b, int steps, int checkpoint_every, int keep_segments, TgpuAdjoint **out) {
     if (!b || !out || steps <= 0 || checkpoint_every < 0) return fail(TGPU_ERR_ARG, "adjoint: bad arguments");
     *out = nullptr;
     if (b->m != model_sph() || b->program != 3)
@@ -298,7 +299,9 @@ int tgpu_adjoint_create(TgpuBatch *b, int steps, int checkpoint_every, TgpuAdjoi
     a->steps = steps;
     a->every = checkpoint_every;
     a->K = sph_adjoint_kernels();
-    const int nrec = checkpoint_every == 0 ? steps : std::min(steps, checkpoint_every);
+    const int segs = checkpoint_every == 0 ? 1 : (steps + checkpoint_every - 1) / checkpoint_every;
+    a->keep = checkpoint_every == 0 ? 0 : std::max(1, std::min(keep_segments, segs));
+    const int nrec = checkpoint_every == 0 ? steps : std::min(steps, checkpoint_every * a->keep);
     const int ncp = checkpoint_every == 0 ? 1 : (steps + checkpoint_every - 1) / checkpoint_every + 1;
     a->rec.resize(nrec);
     a->cp.resize(ncp);
@@ -331,13 +334,16 @@ int tgpu_adjoint_forward(TgpuAdjoint *a) {
     int rc = prepare_specs(b);
     if (rc) return rc;
     cudaEventRecord(a->e0, b->st);
+    const int segs = a->every == 0 ? 1 : (a->steps + a->every - 1) / a->every;
+    const int first_kept = segs - a->keep;  // segments from here on are recorded now
     for (int s = 0; s < a->steps; ++s) {
         if (a->every == 0) {
             if (s == 0) save_checkpoint(b, a->cp[0]);
             recorded_step(a, &a->rec[s]);
         } else {
-            if (s % a->every == 0) save_checkpoint(b, a->cp[s / a->every]);
-            recorded_step(a, nullptr);
+            const int seg = s / a->every;
+            if (s % a->every == 0) save_checkpoint(b, a->cp[seg]);
+            recorded_step(a, seg >= first_kept ? &a->rec[(seg - first_kept) * a->every + s % a->every] : nullptr);
         }
     }
     if (a->every > 0) save_checkpoint(b, a->cp.back());
@@ -368,12 +374,18 @@ int tgpu_adjoint_backward(TgpuAdjoint *a, const float *dl_dpos, const float *dl_
         for (int s = a->steps - 1; s >= 0; --s) backward_step(a, a->rec[s]);
     } else {
         const int segs = (a->steps + a->every - 1) / a->every;
+        const int first_kept = segs - a->keep;
         for (int k = segs - 1; k >= 0; --k) {
             const int first = k * a->every;
             const int len = std::min(a->every, a->steps - first);
-            restore_checkpoint(b, a->cp[k]);
-            for (int s = 0; s < len; ++s) recorded_step(a, &a->rec[s]);
-            for (int s = len - 1; s >= 0; --s) backward_step(a, a->rec[s]);
+            int base = 0;
+            if (k >= first_kept) {
+                base = (k - first_kept) * a->every;  // recorded by the forward run
+            } else {
+                restore_checkpoint(b, a->cp[k]);  // recompute the segment, recording it
+                for (int s = 0; s < len; ++s) recorded_step(a, &a->rec[s]);
+            }
+            for (int s = len - 1; s >= 0; --s) backward_step(a, a->rec[base + s]);
         }
         restore_checkpoint(b, a->cp.back());  // the batch ends where the forward run ended
     }

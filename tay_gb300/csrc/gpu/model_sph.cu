@@ -97,7 +97,9 @@ struct Density {
         }
     }
     TGPU_D static void finish(Seer &s, const float4 &, const PassIO &io, uint32_t i, const Ctx &c, const Ctx &) {
-        io.out_f4[RP][i] = make_float4(s.rho, kPressure ? pressure(s.rho, c) : 0.0f, 0.0f, 0.0f);
+        const float P = kPressure ? pressure(s.rho, c) : 0.0f;
+        // A = P / rho^2, the pressure term every pair of the force pass needs
+        io.out_f4[RP][i] = make_float4(s.rho, P, P / (s.rho * s.rho), 0.0f);
     }
 };
 
@@ -105,7 +107,7 @@ struct Density {
 
 struct ForceSeer {
     float ax, ay, az;
-    float rho, P;
+    float rho, A;
     float4 v;
 };
 
@@ -120,7 +122,7 @@ struct Force {
         s.ax = s.ay = s.az = 0.0f;
         const float4 rp = io.in_f4[RP][i];
         s.rho = rp.x;
-        s.P = rp.y;
+        s.A = rp.z;
         s.v = io.in_f4[VEL][i];
     }
     template <class Acc>
@@ -141,9 +143,7 @@ struct Force {
                 const float rho_bar = 0.5f * (s.rho + brp.x);
                 visc = -(c.alpha * c.c0 * mu) / rho_bar;
             }
-            const float pa = s.P / (s.rho * s.rho);
-            const float pb = brp.y / (brp.x * brp.x);
-            const float coef = -c.m * ((pa + pb) + visc) * (dw / r);
+            const float coef = -c.m * ((s.A + brp.z) + visc) * (dw / r);
             s.ax += coef * dx;
             s.ay += coef * dy;
             s.az += coef * dz;
@@ -265,7 +265,8 @@ struct IntegrateAdj {
 
 struct ForceAdjSeer {
     float4 v, ab;
-    float rho, P;
+    float rho, P, A;
+    float inv_rho2, drho_A;  // 1 / rho^2 and dA/drho at fixed P = -2 P / rho^3
     float xb[3], vb[3];
     float rhob, Pb, ta, tc;
 };
@@ -276,6 +277,7 @@ struct ForceAdjSeer {
 //   rhobar_k += (w.d) dc/drho_k,    Pbar_k += (w.d) dc/dP_k,
 //   theta += (abar_k.d) dc/d(alpha, c0)
 // then the pressure adjoint: rhobar_k += Pbar_k dP/drho, dL/dc0 += Pbar_k 2 P_k / c0.
+// The adjoint decides nothing, so it uses the fast reciprocal square root and divisions.
 struct ForceAdj {
     using SeeCtx = Ctx;
     using ActCtx = Ctx;
@@ -288,6 +290,9 @@ struct ForceAdj {
         const float4 rp = io.in_f4[A_RP][i];
         s.rho = rp.x;
         s.P = rp.y;
+        s.A = rp.z;
+        s.inv_rho2 = __fdividef(1.0f, rp.x * rp.x);
+        s.drho_A = -2.0f * s.A / rp.x;
         s.xb[0] = s.xb[1] = s.xb[2] = 0.0f;
         s.vb[0] = s.vb[1] = s.vb[2] = 0.0f;
         s.rhob = s.Pb = s.ta = s.tc = 0.0f;
@@ -298,46 +303,50 @@ struct ForceAdj {
         const float r2 = dist2(dx, dy, dz);
         if (!(r2 < c.support2 && r2 > 0.0f)) return;
         const float4 bv = acc.f4(1, j), brp = acc.f4(2, j), bab = acc.f4(3, j);
-        const float r = __fsqrt_rn(r2);
+        const float rinv = rsqrtf(r2);
+        const float r = r2 * rinv;
         const float q = r * c.inv_h;
         const float dw = kernel_dw(q, c.sigma, c.inv_h);
         const float d2w = kernel_d2w(q, c.sigma, c.inv_h);
-        const float D = dw / r;
-        const float Dp = (d2w * r - dw) / r2;  // dD/dr
+        const float D = dw * rinv;
+        const float Dp_r = (d2w - D) * rinv * rinv;  // (dD/dr) / r
         const float vx = s.v.x - bv.x, vy = s.v.y - bv.y, vz = s.v.z - bv.z;
         const float sv = (vx * dx + vy * dy) + vz * dz;
-        const float rho_bar = 0.5f * (s.rho + brp.x);
-        const float den = r2 + c.eta2;
         float Pi = 0.0f, Pi_s = 0.0f, Pi_r2 = 0.0f, Pi_rb = 0.0f, Pi_al = 0.0f, Pi_c0 = 0.0f;
         if (sv < 0.0f) {
-            const float k0 = c.h / (den * rho_bar);
+            const float inv_rb = __fdividef(2.0f, s.rho + brp.x);
+            const float inv_den = __fdividef(1.0f, r2 + c.eta2);
+            const float k0 = c.h * inv_den * inv_rb;
             Pi_al = -c.c0 * k0 * sv;
             Pi_c0 = -c.alpha * k0 * sv;
             Pi = c.alpha * Pi_al;
             Pi_s = -c.alpha * c.c0 * k0;
-            Pi_r2 = -Pi / den;
-            Pi_rb = -Pi / rho_bar;
+            Pi_r2 = -Pi * inv_den;
+            Pi_rb = -Pi * inv_rb;
         }
-        const float Ak = s.P / (s.rho * s.rho), Aj = brp.y / (brp.x * brp.x);
-        const float T = (Ak + Aj) + Pi;
-        const float cc = -c.m * T * D;
+        const float T = (s.A + brp.z) + Pi;
+        const float mD = -c.m * D;
+        const float cc = mD * T;
         const float wx = s.ab.x - bab.x, wy = s.ab.y - bab.y, wz = s.ab.z - bab.z;
         const float xw = (dx * wx + dy * wy) + dz * wz;
-        const float coef_d = -c.m * (2.0f * Pi_r2 * D + T * Dp / r);
-        const float coef_v = -c.m * D * Pi_s;
+        const float coef_d = -c.m * (2.0f * Pi_r2 * D + T * Dp_r);
+        const float coef_v = mD * Pi_s;
         s.xb[0] += cc * wx + xw * (coef_v * vx + coef_d * dx);
         s.xb[1] += cc * wy + xw * (coef_v * vy + coef_d * dy);
         s.xb[2] += cc * wz + xw * (coef_v * vz + coef_d * dz);
-        s.vb[0] += xw * coef_v * dx;
-        s.vb[1] += xw * coef_v * dy;
-        s.vb[2] += xw * coef_v * dz;
-        s.rhob += xw * (-c.m * D) * (-2.0f * s.P / (s.rho * s.rho * s.rho) + 0.5f * Pi_rb);
-        s.Pb += xw * (-c.m * D / (s.rho * s.rho));
-        const float ad = (s.ab.x * dx + s.ab.y * dy) + s.ab.z * dz;
-        s.ta += ad * (-c.m * D * Pi_al);
-        s.tc += ad * (-c.m * D * Pi_c0);
+        const float xwv = xw * coef_v;
+        s.vb[0] += xwv * dx;
+        s.vb[1] += xwv * dy;
+        s.vb[2] += xwv * dz;
+        const float xmD = xw * mD;
+        s.rhob += xmD * (s.drho_A + 0.5f * Pi_rb);
+        s.Pb += xmD;
+        const float ad = ((s.ab.x * dx + s.ab.y * dy) + s.ab.z * dz) * mD;
+        s.ta += ad * Pi_al;
+        s.tc += ad * Pi_c0;
     }
     TGPU_D static void finish(Seer &s, const float4 &, const PassIO &io, uint32_t i, const Ctx &c, const Ctx &) {
+        s.Pb *= s.inv_rho2;  // dc/dP_k = -m D / rho_k^2
         const float x = s.rho / c.rho0;
         const float x2 = x * x;
         const float x6 = (x2 * x2) * x2;
@@ -372,8 +381,8 @@ struct DensityAdj {
         const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
         const float r2 = dist2(dx, dy, dz);
         if (!(r2 < c.support2 && r2 > 0.0f)) return;
-        const float r = __fsqrt_rn(r2);
-        const float g = (s.rhob + acc.f4(1, j).x) * c.m * kernel_dw(r * c.inv_h, c.sigma, c.inv_h) / r;
+        const float rinv = rsqrtf(r2);
+        const float g = (s.rhob + acc.f4(1, j).x) * c.m * kernel_dw(r2 * rinv * c.inv_h, c.sigma, c.inv_h) * rinv;
         s.xb[0] += g * dx;
         s.xb[1] += g * dy;
         s.xb[2] += g * dz;

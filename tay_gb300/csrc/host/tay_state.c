@@ -495,7 +495,7 @@ int tay_run_recorded(TayState **states, int count, int steps, int checkpoint_eve
     }
     double t0 = now_s();
     int rc = push_all(b, states, count);
-    if (rc == TGPU_OK) rc = tgpu_adjoint_create(b, steps, checkpoint_every, &g_batch_cache.adjoint);
+    if (rc == TGPU_OK) rc = tgpu_adjoint_create(b, steps, checkpoint_every, 1, &g_batch_cache.adjoint);
     if (rc == TGPU_OK) rc = tgpu_adjoint_forward(g_batch_cache.adjoint);
     if (rc == TGPU_OK) rc = fetch_all(b, states, count);
     if (rc != TGPU_OK) {

@@ -99,8 +99,9 @@ def test_adjoint_matches_finite_differences(gpu_grads):
     assert abs(dp[1] - fd_c) <= TOL * abs(fd_c), (dp[1], fd_c)
 
 
-def test_checkpointing_reproduces_recording(gpu_grads):
-    roll = SphRollout(_instances(), STEPS, checkpoint_every=10)
+@pytest.mark.parametrize("keep", [1, 2])
+def test_checkpointing_reproduces_recording(gpu_grads, keep):
+    roll = SphRollout(_instances(), STEPS, checkpoint_every=10, keep_segments=keep)
     x, _ = roll.forward()
     assert np.array_equal(x, gpu_grads["x"])
     dx0, dv0, dp = roll.backward(_dl_dx(x, gpu_grads["target"], roll))
