@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--adjoint", type=int, default=1, help="1 = add the differentiable SPH leg")
     ap.add_argument("--stage", type=int, default=None, help="see kernel: 1 = stage halos in shared memory")
     ap.add_argument("--union-factor", type=int, default=None, help="see kernel: union walk threshold")
+    ap.add_argument("--cell-order", type=int, default=None, help="0 = Morton cells, 1 = x-rows")
     ap.add_argument("--cell-multiple", type=float, default=None, help="grid cell edge / min part size")
     return ap.parse_args()
 
@@ -358,7 +359,7 @@ def run_gb300(args, rank, world, D):
 
     api.set_tuning()  # library defaults, then the autotuner's choice or command-line overrides
     over = {k: v for k, v in (("stage", args.stage), ("union_factor", args.union_factor),
-                              ("cell_multiple", args.cell_multiple)) if v is not None}
+                              ("cell_multiple", args.cell_multiple), ("cell_order", args.cell_order)) if v is not None}
     tuned = None
     if over:
         api.set_tuning(**over)

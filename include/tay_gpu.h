@@ -127,7 +127,10 @@ int tgpu_batch_program(const TgpuBatch *batch);
  *   union_factor   a warp walks the union of its seers' cell boxes (one read serves all
  *                  32 lanes) when that union is at most union_factor times the largest
  *                  single box; otherwise each lane walks its own box (0 = default)
- *   use_graphs     capture each step in a CUDA graph and replay it */
+ *   use_graphs     capture each step in a CUDA graph and replay it
+ *   cell_order     0: cells in 3-D Morton order, a {first, end} table entry per cell;
+ *                  1: x-rows (x fastest inside (y, z) rows, rows in 2-D Morton order),
+ *                  a seer's box is one candidate range per row (no staging) */
 typedef struct TgpuTuning {
     int stage;
     unsigned stage_cap;
@@ -135,6 +138,7 @@ typedef struct TgpuTuning {
     float cell_multiple;
     unsigned union_factor;
     int use_graphs;
+    unsigned cell_order;
 } TgpuTuning;
 
 void tgpu_set_tuning(const TgpuTuning *tuning);  /* NULL restores the defaults */

@@ -1,8 +1,8 @@
 """Autotuner for the Z-grid engine's knobs.
 
 Picks, by measurement on the GPU, the grid cell-size multiple (cell edge relative to the
-configured minimum part size), the warp walk (union walk threshold) and whether see CTAs
-stage their halos in shared memory.  Each candidate runs a few steps on a throwaway batch
+configured minimum part size), the cell order (3-D Morton cells or x-rows), the warp
+walk (union walk threshold) and whether see CTAs stage their halos in shared memory.  Each candidate runs a few steps on a throwaway batch
 built from the same groups (the caller's state is not advanced); the fastest candidate is
 set as the library's tuning and cached per shape class (model, pass sequence, agent-count
 bucket, segment-count bucket, radius / part-size ratio) in a JSON file, so later runs of the
@@ -18,12 +18,16 @@ import os
 from . import api
 
 DEFAULT_CANDIDATES = [
-    {"cell_multiple": 1.0, "union_factor": 1, "stage": 0},
-    {"cell_multiple": 0.5, "union_factor": 1, "stage": 0},
-    {"cell_multiple": 0.75, "union_factor": 1, "stage": 0},
-    {"cell_multiple": 1.5, "union_factor": 1, "stage": 0},
-    {"cell_multiple": 1.0, "union_factor": 2, "stage": 0},
-    {"cell_multiple": 1.0, "union_factor": 2, "stage": 1},
+    {"cell_multiple": 1.0, "union_factor": 1, "stage": 0, "cell_order": 0},
+    {"cell_multiple": 0.5, "union_factor": 1, "stage": 0, "cell_order": 0},
+    {"cell_multiple": 0.75, "union_factor": 1, "stage": 0, "cell_order": 0},
+    {"cell_multiple": 1.5, "union_factor": 1, "stage": 0, "cell_order": 0},
+    {"cell_multiple": 1.0, "union_factor": 1, "stage": 0, "cell_order": 1},
+    {"cell_multiple": 0.5, "union_factor": 1, "stage": 0, "cell_order": 1},
+    {"cell_multiple": 0.75, "union_factor": 1, "stage": 0, "cell_order": 1},
+    {"cell_multiple": 0.34, "union_factor": 1, "stage": 0, "cell_order": 1},
+    {"cell_multiple": 1.0, "union_factor": 2, "stage": 0, "cell_order": 0},
+    {"cell_multiple": 1.0, "union_factor": 2, "stage": 1, "cell_order": 0},
 ]
 
 
@@ -74,10 +78,12 @@ def autotune(groups, candidates=None, steps: int = 3, use_cache: bool = True) ->
     if key in cache:
         api.set_tuning(**cache[key]["tuning"])
         return dict(cache[key], cached=True)
+    base = api.get_tuning()
     trials = []
     for cand in candidates or DEFAULT_CANDIDATES:
-        trials.append((measure(groups, cand, steps), cand))
+        trials.append((measure(groups, dict(base, **cand), steps), cand))
     best_ms, best = min(trials, key=lambda t: t[0])
+    best = dict(base, **best)
     api.set_tuning(**best)
     entry = {"tuning": best, "ms_per_step": best_ms,
              "trials": [{"tuning": c, "ms_per_step": m} for m, c in trials]}

@@ -79,7 +79,11 @@ const ModelDesc *model_sph();
 // helpers used by the model translation units
 template <class P>
 void launch_see_t(const SeeLaunch &L, size_t smem, cudaStream_t st) {
-    if (L.ctas) see_kernel<P><<<L.ctas, kSeeThreads, smem, st>>>(L);
+    if (!L.ctas) return;
+    if (L.rows)
+        see_rows_kernel<P><<<L.ctas, kSeeThreads, 0, st>>>(L);
+    else
+        see_kernel<P><<<L.ctas, kSeeThreads, smem, st>>>(L);
 }
 template <class A>
 void launch_act_t(const ActLaunch &L, cudaStream_t st) {

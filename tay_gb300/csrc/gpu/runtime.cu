@@ -52,6 +52,7 @@ TgpuTuning default_tuning() {
     t.cell_multiple = 1.0f;
     t.union_factor = 1;
     t.use_graphs = 1;
+    t.cell_order = 0;
     return t;
 }
 TgpuTuning g_tuning = default_tuning();
@@ -99,6 +100,7 @@ void free_batch(TgpuBatch *b) {
     if (!b) return;
     for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
     cudaFree(b->d_specs);
+    cudaFree(b->d_extent);
     cudaFree(b->d_tile_seg);
     cudaFree(b->d_cta);
     cudaFree(b->d_box);
@@ -334,6 +336,7 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E) {
             S.stage_cap = r.stage_cap;
             S.stage_cells = r.stage_cells;
             S.union_factor = r.union_factor;
+            S.rows = b->cell_order == kOrderRows ? 1u : 0u;
             S.pairs = b->d_pairs;
             S.telemetry = b->d_telemetry;
             S.io = io;
@@ -534,6 +537,7 @@ int tgpu_batch_create(const TgpuGroup *groups, int group_count, TgpuBatch **out)
     b->program = program;
     b->nseg = group_count;
     b->use_graphs = g_tuning.use_graphs != 0;
+    b->cell_order = g_tuning.cell_order == kOrderRows ? kOrderRows : kOrderMorton;
     uint32_t total = 0;
     for (int s = 0; s < group_count; ++s) {
         const TgpuGroup &g = groups[s];
@@ -559,6 +563,7 @@ int tgpu_batch_create(const TgpuGroup *groups, int group_count, TgpuBatch **out)
         sp.begin = total;
         sp.count = g.count;
         sp.fixed_box = g.box_fixed ? 1u : 0u;
+        sp.order = b->cell_order;
         for (int a = 0; a < 3; ++a) {
             float part = g.min_part_sizes[a] > 0.0f ? g.min_part_sizes[a] : 1.0f;
             sp.part[a] = part * g_tuning.cell_multiple;
@@ -598,6 +603,7 @@ int tgpu_batch_create(const TgpuGroup *groups, int group_count, TgpuBatch **out)
     CKB(cudaEventCreate(&b->e1));
     const size_t n = std::max<uint32_t>(total, 1);
     CKB(cudaMalloc(&b->d_specs, sizeof(SegmentSpec) * b->nseg));
+    CKB(cudaMalloc(&b->d_extent, sizeof(BoxAcc)));
     CKB(cudaMalloc(&b->d_tile_seg, sizeof(uint32_t) * std::max<uint32_t>(b->tiles, 1)));
     CKB(cudaMalloc(&b->d_cta, sizeof(uint2) * std::max<uint32_t>(b->ctas, 1)));
     CKB(cudaMalloc(&b->d_box, sizeof(BoxAcc) * b->nseg));
@@ -646,7 +652,7 @@ int tgpu_batch_create(const TgpuGroup *groups, int group_count, TgpuBatch **out)
             CKB(cudaMalloc(&r.d_see_ctx, b->ctx_stride * b->nseg));
             const uint32_t cap_default = r.k->staged_f4 <= 1 ? 1024u : 768u;
             r.union_factor = g_tuning.union_factor;
-            if (g_tuning.stage) {
+            if (g_tuning.stage && g_tuning.cell_order != kOrderRows) {
                 r.stage_cap = g_tuning.stage_cap ? g_tuning.stage_cap : cap_default;
                 r.stage_cells = g_tuning.stage_cells ? g_tuning.stage_cells : 512u;
                 r.smem = (size_t)r.k->staged_f4 * r.stage_cap * sizeof(float4) +
@@ -690,24 +696,12 @@ int tgpu_batch_push(TgpuBatch *b, int group, const void *host) {
     HostSeg &h = b->hs[group];
     const SegmentSpec &sp = b->specs[group];
     const uint32_t n = sp.count;
-    // extent of the pushed positions (float4 right after the 8-byte tag)
-    float mn[3] = {0.f, 0.f, 0.f}, mx[3] = {0.f, 0.f, 0.f};
-    const char *rec = (const char *)host;
-    for (uint32_t i = 0; i < n; ++i) {
-        float p[3];
-        memcpy(p, rec + (size_t)i * b->m->agent_bytes + 8, sizeof(p));
-        for (int a = 0; a < 3; ++a) {
-            if (i == 0 || p[a] < mn[a]) mn[a] = p[a];
-            if (i == 0 || p[a] > mx[a]) mx[a] = p[a];
-        }
-    }
-    for (int a = 0; a < 3; ++a) {
-        h.host_min[a] = mn[a];
-        h.host_max[a] = mx[a];
-    }
     h.pushed = true;
     b->specs_dirty = true;
-    if (!n) return TGPU_OK;
+    if (!n) {
+        for (int a = 0; a < 3; ++a) h.host_min[a] = h.host_max[a] = 0.0f;
+        return TGPU_OK;
+    }
     uint32_t *aos = b->d_aos + (size_t)sp.begin * (b->m->agent_bytes / 4);
     CK(cudaMemcpyAsync(aos, host, (size_t)n * b->m->agent_bytes, cudaMemcpyHostToDevice, b->st));
     // pack into the current buffers of every stream
@@ -722,8 +716,17 @@ int tgpu_batch_push(TgpuBatch *b, int group, const void *host) {
         io.in_u32[c] = io.out_u32[c];
     }
     b->m->pack(aos, n, io, b->st);
+    // extent of the pushed positions (it sizes the segment's grid budget), reduced on
+    // the device from the packed position stream
+    launch_extent(io.out_f4[0], n, b->d_extent, b->st);
+    BoxAcc ext;
+    CK(cudaMemcpyAsync(&ext, b->d_extent, sizeof(BoxAcc), cudaMemcpyDeviceToHost, b->st));
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(b->st));
+    for (int a = 0; a < 3; ++a) {
+        h.host_min[a] = ordered_to_float(ext.lo[a]);
+        h.host_max[a] = ordered_to_float(ext.hi[a]);
+    }
     return TGPU_OK;
 }
 

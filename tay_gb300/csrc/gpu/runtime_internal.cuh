@@ -76,6 +76,8 @@ struct TgpuBatch {
     double last_ms = 0.0;
     unsigned long long last_pairs = 0;
     bool use_graphs = true;
+    uint32_t cell_order = kOrderMorton;  // key order and table layout of every segment
+    BoxAcc *d_extent = nullptr;          // pushed extent of one group
     std::map<uint64_t, cudaGraphExec_t> graphs;
 };
 

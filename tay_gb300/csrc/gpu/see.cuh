@@ -354,6 +354,84 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
     }
 }
 
+// See pass over a row-order table (kOrderRows): the agents of x-adjacent cells are
+// contiguous, so a seer's cell box is one candidate range per (y, z) row, read from two
+// start entries of the row.  Lanes of a warp are consecutive seers along a row: their
+// ranges are nearly the same length and their candidate loads fall on neighbouring
+// addresses.  No staging; a warp whose union box is compact walks the union's row
+// ranges with the two-phase batches instead.
+template <class P>
+__global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
+    using namespace see_detail;
+    const uint2 cta = L.cta_table[blockIdx.x];
+    const uint32_t seg = cta.x;
+    const SegmentSpec S = L.specs[seg];
+    const BoxAcc B = L.box[seg];
+    const Grid g = segment_grid(S, B);
+    const float pad = grid_pad(g, S, B);
+    const float4 r4 = L.radii[seg];
+    const typename P::SeeCtx &sctx = *reinterpret_cast<const typename P::SeeCtx *>(L.ctx + (size_t)seg * L.ctx_stride);
+    const typename P::ActCtx &actx =
+        *reinterpret_cast<const typename P::ActCtx *>(L.act_ctx + (size_t)seg * L.act_ctx_stride);
+    const uint32_t seg_end = S.begin + S.count;
+    const uint32_t i = cta.y + threadIdx.x;
+    const bool active = i < seg_end;
+    const uint32_t lane = threadIdx.x & 31u;
+
+    float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
+    typename P::Seer s;
+    int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
+    if (active) {
+        sp = L.io.in_f4[0][i];
+        P::load(s, L.io, i, sctx, actx);
+        axis_range(sp.x, r4.x, g.origin[0], g.inv_cs[0], g.dims[0], pad, lo[0], hi[0]);
+        axis_range(sp.y, r4.y, g.origin[1], g.inv_cs[1], g.dims[1], pad, lo[1], hi[1]);
+        axis_range(sp.z, r4.z, g.origin[2], g.inv_cs[2], g.dims[2], pad, lo[2], hi[2]);
+    }
+    const uint32_t *rows = reinterpret_cast<const uint32_t *>(L.table + S.table_base);
+    const uint32_t rw = (uint32_t)g.dims[0] + 1u, dy0 = (uint32_t)g.dims[1];
+    GlobalSeen<P::kSeenF4> acc;
+#pragma unroll
+    for (int k = 0; k < P::kSeenF4; ++k) acc.s[k] = L.io.in_f4[P::seen_stream(k)];
+    const float4 *pos = L.io.in_f4[0];
+    const uint32_t self = (active && L.skip_self) ? i : 0xFFFFFFFFu;
+    uint32_t pairs = 0;
+    uint32_t tested = 0;
+    if (L.telemetry && threadIdx.x == 0) atomicAdd(L.telemetry + 2, 1ull);
+
+    const int wl0 = warp_min_i(lo[0]), wl1 = warp_min_i(lo[1]), wl2 = warp_min_i(lo[2]);
+    const int wh0 = warp_max_i(hi[0]), wh1 = warp_max_i(hi[1]), wh2 = warp_max_i(hi[2]);
+    if (wl0 <= wh0) {
+        const int lane_vol = active ? (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) * (hi[0] - lo[0] + 1) : 0;
+        const long long union_vol = (long long)(wh0 - wl0 + 1) * (wh1 - wl1 + 1) * (wh2 - wl2 + 1);
+        const bool union_mode = union_vol <= (long long)L.union_factor * warp_max_i(lane_vol);
+        if (L.telemetry && lane == 0) atomicAdd(L.telemetry + (union_mode ? 3 : 4), 1ull);
+        if (union_mode) {
+            for (int z = wl2; z <= wh2; ++z)
+                for (int y = wl1; y <= wh1; ++y) {
+                    const uint32_t *r = rows + ((uint32_t)z * dy0 + (uint32_t)y) * rw;
+                    union_batches<P>(s, sp, r4, active, __ldg(r + wl0), __ldg(r + wh0 + 1), self, pos, acc, sctx, pairs,
+                                     tested);
+                }
+        } else if (active) {
+            for (int z = lo[2]; z <= hi[2]; ++z)
+                for (int y = lo[1]; y <= hi[1]; ++y) {
+                    const uint32_t *r = rows + ((uint32_t)z * dy0 + (uint32_t)y) * rw;
+                    lane_run<P>(s, sp, r4, __ldg(r + lo[0]), __ldg(r + hi[0] + 1), self, pos, acc, sctx, pairs, tested);
+                }
+        }
+    }
+    if (active) P::finish(s, sp, L.io, i, sctx, actx);
+    if (L.pairs) {
+        uint32_t w = warp_sum_u(pairs);
+        if (lane == 0 && w) atomicAdd(L.pairs, (unsigned long long)w);
+    }
+    if (L.telemetry) {
+        uint32_t w = warp_sum_u(tested);
+        if (lane == 0 && w) atomicAdd(L.telemetry, (unsigned long long)w);
+    }
+}
+
 template <class A>
 __global__ void __launch_bounds__(kSortThreads) act_kernel(ActLaunch L) {
     const uint32_t seg = L.tile_seg[blockIdx.x];

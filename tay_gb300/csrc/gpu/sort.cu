@@ -89,6 +89,28 @@ __global__ void __launch_bounds__(kSortThreads) bbox_kernel(const SegmentSpec *_
     }
 }
 
+__global__ void __launch_bounds__(kSortThreads) extent_kernel(const float4 *__restrict__ pos, uint32_t n, BoxAcc *out) {
+    uint32_t lo[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+    uint32_t hi[3] = {0u, 0u, 0u};
+    for (uint32_t i = blockIdx.x * kSortThreads + threadIdx.x; i < n; i += gridDim.x * kSortThreads) {
+        const float4 p = pos[i];
+        const float c[3] = {p.x, p.y, p.z};
+        for (int a = 0; a < 3; ++a) {
+            const uint32_t o = float_to_ordered(c[a]);
+            lo[a] = min(lo[a], o);
+            hi[a] = max(hi[a], o);
+        }
+    }
+    for (int a = 0; a < 3; ++a) {
+        const uint32_t l = warp_min(lo[a]);
+        const uint32_t h = warp_max(hi[a]);
+        if (lane_id() == 0) {
+            atomicMin(&out->lo[a], l);
+            atomicMax(&out->hi[a], h);
+        }
+    }
+}
+
 __global__ void box_reset_kernel(BoxAcc *box, uint32_t segments) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= segments) return;
@@ -127,7 +149,7 @@ __global__ void __launch_bounds__(kSortThreads) key_histogram_kernel(const Segme
         uint32_t cx = (uint32_t)cell_coord(p.x, g.origin[0], g.inv_cs[0], g.dims[0]);
         uint32_t cy = (uint32_t)cell_coord(p.y, g.origin[1], g.inv_cs[1], g.dims[1]);
         uint32_t cz = (uint32_t)cell_coord(p.z, g.origin[2], g.inv_cs[2], g.dims[2]);
-        uint32_t k = morton3(cx, cy, cz);
+        uint32_t k = cell_key(s, cx, cy, cz);
         keys[i] = k;
         atomicAdd(&hist[k & mask], 1u);
     }
@@ -303,7 +325,10 @@ TGPU_D uint32_t table_index(const Grid &g, uint32_t key) {
 }
 
 // Records {first, end} of every run of equal keys at the run's cell (write_runs = 1), or
-// clears those entries again (write_runs = 0) before the next sort.
+// clears those entries again (write_runs = 0) before the next sort.  Row order: the first
+// agent of each cell writes its index into the start entries of the empty cells before
+// it in its row and its own; the last agent of a row writes the row's end into the
+// entries after its cell; a row's first agent clears the whole row.
 __global__ void __launch_bounds__(kSortThreads) cell_table_kernel(const SegmentSpec *__restrict__ specs,
                                                                   const uint32_t *__restrict__ tile_seg,
                                                                   const BoxAcc *__restrict__ box,
@@ -316,6 +341,60 @@ __global__ void __launch_bounds__(kSortThreads) cell_table_kernel(const SegmentS
     const uint32_t beg = s.begin + t * kSortTile;
     const uint32_t seg_end = s.begin + s.count;
     const uint32_t end = min(beg + (uint32_t)kSortTile, seg_end);
+    if (s.order == kOrderRows) {
+        // Each lane derives up to two fills (an entry range of one row and its value);
+        // the warp then writes every lane's fills together, 32 consecutive entries per
+        // store, since the head and tail fills of a row span most of it.
+        uint32_t *rows = reinterpret_cast<uint32_t *>(table + s.table_base);
+        const uint32_t b = axis_bits(s);
+        const uint32_t xmask = (1u << b) - 1u;
+        const uint32_t dx = (uint32_t)g.dims[0], rw = dx + 1u;
+        const uint32_t lane = threadIdx.x & 31u;
+        for (uint32_t base = beg; base < end; base += kSortThreads) {
+            const uint32_t i = base + threadIdx.x;
+            uint32_t off[2] = {0u, 0u}, len[2] = {0u, 0u}, val[2] = {0u, 0u};
+            if (i < end) {
+                const uint32_t k = keys[i];
+                const uint32_t row = k >> b, x = k & xmask;
+                const bool row_first = (i == s.begin) || (keys[i - 1] >> b) != row;
+                const bool row_last = (i + 1 == seg_end) || (keys[i + 1] >> b) != row;
+                const bool first = row_first || keys[i - 1] != k;
+                const uint32_t y = compact2_10(row), z = compact2_10(row >> 1);
+                const uint32_t r0 = (z * (uint32_t)g.dims[1] + y) * rw;
+                if (!write_runs) {
+                    if (row_first) {
+                        off[0] = r0;
+                        len[0] = rw;
+                    }
+                } else {
+                    if (first) {
+                        const uint32_t x0 = row_first ? 0u : (keys[i - 1] & xmask) + 1u;
+                        off[0] = r0 + x0;
+                        len[0] = x + 1u - x0;
+                        val[0] = i;
+                    }
+                    if (row_last) {
+                        off[1] = r0 + x + 1u;
+                        len[1] = dx - x;
+                        val[1] = i + 1u;
+                    }
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+                uint32_t m = __ballot_sync(0xffffffffu, len[t] > 0u);
+                while (m) {
+                    const int l = __ffs(m) - 1;
+                    m &= m - 1u;
+                    const uint32_t o = __shfl_sync(0xffffffffu, off[t], l);
+                    const uint32_t n = __shfl_sync(0xffffffffu, len[t], l);
+                    const uint32_t v = __shfl_sync(0xffffffffu, val[t], l);
+                    for (uint32_t c = lane; c < n; c += 32u) rows[o + c] = v;
+                }
+            }
+        }
+        return;
+    }
     for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads) {
         const uint32_t k = keys[i];
         const bool first = (i == s.begin) || keys[i - 1] != k;
@@ -346,6 +425,11 @@ __global__ void __launch_bounds__(256) gather_kernel(uint32_t n, const uint32_t 
 }
 
 // ------------------------------------------------------------------ host-side launchers
+
+void launch_extent(const float4 *pos, uint32_t n, BoxAcc *out, cudaStream_t st) {
+    box_reset_kernel<<<1, 32, 0, st>>>(out, 1);
+    if (n) extent_kernel<<<std::min<uint32_t>((n + kSortThreads - 1) / kSortThreads, 152u * 8u), kSortThreads, 0, st>>>(pos, n, out);
+}
 
 void launch_box(const SortLaunch &L, cudaStream_t st) {
     box_reset_kernel<<<(L.segments + 127) / 128, 128, 0, st>>>(L.box, L.segments);

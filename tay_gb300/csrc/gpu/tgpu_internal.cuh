@@ -39,6 +39,7 @@ struct SegmentSpec {
     uint32_t tile_count;     // radix tiles of this segment
     uint32_t axis_cells_max; // power of two, <= 1024: bounds each grid axis (key bits)
     uint32_t fixed_box;      // 1: use box_min/box_max instead of the agents' bounding box
+    uint32_t order;          // cell order of the keys and table layout: kOrderMorton / kOrderRows
     float part[3];           // minimum cell edge per axis
     float reach[3];          // largest see radius per axis over the segment's see passes
     float box_min[3];        // fixed space box (tay_fix_space_box)
@@ -157,6 +158,49 @@ TGPU_HD uint32_t compact10(uint32_t v) {
 
 TGPU_HD uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
     return spread10(x) | (spread10(y) << 1) | (spread10(z) << 2);
+}
+
+// 2-D Morton spread / compaction of 10 bits (bit k to bit 2k).
+TGPU_HD uint32_t spread2_10(uint32_t v) {
+    v &= 0x3FFu;
+    v = (v | (v << 8)) & 0x00FF00FFu;
+    v = (v | (v << 4)) & 0x0F0F0F0Fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+
+TGPU_HD uint32_t compact2_10(uint32_t v) {
+    v &= 0x55555555u;
+    v = (v | (v >> 1)) & 0x33333333u;
+    v = (v | (v >> 2)) & 0x0F0F0F0Fu;
+    v = (v | (v >> 4)) & 0x00FF00FFu;
+    v = (v | (v >> 8)) & 0x0000FFFFu;
+    return v & 0x3FFu;
+}
+
+// Two cell orders.  kOrderMorton: the 3-D Morton key above, table of {first, end} per
+// cell.  kOrderRows: x fastest inside rows of constant (y, z), the rows in 2-D Morton
+// order of (y, z): key = (morton2(y, z) << b) | x with b = log2(axis_cells_max), so the
+// agents of x-adjacent cells are contiguous and a seer's box is one candidate range per
+// row.  Its table holds per row dims[0] + 1 start offsets: entry x is the first agent of
+// the row in a cell >= x, entry dims[0] the row's end.  Both orders give the same
+// neighbour sets; only the order in which a seer meets its neighbours differs.
+enum CellOrder : uint32_t { kOrderMorton = 0, kOrderRows = 1 };
+
+TGPU_HD uint32_t axis_bits(const SegmentSpec &s) {
+#ifdef __CUDA_ARCH__
+    return 31u - (uint32_t)__clz(s.axis_cells_max | 1u);
+#else
+    uint32_t b = 0;
+    while ((2u << b) <= s.axis_cells_max && b < 10) ++b;
+    return b;
+#endif
+}
+
+TGPU_HD uint32_t cell_key(const SegmentSpec &s, uint32_t x, uint32_t y, uint32_t z) {
+    if (s.order == kOrderRows) return ((spread2_10(y) | (spread2_10(z) << 1)) << axis_bits(s)) | x;
+    return morton3(x, y, z);
 }
 
 // The step's grid of a segment: from its fixed box, or from the bounding box of its

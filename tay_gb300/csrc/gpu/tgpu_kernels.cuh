@@ -54,6 +54,7 @@ struct SeeLaunch {
     uint32_t stage_cap;       // staged agents per CTA (0: no staging, read through L1)
     uint32_t stage_cells;     // halo cells per CTA
     uint32_t union_factor;    // a warp walks its union box when union <= factor x lane box
+    uint32_t rows;            // 1: the table is in row order (see_rows_kernel)
     unsigned long long *pairs;  // box-test passes, summed over the launch
     // telemetry (the reference's TAY_TELEMETRY counters, tay/space.c:50-60, plus the
     // kernel's own paths): [0] candidates box-tested (broad phase), [1] staged CTAs,
@@ -73,6 +74,8 @@ struct ActLaunch {
 };
 
 void launch_box(const SortLaunch &L, cudaStream_t st);
+// Bounding box of n positions into *out (reset first), for the pushed extent.
+void launch_extent(const float4 *pos, uint32_t n, BoxAcc *out, cudaStream_t st);
 void launch_sort(const SortLaunch &L, cudaStream_t st, uint32_t **sorted_keys, uint32_t **perm);
 void launch_cell_table(const SortLaunch &L, const uint32_t *sorted_keys, int write_runs, cudaStream_t st);
 void launch_gather(uint32_t n, const uint32_t *perm, const GatherSet &set, cudaStream_t st);

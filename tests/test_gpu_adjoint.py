@@ -127,3 +127,20 @@ def test_torch_autograd_harness(gpu_grads):
     np.testing.assert_allclose(params.grad.numpy(), gpu_grads["dp"], rtol=1e-4)
     np.testing.assert_allclose(v0.grad.numpy(), gpu_grads["dv0"], rtol=1e-3, atol=1e-9)
     roll.close()
+
+
+def test_adjoint_row_order(gpu_grads):
+    """The adjoint over the row-order cell table: same gradients up to float summation order."""
+    from tay_gb300 import api
+    try:
+        api.set_tuning(cell_order=1)
+        roll = SphRollout(_instances(), STEPS, checkpoint_every=10, keep_segments=2)
+        x, _ = roll.forward()
+        dx0, dv0, dp = roll.backward(_dl_dx(x, gpu_grads["target"], roll))
+        roll.close()
+    finally:
+        api.set_tuning()
+    assert normwise(x, gpu_grads["x"]) < 1e-5
+    np.testing.assert_allclose(dp, gpu_grads["dp"], rtol=TOL)
+    assert normwise(dx0, gpu_grads["dx0"]) < TOL
+    assert normwise(dv0, gpu_grads["dv0"]) < TOL

@@ -105,3 +105,48 @@ def test_batch_matches_individual_runs(gpu):
         assert np.array_equal(out["p"], single["p"])
         assert np.array_equal(out["v"], single["v"])
         st.end()
+
+
+@pytest.mark.parametrize("tuning", [
+    {"cell_order": 1}, {"cell_order": 1, "cell_multiple": 0.34}, {"cell_order": 1, "union_factor": 2},
+    {"union_factor": 2}, {"stage": 1}, {"cell_multiple": 0.5}, {"cell_multiple": 1.5},
+])
+def test_walk_tunings_match_oracle(gpu, port, tuning):
+    """Every cell order, cell size and see walk gives the oracle's neighbour counts bit for
+    bit and its accumulated vectors within the one-step tolerance."""
+    ps = W.boids_points(30000, seed=9, clusters=8, side=400.0)
+    recs = M.records(M.BOIDS_RECORD, ps.p, ps.v)
+    setup = M.boids_setup(passes=("boids_see",))
+    o = oracle_run(port, O.MODEL_BOIDS, setup, recs, 1)
+    try:
+        api.set_tuning(**tuning)
+        g = M.run(setup, recs, 1)
+    finally:
+        api.set_tuning()
+    assert np.array_equal(g["count"], o["count"])
+    assert np.array_equal(g["sep_count"], o["sep_count"])
+    for f in ("coh", "ali", "sep"):
+        assert normwise(g[f][:, :3], o[f][:, :3]) < TOL_1STEP, f
+
+
+@pytest.mark.parametrize("order", [0, 1])
+def test_cell_orders_many_steps(gpu, port, order):
+    """Both cell orders over 20 see+act steps of boids and 5 SPH steps (all four passes)."""
+    ps = W.boids_points(20000, seed=13, clusters=4, side=300.0)
+    recs = M.records(M.BOIDS_RECORD, ps.p, ps.v)
+    setup = M.boids_setup()
+    sph = W.sph_dam(16, 24, 16)
+    srecs = M.records(M.SPH_RECORD, sph.points.p, sph.points.v)
+    ssetup = M.sph_setup()
+    try:
+        api.set_tuning(cell_order=order)
+        g = M.run(setup, recs, 20)
+        gs = M.run(ssetup, srecs, 5)
+    finally:
+        api.set_tuning()
+    o = oracle_run(port, O.MODEL_BOIDS, setup, recs, 20)
+    assert normwise(g["p"][:, :3], o["p"][:, :3]) < TOL_MANY
+    assert normwise(g["v"][:, :3], o["v"][:, :3]) < TOL_MANY
+    os_ = oracle_run(port, O.MODEL_SPH, ssetup, srecs, 5)
+    assert normwise(gs["p"][:, :3], os_["p"][:, :3]) < TOL_1STEP
+    assert normwise(gs["v"][:, :3], os_["v"][:, :3]) < TOL_MANY
