@@ -11,8 +11,9 @@ One step = sort (keys, radix passes, cell table, reorder) + the fused see+act pa
           test (device counter) / device time of the timed steps (CUDA events on the
           engine's stream), L2 flushed between steps;
   e2e     the same metric through the Tay C API with host buffers: each step is
-          tay_run(state, 1), which copies the AoS records host->device, runs the step and
-          copies them back (the OpenCL path's push/fetch per run, tay/state.c:208-315);
+          tay_mark_agents_changed + tay_run(state, 1) + tay_get_agent, which copies the AoS
+          records host->device, runs the step and copies them back (what the OpenCL
+          path's push/fetch around every run costs, tay/state.c:208-315);
   roofline  of the dominant kernel (the fused see+act pass), from a profiled leg with
           CUDA events around every kernel class on the engine's stream.
 --impl reference times the CPU implementation of the same step (the oracle restatement
@@ -393,7 +394,7 @@ def run_gb300(args, rank, world, D):
     launches = B.launches_per_step() * args.steps
     B.close()
 
-    # e2e through the C API with host buffers (push + step + fetch per tay_run)
+    # e2e through the C API with host buffers (push + step + fetch every step)
     st, g = M.make_state(setup, recs)
     st.start()
     for _ in range(max(1, args.warmup // 2)):
@@ -403,7 +404,9 @@ def run_gb300(args, rank, world, D):
     t0 = time.perf_counter()
     e2e_pairs = 0
     for _ in range(e2e_steps):
+        st.mark_changed(g)   # the step's inputs are the host records: pushed (H2D)
         st.run(1)
+        st.agent_ptr(g, 0)   # the step's result read back into the host records (D2H)
         e2e_pairs += st.pairs()
     e2e_s = time.perf_counter() - t0
     D.barrier()

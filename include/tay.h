@@ -164,6 +164,14 @@ unsigned tay_commit_agents(TayState *state, TayGroup *group, const void *records
 /* NEW: number of committed agents of a group. */
 unsigned tay_get_agent_count(TayState *state, TayGroup *group);
 
+/* NEW: agents stay on the device between tay_run calls; tay_get_agent fetches a group's
+ * records (in cell order) only when the device holds newer ones, and tay_run pushes a
+ * group only when its host records changed through tay_commit_available_agent,
+ * tay_commit_agents, tay_clear_all_agents or tay_configure_space.  A host that writes
+ * records through the pointer tay_get_agent returns calls this so that the next
+ * tay_run pushes them. */
+void tay_mark_agents_changed(TayState *state, TayGroup *group);
+
 /* NEW: differentiable SPH rollouts (the benchmark spec's hand-written adjoint; no
  * counterpart in the reference).  tay_run_recorded advances `count` states (each one
  * TAY_GPU_Z_GRID group running sph_density, sph_pressure, sph_force, sph_integrate) by

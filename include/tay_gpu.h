@@ -61,6 +61,29 @@ typedef struct TgpuGroup {
 int tgpu_batch_create(const TgpuGroup *groups, int group_count, TgpuBatch **out);
 void tgpu_batch_destroy(TgpuBatch *batch);
 
+/* One pass of a state whose groups are mixed by its passes (tay_add_see with
+ * seer_group != seen_group, several see passes per group; tay/state_compile.c:109-120,
+ * test/test_combo.c:114-119).  seer_group is the acting group of an act pass;
+ * seen_group is used by see passes only.  Both index the `groups` array. */
+typedef struct TgpuStatePass {
+    TgpuPass pass;
+    int seer_group;
+    int seen_group;
+} TgpuStatePass;
+
+/* Creates a batch for one state of `group_count` groups of one device model, stepped by
+ * the state-level pass list `passes` (registration order; groups[k].passes is not used).
+ * Every pass runs as its own kernel over its seer (or acting) group, a see pass reading
+ * the seen group's cell table and streams; seer == seen is skipped only inside one group
+ * without self_see.  A group may have several see passes when the model's see function
+ * accumulates onto the seer's stored fields (the test model); otherwise one.  Push,
+ * fetch and run work per group as for tgpu_batch_create. */
+int tgpu_state_create(const TgpuGroup *groups, int group_count, const TgpuStatePass *passes, int pass_count,
+                      TgpuBatch **out);
+
+/* Copies the contexts and radii of a state's passes again (same order as at create). */
+int tgpu_state_set_contexts(TgpuBatch *batch, const TgpuStatePass *passes, int pass_count);
+
 /* Copies the pass contexts of group `group` again (contexts are borrowed by the host
  * API and re-read at every tay_run, as tay/ocl.c:252-259 does). */
 int tgpu_batch_set_contexts(TgpuBatch *batch, int group, const TgpuGroup *desc);

@@ -102,12 +102,22 @@ class RunResult:
     pairs: int = -1  # box-test passes over the run (port only)
 
 
+def _bind_groups(lib, name, real_c):
+    fn = getattr(lib, name)
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                   ctypes.c_void_p, real_c, real_c, ctypes.c_int, ctypes.c_int, ctypes.c_int] + \
+        [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    return fn
+
+
 class _Impl:
-    def __init__(self, so, names, pair_fns=None):
+    def __init__(self, so, names, pair_fns=None, group_names=None):
         if not os.path.exists(so):
             raise FileNotFoundError(so)
         self.lib = ctypes.CDLL(so)
         self.fns = {real: _bind(self.lib, nm, c) for real, (nm, c) in names.items()}
+        self.group_fns = {real: _bind_groups(self.lib, nm, c) for real, (nm, c) in (group_names or {}).items()}
         self.pair_fns = {}
         for real, nm in (pair_fns or {}).items():
             f = getattr(self.lib, nm)
@@ -130,6 +140,31 @@ class _Impl:
         pairs = int(self.pair_fns[real]()) if real in self.pair_fns else -1
         return RunResult(rec, ms.value, pairs)
 
+    def run_groups(self, model, space, groups, passes, see_ctx, act_ctx, radius, part_size, steps, threads=0, mb=250,
+                   real=np.float32):
+        """Several groups of one model; `groups` is a list of record arrays (id order),
+        `passes` a list of ("see", seer, seen, self_see) / ("act", group) tuples.
+        Returns a list of RunResult (one per group; pairs summed over all passes)."""
+        fn = self.group_fns[real]
+        recs = [np.ascontiguousarray(r.copy()) for r in groups]
+        counts = np.array([r.shape[0] for r in recs], np.int32)
+        ptrs = (ctypes.c_void_p * len(recs))(*[r.ctypes.data for r in recs])
+        is_see = np.array([1 if p[0] == "see" else 0 for p in passes], np.int32)
+        seer = np.array([p[1] for p in passes], np.int32)
+        seen = np.array([p[2] if p[0] == "see" else p[1] for p in passes], np.int32)
+        self_see = np.array([int(p[3]) if p[0] == "see" else 0 for p in passes], np.int32)
+        see = np.ascontiguousarray(see_ctx) if see_ctx is not None else np.zeros(4, real)
+        act = np.ascontiguousarray(act_ctx) if act_ctx is not None else see
+        ms = ctypes.c_double()
+        sp = SPACE[space] if isinstance(space, str) else int(space)
+        ran = fn(model, sp, len(recs), counts.ctypes.data, ctypes.cast(ptrs, ctypes.c_void_p), see.ctypes.data,
+                 act.ctypes.data, real(radius), real(part_size), mb, steps, len(passes), is_see.ctypes.data,
+                 seer.ctypes.data, seen.ctypes.data, self_see.ctypes.data, threads, ctypes.byref(ms))
+        if ran != steps:
+            raise RuntimeError(f"oracle group run failed ({ran} of {steps} steps)")
+        pairs = int(self.pair_fns[real]()) if real in self.pair_fns else -1
+        return [RunResult(r, ms.value, pairs) for r in recs]
+
 
 _port = None
 _ref = None
@@ -142,7 +177,9 @@ def port():
             build_port()
         _port = _Impl(PORT_SO, {np.float32: ("oracle_run_f32", ctypes.c_float),
                                 np.float64: ("oracle_run_f64", ctypes.c_double)},
-                      {np.float32: "oracle_last_pairs_f32", np.float64: "oracle_last_pairs_f64"})
+                      {np.float32: "oracle_last_pairs_f32", np.float64: "oracle_last_pairs_f64"},
+                      {np.float32: ("oracle_run_groups_f32", ctypes.c_float),
+                       np.float64: ("oracle_run_groups_f64", ctypes.c_double)})
     return _port
 
 
@@ -152,7 +189,8 @@ def reference():
     if _ref is None:
         if not os.path.exists(REF_SO):
             return None
-        _ref = _Impl(REF_SO, {np.float32: ("ref_run", ctypes.c_float)})
+        _ref = _Impl(REF_SO, {np.float32: ("ref_run", ctypes.c_float)}, None,
+                     {np.float32: ("ref_run_groups", ctypes.c_float)})
     return _ref
 
 

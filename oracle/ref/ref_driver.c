@@ -137,6 +137,88 @@ int ref_run(int model, int space_type, int n, void *agents, const void *see_ctx,
     return run;
 }
 
+/* Several groups of one model in one reference state, with a pass list that mixes groups
+ * (the shape of test/test_combo.c:114-119).  Same contract as oracle_run_groups: pass k
+ * is tay_add_see(group pass_seer[k], group pass_seen[k]) or tay_add_act(group
+ * pass_seer[k]); agents[g] holds counts[g] records in id order on entry and on return. */
+int ref_run_groups(int model, int space_type, int ngroups, const int *counts, void **agents, const void *see_ctx,
+                   const void *act_ctx, float radius, float part_size, int mb, int steps, int npasses,
+                   const int *pass_is_see, const int *pass_seer, const int *pass_seen, const int *pass_self_see,
+                   int threads, double *ms_per_step) {
+    enum { kMaxGroups = 8 };
+    ensure_threads(threads);
+    unsigned agent_size = ref_agent_size(model);
+    if (!agent_size || ngroups <= 0 || ngroups > kMaxGroups || (model != REF_MODEL_TEST && model != REF_MODEL_BOIDS))
+        return 0;
+    for (int k = 0; k < npasses; ++k)
+        if (pass_seer[k] < 0 || pass_seer[k] >= ngroups || (pass_is_see[k] && (pass_seen[k] < 0 || pass_seen[k] >= ngroups)))
+            return 0;
+
+    static SeeContext test_see_ctx;
+    static ActContext test_act_ctx;
+    static OBoidsContext boids_ctx;
+
+    TayState *tay = tay_create_state();
+    TayGroup *groups[kMaxGroups];
+    float4 part = {{{part_size, part_size, part_size, part_size}}};
+    for (int g = 0; g < ngroups; ++g) {
+        groups[g] = tay_add_group(tay, agent_size, (unsigned)counts[g], TAY_TRUE);
+        tay_configure_space(tay, groups[g], (TaySpaceType)space_type, 3, part, mb);
+    }
+    float4 radii = {{{radius, radius, radius, radius}}};
+    if (model == REF_MODEL_TEST) {
+        memcpy(&test_see_ctx, see_ctx, sizeof(test_see_ctx));
+        memcpy(&test_act_ctx, act_ctx, sizeof(test_act_ctx));
+        radii.w = 0.0f;
+    }
+    else {
+        memcpy(&boids_ctx, see_ctx, sizeof(boids_ctx));
+    }
+    for (int k = 0; k < npasses; ++k) {
+        TayGroup *seer = groups[pass_seer[k]];
+        if (pass_is_see[k]) {
+            TayGroup *seen = groups[pass_seen[k]];
+            if (model == REF_MODEL_TEST)
+                tay_add_see(tay, seer, seen, (void (*)(void *, void *, void *))agent_see, "agent_see", radii,
+                            pass_self_see[k], &test_see_ctx, sizeof(test_see_ctx));
+            else
+                tay_add_see(tay, seer, seen, o_boids_see, "boids_see", radii, pass_self_see[k], &boids_ctx,
+                            sizeof(boids_ctx));
+        }
+        else {
+            if (model == REF_MODEL_TEST)
+                tay_add_act(tay, seer, (void (*)(void *, void *))agent_act, "agent_act", &test_act_ctx,
+                            sizeof(test_act_ctx));
+            else
+                tay_add_act(tay, seer, o_boids_act, "boids_act", &boids_ctx, sizeof(boids_ctx));
+        }
+    }
+    for (int g = 0; g < ngroups; ++g)
+        for (int i = 0; i < counts[g]; ++i) {
+            void *slot = tay_get_available_agent(tay, groups[g]);
+            memcpy(slot, (char *)agents[g] + (size_t)agent_size * i, agent_size);
+            tay_commit_available_agent(tay, groups[g]);
+        }
+
+    tay_simulation_start(tay);
+    int run = tay_run(tay, steps);
+    if (ms_per_step)
+        *ms_per_step = tay_get_ms_per_step_for_last_run(tay);
+    for (int g = 0; g < ngroups && run == steps; ++g)
+        for (int i = 0; i < counts[g]; ++i) {
+            char *a = (char *)tay_get_agent(tay, groups[g], i);
+            int id = agent_id(model, a);
+            if (id < 0 || id >= counts[g]) {
+                run = 0;
+                break;
+            }
+            memcpy((char *)agents[g] + (size_t)agent_size * id, a, agent_size);
+        }
+    tay_simulation_end(tay);
+    tay_destroy_state(tay);
+    return run;
+}
+
 int ref_space_enum(const char *name) {
     if (!strcmp(name, "simple")) return TAY_CPU_SIMPLE;
     if (!strcmp(name, "kd_tree")) return TAY_CPU_KD_TREE;

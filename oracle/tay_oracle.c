@@ -364,8 +364,8 @@ static void o_unsort(OGroup *g) {
  * self-see) over space_see_point_point_self_see */
 static unsigned long long O_NAME(pairs_by_thread)[64];
 
-static unsigned long long o_pair(const OGroup *g, const OPass *pass, unsigned seer_beg, unsigned seer_end, unsigned seen_beg,
-                   unsigned seen_end, int skip_self) {
+static unsigned long long o_pair(const OGroup *g, const OGroup *h, const OPass *pass, unsigned seer_beg, unsigned seer_end,
+                                 unsigned seen_beg, unsigned seen_end, int skip_self) {
     unsigned long long pairs = 0;
     for (unsigned s = seer_beg; s < seer_end; ++s) {
         char *seer = g->storage + (size_t)g->agent_size * s;
@@ -373,7 +373,7 @@ static unsigned long long o_pair(const OGroup *g, const OPass *pass, unsigned se
         for (unsigned b = seen_beg; b < seen_end; ++b) {
             if (skip_self && s == b)
                 continue;
-            const REAL *bp = o_pos(g, b);
+            const REAL *bp = o_pos(h, b);
             int skip = 0;
             for (int i = 0; i < 3; ++i) {
                 REAL d = sp[i] - bp[i];
@@ -385,7 +385,7 @@ static unsigned long long o_pair(const OGroup *g, const OPass *pass, unsigned se
             if (skip)
                 continue;
             ++pairs; /* the reference's narrow-phase counter, tay/space.c:56-60 */
-            pass->see(seer, g->storage + (size_t)g->agent_size * b, pass->ctx);
+            pass->see(seer, h->storage + (size_t)h->agent_size * b, pass->ctx);
         }
     }
     return pairs;
@@ -403,26 +403,33 @@ static void o_index_box(const OGroup *g, const REAL *bmin, const REAL *bmax, int
     }
 }
 
+/* g: the seer (or acting) group, h: the seen group (== g for a single-group pass) */
 typedef struct {
     OGroup *g;
+    OGroup *h;
     OPass *pass;
+    int skip_self;
 } OPassArg;
 
+/* tay/cpu_z_grid.c:283-321 (_see_func: seers walked cell run by cell run, seer box = the
+ * seer cell's box in the seer group's grid, widened by the radii) and :232-277
+ * (cpu_z_grid_see_seen: that box mapped to the seen group's grid); tay/cpu_grid.c:244-281
+ * the same on CpuGrid; tay/cpu_simple.c:6-38 against all seen agents. */
 static void o_see_task(OTask *task, int thread_i, int threads) {
     OPassArg *arg = (OPassArg *)task->arg;
     OGroup *g = arg->g;
+    OGroup *h = arg->h;
     OPass *pass = arg->pass;
-    int skip_self = !pass->self_see;
+    int skip_self = arg->skip_self;
     unsigned beg, end;
     o_range(g->count, thread_i, threads, &beg, &end);
 
     unsigned long long pairs = 0;
-    if (g->space == O_SPACE_SIMPLE) { /* tay/cpu_simple.c:6-38 */
-        O_NAME(pairs_by_thread)[thread_i] += o_pair(g, pass, beg, end, 0, g->count, skip_self);
+    if (g->space == O_SPACE_SIMPLE || h->space == O_SPACE_SIMPLE) {
+        O_NAME(pairs_by_thread)[thread_i] += o_pair(g, h, pass, beg, end, 0, h->count, skip_self);
         return;
     }
 
-    /* tay/cpu_z_grid.c:283-321 and tay/cpu_grid.c:244-281: seers walked cell run by cell run */
     unsigned s = beg;
     while (s < end) {
         const OTag *tag = o_tag(g, s);
@@ -451,22 +458,22 @@ static void o_see_task(OTask *task, int thread_i, int threads) {
             bmax[i] = m + g->cell_size[i] + pass->radii[i];
         }
         int lo[3], hi[3];
-        o_index_box(g, bmin, bmax, lo, hi);
+        o_index_box(h, bmin, bmax, lo, hi);
         for (int x = lo[0]; x <= hi[0]; ++x)
             for (int y = lo[1]; y <= hi[1]; ++y)
                 for (int z = lo[2]; z <= hi[2]; ++z) {
                     unsigned first, count;
-                    if (g->space == O_SPACE_Z_GRID) {
-                        const OZCell *c = g->zcells + o_morton3(x, y, z);
+                    if (h->space == O_SPACE_Z_GRID) {
+                        const OZCell *c = h->zcells + o_morton3(x, y, z);
                         first = c->first;
                         count = c->count;
                     }
                     else {
-                        const OGCell *c = g->gcells + (z * g->cell_counts[0] * g->cell_counts[1] + y * g->cell_counts[0] + x);
+                        const OGCell *c = h->gcells + (z * h->cell_counts[0] * h->cell_counts[1] + y * h->cell_counts[0] + x);
                         first = c->first;
                         count = c->count;
                     }
-                    pairs += o_pair(g, pass, s, run_end, first, first + count, skip_self);
+                    pairs += o_pair(g, h, pass, s, run_end, first, first + count, skip_self);
                 }
         s = run_end;
     }
@@ -512,6 +519,56 @@ unsigned O_NAME(oracle_agent_size)(int model) {
     return o_agent_size(model);
 }
 
+static void o_group_init(OGroup *g, unsigned agent_size, int space, int n, const void *agents, REAL part_size, int mb) {
+    memset(g, 0, sizeof(*g));
+    g->agent_size = agent_size;
+    g->count = (unsigned)n;
+    g->space = space;
+    g->part[0] = g->part[1] = g->part[2] = part_size;
+    g->storage = (char *)malloc((size_t)agent_size * (n ? n : 1));
+    g->sort_storage = (char *)malloc((size_t)agent_size * (n ? n : 1));
+    memcpy(g->storage, agents, (size_t)agent_size * n);
+    size_t shared = (size_t)mb << 20;
+    if (space == O_SPACE_Z_GRID) {
+        g->max_cells = (unsigned)(shared / 8u); /* sizeof(ZGridCell), tay/cpu_z_grid.c:7-10,152 */
+        g->zcells = (OZCell *)calloc(g->max_cells, sizeof(OZCell));
+    }
+    else if (space == O_SPACE_GRID) {
+        g->max_cells = (unsigned)(shared / 32u); /* sizeof(GridCell) on LP64, tay/cpu_grid.c:6-11,62 */
+        g->gcells = (OGCell *)calloc(g->max_cells, sizeof(OGCell));
+    }
+}
+
+/* Writes the group's records back to `agents` in id order; 0 if an id is out of range. */
+static int o_group_finish(OGroup *g, int model, void *agents) {
+    int ok = 1;
+    for (unsigned a = 0; a < g->count; ++a) {
+        const char *rec = g->storage + (size_t)g->agent_size * a;
+        int id = o_agent_id(model, rec);
+        if (id < 0 || id >= (int)g->count) {
+            ok = 0;
+            break;
+        }
+        memcpy((char *)agents + (size_t)g->agent_size * id, rec, g->agent_size);
+    }
+    free(g->storage);
+    free(g->sort_storage);
+    free(g->zcells);
+    free(g->gcells);
+    return ok;
+}
+
+static void o_sort(OGroup *g) {
+    if (g->space == O_SPACE_Z_GRID)
+        o_z_grid_sort(g);
+    else if (g->space == O_SPACE_GRID)
+        o_grid_sort(g);
+}
+
+static double o_seconds(const struct timespec *t0, const struct timespec *t1) {
+    return (double)(t1->tv_sec - t0->tv_sec) + 1e-9 * (double)(t1->tv_nsec - t0->tv_nsec);
+}
+
 /* Runs `steps` steps of one model on one group.  Same contract as the reference driver:
  * `agents` holds n AoS records in id order on entry and on return; the pass mask selects
  * which of the model's passes are registered, in the model's order; returns the number
@@ -527,23 +584,7 @@ int O_NAME(oracle_run)(int model, int space, int n, void *agents, const void *se
     O_NAME(pool_start)(threads);
 
     OGroup g;
-    memset(&g, 0, sizeof(g));
-    g.agent_size = agent_size;
-    g.count = (unsigned)n;
-    g.space = space;
-    g.part[0] = g.part[1] = g.part[2] = part_size;
-    g.storage = (char *)malloc((size_t)agent_size * n);
-    g.sort_storage = (char *)malloc((size_t)agent_size * n);
-    memcpy(g.storage, agents, (size_t)agent_size * n);
-    size_t shared = (size_t)mb << 20;
-    if (space == O_SPACE_Z_GRID) {
-        g.max_cells = (unsigned)(shared / 8u); /* sizeof(ZGridCell), tay/cpu_z_grid.c:7-10,152 */
-        g.zcells = (OZCell *)calloc(g.max_cells, sizeof(OZCell));
-    }
-    else if (space == O_SPACE_GRID) {
-        g.max_cells = (unsigned)(shared / 32u); /* sizeof(GridCell) on LP64, tay/cpu_grid.c:6-11,62 */
-        g.gcells = (OGCell *)calloc(g.max_cells, sizeof(OGCell));
-    }
+    o_group_init(&g, agent_size, space, n, agents, part_size, mb);
 
     /* contexts are copied, as the OpenCL path copies them per run (tay/ocl.c:252-259) */
     OTestActContext test_act;
@@ -582,36 +623,95 @@ int O_NAME(oracle_run)(int model, int space, int n, void *agents, const void *se
     struct timespec t0, t1;
     clock_gettime(CLOCK_MONOTONIC, &t0);
     for (int step = 0; step < steps; ++step) {
-        if (space == O_SPACE_Z_GRID)
-            o_z_grid_sort(&g);
-        else if (space == O_SPACE_GRID)
-            o_grid_sort(&g);
+        o_sort(&g);
         for (int p = 0; p < passes_count; ++p) {
-            OPassArg arg = {&g, passes + p};
+            OPassArg arg = {&g, &g, passes + p, passes[p].is_see && !passes[p].self_see};
             OTask task = {passes[p].is_see ? o_see_task : o_act_task, &arg};
             O_NAME(pool_run)(&task);
         }
         o_unsort(&g);
     }
     clock_gettime(CLOCK_MONOTONIC, &t1);
-    if (ms_per_step) {
-        double t = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
-        *ms_per_step = steps ? t / steps * 1000.0 : 0.0;
+    if (ms_per_step)
+        *ms_per_step = steps ? o_seconds(&t0, &t1) / steps * 1000.0 : 0.0;
+    return o_group_finish(&g, model, agents) ? steps : 0;
+}
+
+/* Runs `steps` steps of a state with several groups of one model (the test model's
+ * agent_see / agent_act or the boids' see / act), each group on its own structure of
+ * type `space`, with a pass list that mixes groups (tay/state.c:208-316; the combination
+ * test's pass list is test/test_combo.c:114-119).  Pass k is a see of group
+ * pass_seer[k] over group pass_seen[k] (is_see) or an act of group pass_seer[k]; a see
+ * pass skips seer == seen only inside one group and without self_see
+ * (tay/state_compile.c:109-120).  agents[g] holds counts[g] records in id order on entry
+ * and on return. */
+int O_NAME(oracle_run_groups)(int model, int space, int ngroups, const int *counts, void **agents, const void *see_ctx,
+                              const void *act_ctx, REAL radius, REAL part_size, int mb, int steps, int npasses,
+                              const int *pass_is_see, const int *pass_seer, const int *pass_seen,
+                              const int *pass_self_see, int threads, double *ms_per_step) {
+    enum { kMaxGroups = 8, kMaxPasses = 32 };
+    unsigned agent_size = o_agent_size(model);
+    if (!agent_size || ngroups <= 0 || ngroups > kMaxGroups || npasses < 0 || npasses > kMaxPasses || steps < 0)
+        return 0;
+    if (model != O_MODEL_TEST && model != O_MODEL_BOIDS)
+        return 0;
+    if (space != O_SPACE_SIMPLE && space != O_SPACE_GRID && space != O_SPACE_Z_GRID)
+        return 0;
+    for (int k = 0; k < ngroups; ++k)
+        if (counts[k] <= 0)
+            return 0;
+    for (int k = 0; k < npasses; ++k)
+        if (pass_seer[k] < 0 || pass_seer[k] >= ngroups || (pass_is_see[k] && (pass_seen[k] < 0 || pass_seen[k] >= ngroups)))
+            return 0;
+    O_NAME(pool_start)(threads);
+
+    OGroup g[kMaxGroups];
+    for (int k = 0; k < ngroups; ++k)
+        o_group_init(g + k, agent_size, space, counts[k], agents[k], part_size, mb);
+    OTestActContext test_act;
+    OBoidsContext boids;
+    if (model == O_MODEL_TEST)
+        memcpy(&test_act, act_ctx, sizeof(test_act));
+    else
+        memcpy(&boids, see_ctx, sizeof(boids));
+    OPass passes[kMaxPasses];
+    for (int k = 0; k < npasses; ++k) {
+        OPass p = {pass_is_see[k], 0, 0, {radius, radius, radius}, pass_self_see[k], 0};
+        if (model == O_MODEL_TEST) {
+            p.see = o_test_see;
+            p.act = o_test_act;
+            p.ctx = pass_is_see[k] ? 0 : &test_act;
+        }
+        else {
+            p.see = o_boids_see;
+            p.act = o_boids_act;
+            p.ctx = &boids;
+        }
+        passes[k] = p;
     }
 
-    int ok = steps;
-    for (unsigned a = 0; a < g.count; ++a) {
-        const char *rec = g.storage + (size_t)agent_size * a;
-        int id = o_agent_id(model, rec);
-        if (id < 0 || id >= n) {
-            ok = 0;
-            break;
+    memset(O_NAME(pairs_by_thread), 0, sizeof(O_NAME(pairs_by_thread)));
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    for (int step = 0; step < steps; ++step) {
+        for (int k = 0; k < ngroups; ++k)
+            o_sort(g + k);
+        for (int p = 0; p < npasses; ++p) {
+            OGroup *seer = g + pass_seer[p];
+            OGroup *seen = passes[p].is_see ? g + pass_seen[p] : seer;
+            OPassArg arg = {seer, seen, passes + p, passes[p].is_see && seer == seen && !passes[p].self_see};
+            OTask task = {passes[p].is_see ? o_see_task : o_act_task, &arg};
+            O_NAME(pool_run)(&task);
         }
-        memcpy((char *)agents + (size_t)agent_size * id, rec, agent_size);
+        for (int k = 0; k < ngroups; ++k)
+            o_unsort(g + k);
     }
-    free(g.storage);
-    free(g.sort_storage);
-    free(g.zcells);
-    free(g.gcells);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    if (ms_per_step)
+        *ms_per_step = steps ? o_seconds(&t0, &t1) / steps * 1000.0 : 0.0;
+    int ok = steps;
+    for (int k = 0; k < ngroups; ++k)
+        if (!o_group_finish(g + k, model, agents[k]))
+            ok = 0;
     return ok;
 }

@@ -51,6 +51,7 @@ TAY_SYMBOLS = [
     ("tay_add_see", None, [_VP, _VP, _VP, _VP, ctypes.c_char_p, Float4, ctypes.c_int, _VP, ctypes.c_uint]),
     ("tay_add_act", None, [_VP, _VP, _VP, ctypes.c_char_p, _VP, ctypes.c_uint]),
     ("tay_clear_all_agents", None, [_VP, _VP]),
+    ("tay_mark_agents_changed", None, [_VP, _VP]),
     ("tay_get_available_agent", _VP, [_VP, _VP]),
     ("tay_commit_available_agent", None, [_VP, _VP]),
     ("tay_get_agent", _VP, [_VP, _VP, ctypes.c_int]),
@@ -78,6 +79,8 @@ TAY_SYMBOLS = [
 TGPU_SYMBOLS = [
     ("tgpu_batch_create", ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(_VP)]),
     ("tgpu_batch_destroy", None, [_VP]),
+    ("tgpu_state_create", ctypes.c_int, [_VP, ctypes.c_int, _VP, ctypes.c_int, ctypes.POINTER(_VP)]),
+    ("tgpu_state_set_contexts", ctypes.c_int, [_VP, _VP, ctypes.c_int]),
     ("tgpu_batch_set_contexts", ctypes.c_int, [_VP, ctypes.c_int, _VP]),
     ("tgpu_batch_push", ctypes.c_int, [_VP, ctypes.c_int, _VP]),
     ("tgpu_batch_run", ctypes.c_int, [_VP, ctypes.c_int]),
@@ -207,6 +210,13 @@ class State:
         raw = ctypes.string_at(p, n * dtype.itemsize)
         return np.frombuffer(raw, dtype=dtype).copy()
 
+    def mark_changed(self, group):
+        self.L.tay_mark_agents_changed(self.ptr, group)
+
+    def agent_ptr(self, group, index=0):
+        """tay_get_agent: fetches the group's records when the device holds newer ones."""
+        return self.L.tay_get_agent(self.ptr, group, index)
+
     def start(self):
         self.L.tay_simulation_start(self.ptr)
         self.check("tay_simulation_start")
@@ -241,6 +251,10 @@ class TgpuGroup(ctypes.Structure):
                 ("shared_megabytes", ctypes.c_int), ("box_fixed", ctypes.c_int), ("box_min", ctypes.c_float * 4),
                 ("box_max", ctypes.c_float * 4), ("pass_count", ctypes.c_int),
                 ("passes", ctypes.POINTER(TgpuPass))]
+
+
+class TgpuStatePass(ctypes.Structure):
+    _fields_ = [("pass_", TgpuPass), ("seer_group", ctypes.c_int), ("seen_group", ctypes.c_int)]
 
 
 class Batch:

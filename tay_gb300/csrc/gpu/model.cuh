@@ -31,6 +31,8 @@ struct KernelDesc {
     void (*launch_see)(const SeeLaunch &L, size_t smem, cudaStream_t st);
     void (*launch_act)(const ActLaunch &L, cudaStream_t st);
     cudaError_t (*prepare)(size_t smem);  // raises the kernel's dynamic shared memory limit
+    int accumulates;                   // see kernel adds onto the seer's stored fields (several see
+                                       // passes of one group accumulate); 0: starts from zero
 };
 
 // A supported pass sequence: the func names in registration order, and the kernels

@@ -157,6 +157,31 @@ struct SeeAct {
     }
 };
 
+// boids_act as its own pass (after a boids_see of the same group, e.g. over another
+// group): folds the accumulators the see pass left in ACC0..2.
+struct Act {
+    using ActCtx = Ctx;
+    TGPU_D static void act(const PassIO &io, uint32_t i, const Ctx &c) {
+        float4 p = io.in_f4[POS][i], v = io.in_f4[VEL][i];
+        const float4 a0 = io.in_f4[ACC0][i], a1 = io.in_f4[ACC1][i], a2 = io.in_f4[ACC2][i];
+        Seer s;
+        s.cx = a0.x;
+        s.cy = a0.y;
+        s.cz = a0.z;
+        s.count = __float_as_int(a0.w);
+        s.ax = a1.x;
+        s.ay = a1.y;
+        s.az = a1.z;
+        s.sep_count = __float_as_int(a1.w);
+        s.sx = a2.x;
+        s.sy = a2.y;
+        s.sz = a2.z;
+        act_fn(p, v, s, c);
+        io.out_f4[POS][i] = p;
+        io.out_f4[VEL][i] = v;
+    }
+};
+
 struct Codec {
     static constexpr uint32_t kAgentBytes = 104;
     TGPU_D static void pack(const uint32_t *w, const PassIO &io, uint32_t i) {
@@ -193,16 +218,18 @@ const KernelDesc kKernels[] = {
      prepare_see_t<SeeOnly>},
     {"boids_see", "boids_act", bit(POS) | bit(VEL), 0, bit(POS) | bit(VEL), 2, launch_see_t<SeeAct>, nullptr,
      prepare_see_t<SeeAct>},
+    {nullptr, "boids_act", bit(POS) | bit(VEL), 0, 0, 0, nullptr, launch_act_t<Act>, nullptr},
 };
 
 const ProgramDesc kPrograms[] = {
     {1, {"boids_see"}, 1, {0}},
     {2, {"boids_see", "boids_act"}, 1, {1}},
+    {1, {"boids_act"}, 1, {2}},
 };
 
 const ModelDesc kModel = {
     "boids", 104, 5, 1, {kState, kState, kStep, kStep, kStep}, {kState}, (uint32_t)sizeof(Ctx), (uint32_t)sizeof(Ctx),
-    kKernels, 2, kPrograms, 2, pack_t<Codec>, unpack_t<Codec>,
+    kKernels, 3, kPrograms, 3, pack_t<Codec>, unpack_t<Codec>,
 };
 
 }  // namespace boids

@@ -7,6 +7,7 @@
 // (the step of tay/state.c:221-311: sort every group, run the passes in order, unsort).
 // Steps are captured once per buffer-parity pattern into CUDA graphs and replayed.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -337,6 +338,13 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E) {
             S.stage_cells = r.stage_cells;
             S.union_factor = r.union_factor;
             S.rows = b->cell_order == kOrderRows ? 1u : 0u;
+            if (r.seer_seg >= 0) {
+                // one seer segment; the seen agents are another segment's (or its own)
+                S.cta_offset = b->cta_begin[r.seer_seg];
+                S.ctas = b->cta_begin[r.seer_seg + 1] - b->cta_begin[r.seer_seg];
+                S.cross = r.seen_seg != r.seer_seg ? 1u : 0u;
+                S.seen_seg = (uint32_t)r.seen_seg;
+            }
             S.pairs = b->d_pairs;
             S.telemetry = b->d_telemetry;
             S.io = io;
@@ -351,6 +359,10 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E) {
             A.ctx = r.d_act_ctx;
             A.ctx_stride = (uint32_t)b->ctx_stride;
             A.tiles = b->tiles;
+            if (r.seer_seg >= 0) {
+                A.tile_offset = b->specs[r.seer_seg].tile_begin;
+                A.tiles = b->specs[r.seer_seg].tile_count;
+            }
             A.io = io;
             r.k->launch_act(A, st);
         }
@@ -518,41 +530,22 @@ int tgpu_batch_launches_per_step(const TgpuBatch *b) { return b ? b->launches_pe
 
 void tgpu_batch_destroy(TgpuBatch *b) { free_batch(b); }
 
-int tgpu_batch_create(const TgpuGroup *groups, int group_count, TgpuBatch **out) {
-    if (!out || !groups || group_count <= 0) return fail(TGPU_ERR_ARG, "no groups");
-    *out = nullptr;
-    const TgpuGroup &g0 = groups[0];
-    if (g0.pass_count <= 0 || !g0.passes) return fail(TGPU_ERR_ARG, "group has no passes");
-    const ModelDesc *m = find_model(g0.passes[0].func_name ? g0.passes[0].func_name : "");
-    if (!m) return fail(TGPU_ERR_UNKNOWN_FUNC, "no device model provides '%s'", g0.passes[0].func_name);
-    for (int k = 0; k < g0.pass_count; ++k)
-        if (!g0.passes[k].func_name || !model_has_func(m, g0.passes[k].func_name))
-            return fail(TGPU_ERR_UNKNOWN_FUNC, "func '%s' is not part of device model '%s'",
-                        g0.passes[k].func_name ? g0.passes[k].func_name : "(null)", m->name);
-    const int program = match_program(m, g0);
-    if (program < 0) return fail(TGPU_ERR_PROGRAM, "pass sequence not supported by device model '%s'", m->name);
+}  // extern "C"
 
-    TgpuBatch *b = new TgpuBatch();
-    b->m = m;
-    b->program = program;
-    b->nseg = group_count;
-    b->use_graphs = g_tuning.use_graphs != 0;
-    b->cell_order = g_tuning.cell_order == kOrderRows ? kOrderRows : kOrderMorton;
+namespace {
+
+// Segments of a new batch, one per group: packed agent ranges, radix tiles and see CTAs.
+// reach[g][a] is the largest see radius per axis of the passes whose seers are group g.
+int add_segments(TgpuBatch *b, const TgpuGroup *groups, int group_count, const std::vector<std::array<float, 3>> &reach) {
     uint32_t total = 0;
     for (int s = 0; s < group_count; ++s) {
         const TgpuGroup &g = groups[s];
-        if (g.agent_size != m->agent_bytes) {
-            free_batch(b);
-            return fail(TGPU_ERR_ARG, "group %d: agent size %u, device model '%s' expects %u", s, g.agent_size, m->name,
-                        m->agent_bytes);
-        }
-        if (match_program(m, g) != program) {
-            free_batch(b);
-            return fail(TGPU_ERR_ARG, "group %d: pass sequence differs from group 0", s);
-        }
+        if (g.agent_size != b->m->agent_bytes)
+            return fail(TGPU_ERR_ARG, "group %d: agent size %u, device model '%s' expects %u", s, g.agent_size,
+                        b->m->name, b->m->agent_bytes);
         HostSeg h;
         h.g = g;
-        h.passes.assign(g.passes, g.passes + g.pass_count);
+        if (g.passes && g.pass_count > 0) h.passes.assign(g.passes, g.passes + g.pass_count);
         h.g.passes = nullptr;
         for (int a = 0; a < 3; ++a) {
             h.host_min[a] = 0.0f;
@@ -569,119 +562,265 @@ int tgpu_batch_create(const TgpuGroup *groups, int group_count, TgpuBatch **out)
             sp.part[a] = part * g_tuning.cell_multiple;
             sp.box_min[a] = g.box_min[a];
             sp.box_max[a] = g.box_max[a];
-            float reach = 0.0f;
-            for (int k = 0; k < g.pass_count; ++k)
-                if (g.passes[k].is_see) reach = std::max(reach, g.passes[k].radii[a]);
-            sp.reach[a] = reach;
+            sp.reach[a] = reach[s][a];
         }
         sp.tile_begin = (uint32_t)b->tile_seg.size();
         sp.tile_count = (g.count + kSortTile - 1) / kSortTile;
         for (uint32_t t = 0; t < sp.tile_count; ++t) b->tile_seg.push_back((uint32_t)s);
+        b->cta_begin.push_back((uint32_t)b->cta.size());
         for (uint32_t c = 0; c < g.count; c += kSeeThreads) b->cta.push_back(make_uint2((uint32_t)s, total + c));
         b->specs.push_back(sp);
         total += g.count;
     }
+    b->cta_begin.push_back((uint32_t)b->cta.size());
     b->total = total;
     b->tiles = (uint32_t)b->tile_seg.size();
     b->ctas = (uint32_t)b->cta.size();
+    return TGPU_OK;
+}
 
-    auto bail = [&](int code) {
-        free_batch(b);
-        return code;
-    };
-#define CKB(call)                                                                                    \
+#define CKR(call)                                                                                    \
     do {                                                                                             \
         cudaError_t e_ = (call);                                                                     \
-        if (e_ != cudaSuccess) {                                                                     \
-            fail(TGPU_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));                     \
-            return bail(TGPU_ERR_CUDA);                                                              \
-        }                                                                                            \
+        if (e_ != cudaSuccess) return fail(TGPU_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
     } while (0)
 
-    CKB(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
-    CKB(cudaEventCreate(&b->e0));
-    CKB(cudaEventCreate(&b->e1));
-    const size_t n = std::max<uint32_t>(total, 1);
-    CKB(cudaMalloc(&b->d_specs, sizeof(SegmentSpec) * b->nseg));
-    CKB(cudaMalloc(&b->d_extent, sizeof(BoxAcc)));
-    CKB(cudaMalloc(&b->d_tile_seg, sizeof(uint32_t) * std::max<uint32_t>(b->tiles, 1)));
-    CKB(cudaMalloc(&b->d_cta, sizeof(uint2) * std::max<uint32_t>(b->ctas, 1)));
-    CKB(cudaMalloc(&b->d_box, sizeof(BoxAcc) * b->nseg));
-    if (b->tiles) CKB(cudaMemcpy(b->d_tile_seg, b->tile_seg.data(), sizeof(uint32_t) * b->tiles, cudaMemcpyHostToDevice));
-    if (b->ctas) CKB(cudaMemcpy(b->d_cta, b->cta.data(), sizeof(uint2) * b->ctas, cudaMemcpyHostToDevice));
+// Stream, events and every device buffer of a batch whose segments are set.
+int alloc_batch(TgpuBatch *b) {
+    const ModelDesc *m = b->m;
+    CKR(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+    CKR(cudaEventCreate(&b->e0));
+    CKR(cudaEventCreate(&b->e1));
+    const size_t n = std::max<uint32_t>(b->total, 1);
+    CKR(cudaMalloc(&b->d_specs, sizeof(SegmentSpec) * b->nseg));
+    CKR(cudaMalloc(&b->d_extent, sizeof(BoxAcc)));
+    CKR(cudaMalloc(&b->d_tile_seg, sizeof(uint32_t) * std::max<uint32_t>(b->tiles, 1)));
+    CKR(cudaMalloc(&b->d_cta, sizeof(uint2) * std::max<uint32_t>(b->ctas, 1)));
+    CKR(cudaMalloc(&b->d_box, sizeof(BoxAcc) * b->nseg));
+    if (b->tiles) CKR(cudaMemcpy(b->d_tile_seg, b->tile_seg.data(), sizeof(uint32_t) * b->tiles, cudaMemcpyHostToDevice));
+    if (b->ctas) CKR(cudaMemcpy(b->d_cta, b->cta.data(), sizeof(uint2) * b->ctas, cudaMemcpyHostToDevice));
     for (int c = 0; c < m->nf4; ++c) {
-        CKB(cudaMalloc(&b->f4[c][0], sizeof(float4) * n));
-        CKB(cudaMemset(b->f4[c][0], 0, sizeof(float4) * n));
+        CKR(cudaMalloc(&b->f4[c][0], sizeof(float4) * n));
+        CKR(cudaMemset(b->f4[c][0], 0, sizeof(float4) * n));
         if (m->role_f4[c] == kState) {
-            CKB(cudaMalloc(&b->f4[c][1], sizeof(float4) * n));
-            CKB(cudaMemset(b->f4[c][1], 0, sizeof(float4) * n));
+            CKR(cudaMalloc(&b->f4[c][1], sizeof(float4) * n));
+            CKR(cudaMemset(b->f4[c][1], 0, sizeof(float4) * n));
         }
     }
     for (int c = 0; c < m->nu32; ++c) {
-        CKB(cudaMalloc(&b->u32[c][0], sizeof(uint32_t) * n));
-        CKB(cudaMalloc(&b->u32[c][1], sizeof(uint32_t) * n));
+        CKR(cudaMalloc(&b->u32[c][0], sizeof(uint32_t) * n));
+        CKR(cudaMalloc(&b->u32[c][1], sizeof(uint32_t) * n));
     }
     for (int k = 0; k < 2; ++k) {
-        CKB(cudaMalloc(&b->keys[k], sizeof(uint32_t) * n));
-        CKB(cudaMalloc(&b->vals[k], sizeof(uint32_t) * n));
+        CKR(cudaMalloc(&b->keys[k], sizeof(uint32_t) * n));
+        CKR(cudaMalloc(&b->vals[k], sizeof(uint32_t) * n));
     }
     const size_t ncounts = 256ull * std::max<uint32_t>(b->tiles, 1);
-    CKB(cudaMalloc(&b->counts, sizeof(uint32_t) * ncounts));
-    CKB(cudaMalloc(&b->partials, sizeof(uint32_t) * ((ncounts + 4095) / 4096 + 1)));
-    if ((ncounts + 4095) / 4096 > 4096) {
-        fail(TGPU_ERR_ARG, "batch too large for the scan spine (%u tiles)", b->tiles);
-        return bail(TGPU_ERR_ARG);
-    }
-    CKB(cudaMalloc(&b->d_aos, (size_t)m->agent_bytes * n));
-    CKB(cudaMalloc(&b->d_pairs, sizeof(unsigned long long)));
-    CKB(cudaMalloc(&b->d_telemetry, sizeof(unsigned long long) * 8));
-
+    if ((ncounts + 4095) / 4096 > 4096) return fail(TGPU_ERR_ARG, "batch too large for the scan spine (%u tiles)", b->tiles);
+    CKR(cudaMalloc(&b->counts, sizeof(uint32_t) * ncounts));
+    CKR(cudaMalloc(&b->partials, sizeof(uint32_t) * ((ncounts + 4095) / 4096 + 1)));
+    CKR(cudaMalloc(&b->d_aos, (size_t)m->agent_bytes * n));
+    CKR(cudaMalloc(&b->d_pairs, sizeof(unsigned long long)));
+    CKR(cudaMalloc(&b->d_telemetry, sizeof(unsigned long long) * 8));
     b->ctx_stride = (std::max(m->see_ctx_bytes, m->act_ctx_bytes) + 15u) & ~15u;
+    return TGPU_OK;
+}
+
+// Per-kernel see configuration from the tuning: radii / context buffers, staging.
+int setup_see_run(TgpuBatch *b, KernelRun &r, int self_see) {
+    r.skip_self = self_see ? 0 : 1;
+    CKR(cudaMalloc(&r.d_radii, sizeof(float4) * b->nseg));
+    CKR(cudaMemset(r.d_radii, 0, sizeof(float4) * b->nseg));
+    CKR(cudaMalloc(&r.d_see_ctx, b->ctx_stride * b->nseg));
+    CKR(cudaMemset(r.d_see_ctx, 0, b->ctx_stride * b->nseg));
+    const uint32_t cap_default = r.k->staged_f4 <= 1 ? 1024u : 768u;
+    r.union_factor = g_tuning.union_factor;
+    if (g_tuning.stage && g_tuning.cell_order != kOrderRows) {
+        r.stage_cap = g_tuning.stage_cap ? g_tuning.stage_cap : cap_default;
+        r.stage_cells = g_tuning.stage_cells ? g_tuning.stage_cells : 512u;
+        r.smem = (size_t)r.k->staged_f4 * r.stage_cap * sizeof(float4) + (2ull * r.stage_cells + 1) * sizeof(uint32_t);
+    } else {
+        r.stage_cap = 0;
+        r.stage_cells = 0;
+        r.smem = 0;
+    }
+    if (r.smem > 220 * 1024) return fail(TGPU_ERR_ARG, "staging buffer of %zu bytes exceeds shared memory", r.smem);
+    CKR(r.k->prepare(r.smem));
+    return TGPU_OK;
+}
+
+#undef CKR
+
+const KernelDesc *find_kernel(const ModelDesc *m, const char *see, const char *act) {
+    for (int k = 0; k < m->nkernels; ++k) {
+        const KernelDesc &d = m->kernels[k];
+        const bool see_ok = see ? (d.see && !strcmp(d.see, see)) : !d.see;
+        const bool act_ok = act ? (d.act && !strcmp(d.act, act)) : !d.act;
+        if (see_ok && act_ok) return &d;
+    }
+    return nullptr;
+}
+
+// Contexts and radii of a state-level pass list (tgpu_state_create), one per seer segment.
+int upload_state_contexts(TgpuBatch *b) {
+    std::vector<char> buf(b->ctx_stride);
+    for (size_t k = 0; k < b->runs.size(); ++k) {
+        const KernelRun &r = b->runs[k];
+        const TgpuPass &tp = b->state_passes[k].pass;
+        std::fill(buf.begin(), buf.end(), 0);
+        if (tp.context && tp.context_size) memcpy(buf.data(), tp.context, std::min((size_t)tp.context_size, b->ctx_stride));
+        char *dst = r.k->see ? r.d_see_ctx : r.d_act_ctx;
+        CK(cudaMemcpyAsync(dst + (size_t)r.seer_seg * b->ctx_stride, buf.data(), b->ctx_stride, cudaMemcpyHostToDevice,
+                           b->st));
+        if (r.k->see) {
+            float4 rr = make_float4(tp.radii[0], tp.radii[1], tp.radii[2], tp.radii[3]);
+            CK(cudaMemcpyAsync(r.d_radii + r.seer_seg, &rr, sizeof(float4), cudaMemcpyHostToDevice, b->st));
+        }
+    }
+    CK(cudaStreamSynchronize(b->st));
+    return TGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tgpu_batch_create(const TgpuGroup *groups, int group_count, TgpuBatch **out) {
+    if (!out || !groups || group_count <= 0) return fail(TGPU_ERR_ARG, "no groups");
+    *out = nullptr;
+    const TgpuGroup &g0 = groups[0];
+    if (g0.pass_count <= 0 || !g0.passes) return fail(TGPU_ERR_ARG, "group has no passes");
+    const ModelDesc *m = find_model(g0.passes[0].func_name ? g0.passes[0].func_name : "");
+    if (!m) return fail(TGPU_ERR_UNKNOWN_FUNC, "no device model provides '%s'", g0.passes[0].func_name);
+    for (int k = 0; k < g0.pass_count; ++k)
+        if (!g0.passes[k].func_name || !model_has_func(m, g0.passes[k].func_name))
+            return fail(TGPU_ERR_UNKNOWN_FUNC, "func '%s' is not part of device model '%s'",
+                        g0.passes[k].func_name ? g0.passes[k].func_name : "(null)", m->name);
+    const int program = match_program(m, g0);
+    if (program < 0) return fail(TGPU_ERR_PROGRAM, "pass sequence not supported by device model '%s'", m->name);
+    std::vector<std::array<float, 3>> reach(group_count);
+    for (int s = 0; s < group_count; ++s) {
+        const TgpuGroup &g = groups[s];
+        if (!g.passes || match_program(m, g) != program) return fail(TGPU_ERR_ARG, "group %d: pass sequence differs from group 0", s);
+        for (int a = 0; a < 3; ++a) {
+            reach[s][a] = 0.0f;
+            for (int k = 0; k < g.pass_count; ++k)
+                if (g.passes[k].is_see) reach[s][a] = std::max(reach[s][a], g.passes[k].radii[a]);
+        }
+    }
+
+    TgpuBatch *b = new TgpuBatch();
+    b->m = m;
+    b->program = program;
+    b->nseg = group_count;
+    b->use_graphs = g_tuning.use_graphs != 0;
+    b->cell_order = g_tuning.cell_order == kOrderRows ? kOrderRows : kOrderMorton;
+    int rc = add_segments(b, groups, group_count, reach);
+    if (!rc) rc = alloc_batch(b);
     const ProgramDesc &pd = m->programs[program];
     int cursor = 0;
-    for (int k = 0; k < pd.kernels; ++k) {
+    for (int k = 0; k < pd.kernels && !rc; ++k) {
         KernelRun r{};
         r.k = &m->kernels[pd.kernel_index[k]];
         r.see_pass = r.k->see ? pass_index(g0, r.k->see, cursor) : -1;
         r.act_pass = r.k->act ? pass_index(g0, r.k->act, r.see_pass >= 0 ? r.see_pass + 1 : cursor) : -1;
         cursor = std::max(r.see_pass, r.act_pass) + 1;
-        if (r.see_pass >= 0) {
-            const TgpuPass &tp = g0.passes[r.see_pass];
-            r.skip_self = tp.self_see ? 0 : 1;
-            CKB(cudaMalloc(&r.d_radii, sizeof(float4) * b->nseg));
-            CKB(cudaMalloc(&r.d_see_ctx, b->ctx_stride * b->nseg));
-            const uint32_t cap_default = r.k->staged_f4 <= 1 ? 1024u : 768u;
-            r.union_factor = g_tuning.union_factor;
-            if (g_tuning.stage && g_tuning.cell_order != kOrderRows) {
-                r.stage_cap = g_tuning.stage_cap ? g_tuning.stage_cap : cap_default;
-                r.stage_cells = g_tuning.stage_cells ? g_tuning.stage_cells : 512u;
-                r.smem = (size_t)r.k->staged_f4 * r.stage_cap * sizeof(float4) +
-                         (2ull * r.stage_cells + 1) * sizeof(uint32_t);
-            } else {
-                r.stage_cap = 0;
-                r.stage_cells = 0;
-                r.smem = 0;
-            }
-            if (r.smem > 220 * 1024) {
-                fail(TGPU_ERR_ARG, "staging buffer of %zu bytes exceeds shared memory", r.smem);
-                return bail(TGPU_ERR_ARG);
-            }
-            CKB(r.k->prepare(r.smem));
+        if (r.see_pass >= 0) rc = setup_see_run(b, r, g0.passes[r.see_pass].self_see);
+        if (!rc && r.act_pass >= 0) {
+            if (cudaMalloc(&r.d_act_ctx, b->ctx_stride * b->nseg) != cudaSuccess)
+                rc = fail(TGPU_ERR_CUDA, "cudaMalloc of the act contexts failed");
         }
-        if (r.act_pass >= 0) CKB(cudaMalloc(&r.d_act_ctx, b->ctx_stride * b->nseg));
         b->runs.push_back(r);
     }
-    for (int s = 0; s < b->nseg; ++s) {
-        int rc = upload_contexts(b, s);
-        if (rc) return bail(rc);
+    for (int s = 0; s < b->nseg && !rc; ++s) rc = upload_contexts(b, s);
+    if (rc) {
+        free_batch(b);
+        return rc;
     }
     *out = b;
-#undef CKB
     return TGPU_OK;
+}
+
+int tgpu_state_create(const TgpuGroup *groups, int group_count, const TgpuStatePass *passes, int pass_count,
+                      TgpuBatch **out) {
+    if (!out || !groups || group_count <= 0 || !passes || pass_count <= 0) return fail(TGPU_ERR_ARG, "no groups or passes");
+    *out = nullptr;
+    const ModelDesc *m = find_model(passes[0].pass.func_name ? passes[0].pass.func_name : "");
+    if (!m) return fail(TGPU_ERR_UNKNOWN_FUNC, "no device model provides '%s'", passes[0].pass.func_name);
+    std::vector<std::array<float, 3>> reach(group_count);
+    for (auto &r : reach) r = {0.0f, 0.0f, 0.0f};
+    std::vector<int> see_passes(group_count, 0);
+    std::vector<const KernelDesc *> kernels(pass_count);
+    for (int k = 0; k < pass_count; ++k) {
+        const TgpuStatePass &sp = passes[k];
+        const char *fn = sp.pass.func_name;
+        if (!fn || !model_has_func(m, fn))
+            return fail(TGPU_ERR_UNKNOWN_FUNC, "func '%s' is not part of device model '%s'", fn ? fn : "(null)", m->name);
+        if (sp.seer_group < 0 || sp.seer_group >= group_count || (sp.pass.is_see && (sp.seen_group < 0 || sp.seen_group >= group_count)))
+            return fail(TGPU_ERR_ARG, "pass %d: group index out of range", k);
+        kernels[k] = sp.pass.is_see ? find_kernel(m, fn, nullptr) : find_kernel(m, nullptr, fn);
+        if (!kernels[k])
+            return fail(TGPU_ERR_PROGRAM, "pass %d: device model '%s' has no standalone %s kernel for '%s'", k, m->name,
+                        sp.pass.is_see ? "see" : "act", fn);
+        const KernelDesc &d = *kernels[k];
+        for (int c = 0; c < m->nf4; ++c)
+            if (m->role_f4[c] == kState && (d.writes_f4 >> c & 1u) && (d.seen_f4 >> c & 1u))
+                return fail(TGPU_ERR_PROGRAM, "pass %d: '%s' writes a stream other agents see", k, fn);
+        if (sp.pass.is_see) {
+            if (++see_passes[sp.seer_group] > 1 && !d.accumulates)
+                return fail(TGPU_ERR_PROGRAM, "group %d: several '%s' see passes, and the see function of model '%s' does not accumulate",
+                            sp.seer_group, fn, m->name);
+            for (int a = 0; a < 3; ++a) reach[sp.seer_group][a] = std::max(reach[sp.seer_group][a], sp.pass.radii[a]);
+        }
+    }
+
+    TgpuBatch *b = new TgpuBatch();
+    b->m = m;
+    b->program = -1;
+    b->nseg = group_count;
+    b->use_graphs = g_tuning.use_graphs != 0;
+    b->cell_order = g_tuning.cell_order == kOrderRows ? kOrderRows : kOrderMorton;
+    b->state_passes.assign(passes, passes + pass_count);
+    int rc = add_segments(b, groups, group_count, reach);
+    if (!rc) rc = alloc_batch(b);
+    for (int k = 0; k < pass_count && !rc; ++k) {
+        const TgpuStatePass &sp = passes[k];
+        KernelRun r{};
+        r.k = kernels[k];
+        r.see_pass = sp.pass.is_see ? k : -1;
+        r.act_pass = sp.pass.is_see ? -1 : k;
+        r.seer_seg = sp.seer_group;
+        r.seen_seg = sp.pass.is_see ? sp.seen_group : sp.seer_group;
+        if (sp.pass.is_see) {
+            rc = setup_see_run(b, r, sp.pass.self_see || sp.seen_group != sp.seer_group);
+        } else if (cudaMalloc(&r.d_act_ctx, b->ctx_stride * b->nseg) != cudaSuccess) {
+            rc = fail(TGPU_ERR_CUDA, "cudaMalloc of the act contexts failed");
+        }
+        b->runs.push_back(r);
+    }
+    if (!rc) rc = upload_state_contexts(b);
+    if (rc) {
+        free_batch(b);
+        return rc;
+    }
+    *out = b;
+    return TGPU_OK;
+}
+
+int tgpu_state_set_contexts(TgpuBatch *b, const TgpuStatePass *passes, int pass_count) {
+    if (!b || !passes || b->state_passes.empty()) return fail(TGPU_ERR_ARG, "not a state batch");
+    if (pass_count != (int)b->state_passes.size()) return fail(TGPU_ERR_ARG, "pass count changed");
+    for (int k = 0; k < pass_count; ++k) {
+        b->state_passes[k].pass.context = passes[k].pass.context;
+        b->state_passes[k].pass.context_size = passes[k].pass.context_size;
+        for (int a = 0; a < 4; ++a) b->state_passes[k].pass.radii[a] = passes[k].pass.radii[a];
+    }
+    return upload_state_contexts(b);
 }
 
 int tgpu_batch_set_contexts(TgpuBatch *b, int group, const TgpuGroup *desc) {
     if (!b || !desc || group < 0 || group >= b->nseg) return fail(TGPU_ERR_ARG, "bad group");
+    if (!b->state_passes.empty()) return fail(TGPU_ERR_ARG, "state batch: use tgpu_state_set_contexts");
     if (desc->pass_count != (int)b->hs[group].passes.size()) return fail(TGPU_ERR_ARG, "pass count changed");
     for (int k = 0; k < desc->pass_count; ++k) {
         b->hs[group].passes[k].context = desc->passes[k].context;
@@ -788,7 +927,14 @@ int tgpu_batch_fetch(TgpuBatch *b, int group, void *host) {
     if (!sp.count) return TGPU_OK;
     uint32_t *aos = b->d_aos + (size_t)sp.begin * (b->m->agent_bytes / 4);
     PassIO io = make_io(b, nullptr, false, sp.begin);
-    b->m->unpack(aos, sp.count, io, (uint32_t)b->program, b->st);
+    // state batches: accumulators are visible when no act pass consumed them
+    uint32_t program = (uint32_t)b->program;
+    if (!b->state_passes.empty()) {
+        program = 0u;
+        for (const auto &p : b->state_passes)
+            if (!p.pass.is_see) program = 0xFFFFFFFFu;
+    }
+    b->m->unpack(aos, sp.count, io, program, b->st);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(host, aos, (size_t)sp.count * b->m->agent_bytes, cudaMemcpyDeviceToHost, b->st));
     CK(cudaStreamSynchronize(b->st));

@@ -19,6 +19,8 @@ struct KernelRun {
     size_t smem = 0;
     uint32_t stage_cap = 0, stage_cells = 0, union_factor = 2;
     int skip_self = 0;
+    int seer_seg = -1;  // state batches: the pass's seer (acting) segment; -1: every segment
+    int seen_seg = -1;  // state batches: the segment whose agents a see pass reads
 };
 
 struct HostSeg {
@@ -49,6 +51,8 @@ struct TgpuBatch {
     std::vector<SegmentSpec> specs;
     std::vector<uint32_t> tile_seg;
     std::vector<uint2> cta;
+    std::vector<uint32_t> cta_begin;           // first CTA of each segment, + total
+    std::vector<TgpuStatePass> state_passes;   // tgpu_state_create: the state's pass list
     uint32_t tiles = 0, ctas = 0, key_bits = 0;
     bool specs_dirty = true;
 

@@ -163,12 +163,13 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
     __shared__ uint32_t warp_sums[kSeeThreads / 32];
     __shared__ uint32_t s_total;
 
-    const uint2 cta = L.cta_table[blockIdx.x];
+    const uint2 cta = L.cta_table[L.cta_offset + blockIdx.x];
     const uint32_t seg = cta.x;
-    const SegmentSpec S = L.specs[seg];
-    const BoxAcc B = L.box[seg];
-    const Grid g = segment_grid(S, B);
-    const float pad = grid_pad(g, S, B);
+    const SegmentSpec S = L.specs[seg];                       // seers
+    const SegmentSpec T = L.specs[L.cross ? L.seen_seg : seg];  // seen agents: grid and table
+    const BoxAcc B = L.box[L.cross ? L.seen_seg : seg];
+    const Grid g = segment_grid(T, B);
+    const float pad = grid_pad(g, T, B);
     const float4 r4 = L.radii[seg];
     const typename P::SeeCtx &sctx = *reinterpret_cast<const typename P::SeeCtx *>(L.ctx + (size_t)seg * L.ctx_stride);
     const typename P::ActCtx &actx =
@@ -209,7 +210,7 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
     const int hx = hbox[3] - H0x + 1, hy = hbox[4] - H0y + 1, hz = hbox[5] - H0z + 1;
     const long long V = (hx > 0 && hy > 0 && hz > 0) ? (long long)hx * hy * hz : 0;
     bool staged = L.stage_cap > 0 && V > 0 && V <= (long long)L.stage_cells;
-    const uint2 *table = L.table + S.table_base;
+    const uint2 *table = L.table + T.table_base;
     const uint32_t dx0 = (uint32_t)g.dims[0], dy0 = (uint32_t)g.dims[1];
 
     uint32_t total = 0;
@@ -363,12 +364,13 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
 template <class P>
 __global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
     using namespace see_detail;
-    const uint2 cta = L.cta_table[blockIdx.x];
+    const uint2 cta = L.cta_table[L.cta_offset + blockIdx.x];
     const uint32_t seg = cta.x;
-    const SegmentSpec S = L.specs[seg];
-    const BoxAcc B = L.box[seg];
-    const Grid g = segment_grid(S, B);
-    const float pad = grid_pad(g, S, B);
+    const SegmentSpec S = L.specs[seg];                       // seers
+    const SegmentSpec T = L.specs[L.cross ? L.seen_seg : seg];  // seen agents: grid and table
+    const BoxAcc B = L.box[L.cross ? L.seen_seg : seg];
+    const Grid g = segment_grid(T, B);
+    const float pad = grid_pad(g, T, B);
     const float4 r4 = L.radii[seg];
     const typename P::SeeCtx &sctx = *reinterpret_cast<const typename P::SeeCtx *>(L.ctx + (size_t)seg * L.ctx_stride);
     const typename P::ActCtx &actx =
@@ -388,7 +390,7 @@ __global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
         axis_range(sp.y, r4.y, g.origin[1], g.inv_cs[1], g.dims[1], pad, lo[1], hi[1]);
         axis_range(sp.z, r4.z, g.origin[2], g.inv_cs[2], g.dims[2], pad, lo[2], hi[2]);
     }
-    const uint32_t *rows = reinterpret_cast<const uint32_t *>(L.table + S.table_base);
+    const uint32_t *rows = reinterpret_cast<const uint32_t *>(L.table + T.table_base);
     const uint32_t rw = (uint32_t)g.dims[0] + 1u, dy0 = (uint32_t)g.dims[1];
     GlobalSeen<P::kSeenF4> acc;
 #pragma unroll
@@ -434,10 +436,11 @@ __global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
 
 template <class A>
 __global__ void __launch_bounds__(kSortThreads) act_kernel(ActLaunch L) {
-    const uint32_t seg = L.tile_seg[blockIdx.x];
+    const uint32_t tile = L.tile_offset + blockIdx.x;
+    const uint32_t seg = L.tile_seg[tile];
     const SegmentSpec S = L.specs[seg];
     const typename A::ActCtx &actx = *reinterpret_cast<const typename A::ActCtx *>(L.ctx + (size_t)seg * L.ctx_stride);
-    const uint32_t t = blockIdx.x - S.tile_begin;
+    const uint32_t t = tile - S.tile_begin;
     const uint32_t beg = S.begin + t * kSortTile;
     const uint32_t end = min(beg + (uint32_t)kSortTile, S.begin + S.count);
     for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads) A::act(L.io, i, actx);

@@ -55,6 +55,9 @@ struct SeeLaunch {
     uint32_t stage_cells;     // halo cells per CTA
     uint32_t union_factor;    // a warp walks its union box when union <= factor x lane box
     uint32_t rows;            // 1: the table is in row order (see_rows_kernel)
+    uint32_t cta_offset;      // first entry of cta_table this launch covers
+    uint32_t cross;           // 1: the seen agents are segment seen_seg (a two-group pass)
+    uint32_t seen_seg;
     unsigned long long *pairs;  // box-test passes, summed over the launch
     // telemetry (the reference's TAY_TELEMETRY counters, tay/space.c:50-60, plus the
     // kernel's own paths): [0] candidates box-tested (broad phase), [1] staged CTAs,
@@ -70,6 +73,7 @@ struct ActLaunch {
     const char *ctx;
     uint32_t ctx_stride;
     uint32_t tiles;
+    uint32_t tile_offset;     // first entry of tile_seg this launch covers
     PassIO io;
 };
 

@@ -3,9 +3,13 @@
  * Keeps the reference's state model (tay/state.c, tay/state.h:217-271): a state owns up
  * to TAY_MAX_GROUPS groups with host AoS storage and up to TAY_MAX_PASSES passes in
  * registration order; errors are sticky and functions return 0/NULL on failure.
- * tay_run compiles the state on first use (tay/state_compile.c:5-175), pushes the host
- * agents, runs the steps on the device and fetches the agents back in cell order, like
- * the reference's OpenCL path does for every run (tay/state.c:208-218, 313-315).
+ * tay_run compiles the state on first use (tay/state_compile.c:5-175) and runs the steps
+ * on the device.  The agents stay on the device between runs: a group's host records are
+ * pushed only when they changed (commit, clear, configure, tay_mark_agents_changed; the
+ * reference's OpenCL path pushes on configure/clear, tay/ocl.c:238-250) and fetched back
+ * in cell order only when the host reads them (tay_get_agent, tay_simulation_end), where
+ * the OpenCL path fetches after every run (tay/ocl.c:261-272).  States with several
+ * groups, mixed by their see passes, run as one state batch (tgpu_state_create).
  * The device work is delegated to the C ABI in tay_gpu.h.
  */
 #include "tay.h"
@@ -35,6 +39,9 @@ struct TayGroup {
     int box_fixed;
     float4 box_min, box_max;
     unsigned id;
+    int host_dirty; /* host records changed since the last push */
+    int host_stale; /* the device holds newer records than the host */
+    int slot;       /* segment of the compiled batch, or -1 */
 };
 
 struct TayPass {
@@ -62,10 +69,15 @@ struct TayState {
     unsigned next_group_id;
     /* compiled form */
     TgpuBatch *batch;
-    int gpu_group; /* index of the GPU group */
+    int gpu_group;                  /* single-group states: index of the group */
+    int ngpu;                       /* groups of the compiled state */
+    int gpu_slots[TAY_MAX_GROUPS];  /* group index of each segment */
+    int state_batch;                /* the batch was made by tgpu_state_create */
     TgpuPass tpasses[TAY_MAX_PASSES];
-    TgpuGroup tgroup;
-    unsigned version; /* bumped by every successful validation */
+    TgpuStatePass spasses[TAY_MAX_PASSES];
+    TgpuGroup tgroup;               /* single-group form (tgpu_batch_create, tay_run_batch) */
+    TgpuGroup tgroups[TAY_MAX_GROUPS];
+    unsigned version;               /* bumped by every successful validation */
 };
 
 static unsigned g_threads = 0;
@@ -89,9 +101,36 @@ TayState *tay_create_state(void) {
     return state;
 }
 
+static int device_fail(TayState *state, int rc);
+
+/* Brings a group's host records up to date with the device (a lazy fetch). */
+static int fetch_group(TayState *state, TayGroup *g) {
+    if (!g->host_stale) return 1;
+    g->host_stale = 0;
+    if (!state->batch || g->slot < 0) return 1;
+    int rc = tgpu_batch_fetch(state->batch, g->slot, g->storage);
+    return rc == TGPU_OK ? 1 : device_fail(state, rc);
+}
+
+static int sync_host(TayState *state) {
+    int ok = 1;
+    for (int i = 0; i < TAY_MAX_GROUPS; ++i)
+        if (group_active(state->groups + i) && !fetch_group(state, state->groups + i)) ok = 0;
+    return ok;
+}
+
+/* Drops the device batch after fetching what only the device holds. */
 static void release_batch(TayState *state) {
-    if (state->batch) tgpu_batch_destroy(state->batch);
+    if (state->batch) {
+        sync_host(state);
+        tgpu_batch_destroy(state->batch);
+    }
     state->batch = 0;
+    for (int i = 0; i < TAY_MAX_GROUPS; ++i) {
+        state->groups[i].slot = -1;
+        state->groups[i].host_dirty = 1;
+        state->groups[i].host_stale = 0;
+    }
 }
 
 static void drop_batch_cache(void);
@@ -143,11 +182,15 @@ TayGroup *tay_add_group(TayState *state, unsigned agent_size, unsigned agent_cap
     g->dims = 3;
     g->part.x = g->part.y = g->part.z = g->part.w = 1.0f;
     g->id = state->next_group_id++;
+    g->host_dirty = 1;
+    g->slot = -1;
     state->recompile = 1;
     return g;
 }
 
 void tay_configure_space(TayState *state, TayGroup *group, TaySpaceType space_type, int space_dims, float4 min_part_sizes, int shared_size_in_megabytes) {
+    fetch_group(state, group);
+    group->host_dirty = 1;
     group->type = space_type;
     group->dims = space_dims;
     group->part = min_part_sizes;
@@ -199,6 +242,8 @@ void tay_add_act(TayState *state, TayGroup *act_group, void (*func)(void *, void
 }
 
 void tay_clear_all_agents(TayState *state, TayGroup *group) {
+    group->host_stale = 0;
+    group->host_dirty = 1;
     group->count = 0;
     state->recompile = 1;
 }
@@ -212,11 +257,15 @@ void *tay_get_available_agent(TayState *state, TayGroup *group) {
 }
 
 void tay_commit_available_agent(TayState *state, TayGroup *group) {
+    fetch_group(state, group);
+    group->host_dirty = 1;
     if (group->count < group->capacity) ++group->count;
     state->recompile = 1;
 }
 
 unsigned tay_commit_agents(TayState *state, TayGroup *group, const void *records, unsigned count) {
+    fetch_group(state, group);
+    group->host_dirty = 1;
     unsigned room = group->capacity - group->count;
     unsigned n = count < room ? count : room;
     if (n < count) set_error(state, TAY_ERROR_GROUP_INDEX_OUT_OF_RANGE, "group is full");
@@ -232,8 +281,14 @@ unsigned tay_get_agent_count(TayState *state, TayGroup *group) {
 }
 
 void *tay_get_agent(TayState *state, TayGroup *group, int index) {
-    (void)state;
+    if (!fetch_group(state, group)) return 0;
     return group->storage + (size_t)group->agent_size * (size_t)index;
+}
+
+void tay_mark_agents_changed(TayState *state, TayGroup *group) {
+    (void)state;
+    group->host_stale = 0;
+    group->host_dirty = 1;
 }
 
 void tay_simulation_start(TayState *state) {
@@ -254,12 +309,19 @@ void tay_simulation_end(TayState *state) {
     release_batch(state);
 }
 
+static int find_group(const TayState *state, const TayGroup *g) {
+    for (int i = 0; i < TAY_MAX_GROUPS; ++i)
+        if (g == state->groups + i) return group_active(g) ? i : -1;
+    return -1;
+}
+
 /* Validation (the GPU counterpart of tay/state_compile.c:5-175): checks the groups and
  * passes and fills the device descriptors; the device batch is built lazily. */
 static int validate(TayState *state) {
     if (!state->recompile) return 1;
     release_batch(state);
     state->gpu_group = -1;
+    state->ngpu = 0;
     for (int i = 0; i < TAY_MAX_GROUPS; ++i) {
         TayGroup *g = state->groups + i;
         if (!group_active(g)) continue;
@@ -276,21 +338,22 @@ static int validate(TayState *state) {
             set_error(state, TAY_ERROR_NOT_IMPLEMENTED, "the GPU Z-grid supports 3 dimensions");
             return 0;
         }
-        if (state->gpu_group >= 0) {
-            set_error(state, TAY_ERROR_NOT_IMPLEMENTED, "the GPU Z-grid runs one group per state");
-            return 0;
-        }
-        state->gpu_group = i;
+        g->slot = state->ngpu;
+        state->gpu_slots[state->ngpu++] = i;
     }
-    if (state->gpu_group < 0) {
+    if (state->ngpu == 0) {
         set_error(state, TAY_ERROR_STATE_STATUS, "no active group");
         return 0;
     }
-    TayGroup *g = state->groups + state->gpu_group;
+    if (state->passes_count == 0) {
+        set_error(state, TAY_ERROR_STATE_STATUS, "no passes");
+        return 0;
+    }
     for (unsigned k = 0; k < state->passes_count; ++k) {
         TayPass *p = state->passes + k;
-        if (p->seer_group != g || p->seen_group != g) {
-            set_error(state, TAY_ERROR_NOT_IMPLEMENTED, "pass %u: see passes between two groups are not supported on the GPU path", k);
+        int seer = find_group(state, p->seer_group), seen = find_group(state, p->seen_group);
+        if (seer < 0 || (p->is_see && seen < 0)) {
+            set_error(state, TAY_ERROR_GROUP_INDEX_OUT_OF_RANGE, "pass %u: group is not part of this state", k);
             return 0;
         }
         if (p->context && !p->context_size) {
@@ -315,20 +378,31 @@ static int validate(TayState *state) {
         t->self_see = p->self_see;
         t->context = p->context;
         t->context_size = p->context_size;
+        TgpuStatePass *sp = state->spasses + k;
+        sp->pass = *t;
+        sp->seer_group = state->groups[seer].slot;
+        sp->seen_group = p->is_see ? state->groups[seen].slot : sp->seer_group;
     }
-    TgpuGroup *tg = &state->tgroup;
-    memset(tg, 0, sizeof(*tg));
-    tg->agent_size = g->agent_size;
-    tg->count = g->count;
-    for (int a = 0; a < 4; ++a) {
-        tg->min_part_sizes[a] = g->part.arr[a];
-        tg->box_min[a] = g->box_min.arr[a];
-        tg->box_max[a] = g->box_max.arr[a];
+    for (int s = 0; s < state->ngpu; ++s) {
+        const TayGroup *g = state->groups + state->gpu_slots[s];
+        TgpuGroup *tg = state->tgroups + s;
+        memset(tg, 0, sizeof(*tg));
+        tg->agent_size = g->agent_size;
+        tg->count = g->count;
+        for (int a = 0; a < 4; ++a) {
+            tg->min_part_sizes[a] = g->part.arr[a];
+            tg->box_min[a] = g->box_min.arr[a];
+            tg->box_max[a] = g->box_max.arr[a];
+        }
+        tg->shared_megabytes = g->shared_mb;
+        tg->box_fixed = g->box_fixed;
     }
-    tg->shared_megabytes = g->shared_mb;
-    tg->box_fixed = g->box_fixed;
-    tg->pass_count = (int)state->passes_count;
-    tg->passes = state->tpasses;
+    if (state->ngpu == 1) {
+        state->gpu_group = state->gpu_slots[0];
+        state->tgroup = state->tgroups[0];
+        state->tgroup.pass_count = (int)state->passes_count;
+        state->tgroup.passes = state->tpasses;
+    }
     if (!tgpu_model_of(state->tpasses[0].func_name)) {
         set_error(state, TAY_ERROR_DEVICE_MODEL, "no device model provides '%s'", state->tpasses[0].func_name);
         return 0;
@@ -338,15 +412,24 @@ static int validate(TayState *state) {
     return 1;
 }
 
+/* A single group whose pass list a device model runs as a program gets a program batch
+ * (fused see + act kernels, and tay_run_batch); anything else a state batch. */
 static int compile(TayState *state) {
     if (!validate(state)) return 0;
     if (state->batch) return 1;
-    int rc = tgpu_batch_create(&state->tgroup, 1, &state->batch);
+    int rc = TGPU_ERR_PROGRAM;
+    state->state_batch = 0;
+    if (state->ngpu == 1) rc = tgpu_batch_create(&state->tgroup, 1, &state->batch);
+    if (rc == TGPU_ERR_PROGRAM) {
+        state->state_batch = 1;
+        rc = tgpu_state_create(state->tgroups, state->ngpu, state->spasses, (int)state->passes_count, &state->batch);
+    }
     if (rc != TGPU_OK) {
         set_error(state, rc == TGPU_ERR_CUDA ? TAY_ERROR_CUDA : TAY_ERROR_DEVICE_MODEL, "%s", tgpu_last_error());
         state->batch = 0;
         return 0;
     }
+    for (int s = 0; s < state->ngpu; ++s) state->groups[state->gpu_slots[s]].host_dirty = 1;
     return 1;
 }
 
@@ -369,12 +452,17 @@ int tay_run(TayState *state, int steps) {
     }
     if (!compile(state)) return 0;
     double t0 = now_s();
-    TayGroup *g = state->groups + state->gpu_group;
-    int rc = tgpu_batch_set_contexts(state->batch, 0, &state->tgroup);
-    if (rc == TGPU_OK) rc = tgpu_batch_push(state->batch, 0, g->storage);
+    int rc = state->state_batch ? tgpu_state_set_contexts(state->batch, state->spasses, (int)state->passes_count)
+                                : tgpu_batch_set_contexts(state->batch, 0, &state->tgroup);
+    for (int s = 0; s < state->ngpu && rc == TGPU_OK; ++s) {
+        TayGroup *g = state->groups + state->gpu_slots[s];
+        if (!g->host_dirty) continue;
+        rc = tgpu_batch_push(state->batch, s, g->storage);
+        g->host_dirty = 0;
+    }
     if (rc == TGPU_OK) rc = tgpu_batch_run(state->batch, steps);
-    if (rc == TGPU_OK) rc = tgpu_batch_fetch(state->batch, 0, g->storage);
     if (rc != TGPU_OK) return device_fail(state, rc);
+    for (int s = 0; s < state->ngpu; ++s) state->groups[state->gpu_slots[s]].host_stale = 1;
     double t = now_s() - t0;
     state->ms_per_step = steps ? t / (double)steps * 1000.0 : 0.0;
     state->device_ms = tgpu_batch_last_device_ms(state->batch);
@@ -423,6 +511,11 @@ static TgpuBatch *batch_for(TayState **states, int count) {
             return 0;
         }
         if (!validate(states[i])) return 0;
+        if (states[i]->ngpu != 1) {
+            set_error(states[i], TAY_ERROR_BATCH, "tay_run_batch runs states of one group each");
+            return 0;
+        }
+        if (!sync_host(states[i])) return 0;
     }
     if (!cache_matches(states, count)) {
         drop_batch_cache();
@@ -457,10 +550,16 @@ static int push_all(TgpuBatch *b, TayState **states, int count) {
     return rc;
 }
 
+/* Batched runs keep the eager contract: every state's records are pushed before and
+ * fetched after; each state's own device copy is then out of date. */
 static int fetch_all(TgpuBatch *b, TayState **states, int count) {
     int rc = TGPU_OK;
-    for (int i = 0; i < count && rc == TGPU_OK; ++i)
-        rc = tgpu_batch_fetch(b, i, states[i]->groups[states[i]->gpu_group].storage);
+    for (int i = 0; i < count && rc == TGPU_OK; ++i) {
+        TayGroup *g = states[i]->groups + states[i]->gpu_group;
+        rc = tgpu_batch_fetch(b, i, g->storage);
+        g->host_dirty = 1;
+        g->host_stale = 0;
+    }
     return rc;
 }
 

@@ -140,3 +140,31 @@ def run(setup: Setup, recs: np.ndarray, steps: int):
     st.end()
     st.close()
     return out
+
+
+def run_groups(dtype, funcs, groups, passes, see_ctx, act_ctx, radius, part, steps, mb=8):
+    """A state of several groups of one model mixed by its passes, through the C API.
+    `funcs` = (see func name, act func name); `groups` = record arrays (id order);
+    `passes` = ("see", seer, seen, self_see) / ("act", group) tuples in registration
+    order.  Returns each group's records ordered by id."""
+    from . import api
+
+    st = api.State()
+    gs = []
+    for recs in groups:
+        g = st.add_group(dtype.itemsize, recs.shape[0], True)
+        st.configure_space(g, api.TAY_GPU_Z_GRID, 3, part, mb)
+        gs.append(g)
+    for p in passes:
+        if p[0] == "see":
+            st.add_see(gs[p[1]], gs[p[2]], funcs[0], radius, p[3], see_ctx)
+        else:
+            st.add_act(gs[p[1]], funcs[1], act_ctx)
+    for g, recs in zip(gs, groups):
+        st.commit(g, recs)
+    st.start()
+    st.run(steps)
+    out = [by_id(st.agents(g, dtype)) for g in gs]
+    st.end()
+    st.close()
+    return out

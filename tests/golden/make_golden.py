@@ -17,6 +17,13 @@ Cases (small enough for CpuSimple):
   boids_full     same, see + act, 5 steps, CpuZGrid
   sph_density    6x6x6 lattice, density pass only, 1 step, CpuZGrid
   sph_full       8x8x8 lattice, all four passes, 5 steps, CpuZGrid
+
+Two-group cases (golden_groups.npz; the pass list of test/test_combo.c:114-119):
+  combo_see_*    test model, groups of 1200 and 800 agents, see a->a, a->b, b->b, b->a,
+                 1 step, CpuSimple / CpuZGrid
+  combo_full_*   the same passes + act a, act b, 5 steps, CpuGrid / CpuZGrid
+  boids_pair     boids groups of 1500 and 1000, see a->b, b->a, act a, act b, 3 steps,
+                 CpuZGrid
 """
 import os
 import sys
@@ -53,6 +60,32 @@ def cases():
     yield "sph_full", O.MODEL_SPH, "z_grid", srec8, sctx, sctx, 0.04, 0.04, 5, 15
 
 
+COMBO = [("see", 0, 0, False), ("see", 0, 1, False), ("see", 1, 1, False), ("see", 1, 0, False)]
+COMBO_FULL = COMBO + [("act", 0), ("act", 1)]
+BOIDS_PAIR = [("see", 0, 1, False), ("see", 1, 0, False), ("act", 0), ("act", 1)]
+
+
+def group_cases():
+    a = W.basic_points(1200, seed=111)
+    b = W.basic_points(800, seed=112)
+    recs = [O.make_records(O.MODEL_TEST, a.p, a.v), O.make_records(O.MODEL_TEST, b.p, b.v)]
+    see, act = np.array([50, 50, 50, 0], np.float32), O.test_act_context(np.float32)
+    for space in ("simple", "z_grid"):
+        yield f"combo_see_{space}", O.MODEL_TEST, space, recs, COMBO, see, act, 50.0, 1
+    for space in ("grid", "z_grid"):
+        yield f"combo_full_{space}", O.MODEL_TEST, space, recs, COMBO_FULL, see, act, 50.0, 5
+    ba = W.boids_points(1500, seed=113, clusters=2, side=120.0)
+    bb = W.boids_points(1000, seed=114, clusters=2, side=120.0)
+    brecs = [O.make_records(O.MODEL_BOIDS, ba.p, ba.v), O.make_records(O.MODEL_BOIDS, bb.p, bb.v)]
+    bctx = O.boids_context(np.float32)
+    yield "boids_pair", O.MODEL_BOIDS, "z_grid", brecs, BOIDS_PAIR, bctx, bctx, 10.0, 3
+
+
+def pass_table(passes):
+    return np.array([[1 if p[0] == "see" else 0, p[1], p[2] if p[0] == "see" else p[1], int(p[3]) if p[0] == "see" else 0]
+                     for p in passes], np.int64)
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     O.build_reference(ref_root)
@@ -70,6 +103,19 @@ def main():
         out[f"{name}__act"] = act
         print(f"{name}: {rec.shape[0]} agents, {steps} steps")
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
+    out = {}
+    for name, model, space, recs, passes, see, act, radius, steps in group_cases():
+        res = ref.run_groups(model, space, recs, passes, see, act, radius, radius, steps, threads=4)
+        for k, (rec, r) in enumerate(zip(recs, res)):
+            out[f"{name}__in{k}"] = rec
+            out[f"{name}__out{k}"] = r.records
+        out[f"{name}__meta"] = np.array([model, O.SPACE[space], steps, len(recs)], np.int64)
+        out[f"{name}__passes"] = pass_table(passes)
+        out[f"{name}__params"] = np.array([radius, radius], np.float64)
+        out[f"{name}__see"] = see
+        out[f"{name}__act"] = act
+        print(f"{name}: {[r.shape[0] for r in recs]} agents, {steps} steps")
+    np.savez_compressed(os.path.join(HERE, "golden_groups.npz"), **out)
 
 
 if __name__ == "__main__":

@@ -52,16 +52,66 @@ def test_non_point_group_is_rejected(built):
     assert _run_error(st) == "TAY_ERROR_POINT_NONPOINT_MISMATCH"
 
 
-def test_two_group_see_is_not_implemented(built):
+def _two_boids_groups(st):
+    groups = []
+    for _ in range(2):
+        g = st.add_group(M.BOIDS_RECORD.itemsize, 10, True)
+        st.configure_space(g, api.TAY_GPU_Z_GRID, 3, 10.0, 8)
+        groups.append(g)
+    return groups
+
+
+def test_two_sees_of_one_group_need_an_accumulating_model(built):
+    """Boids' see function starts its accumulators from zero, so one boids group cannot
+    have two see passes (here over itself and over a second group); refused before any
+    device work."""
     st = api.State()
-    a = st.add_group(80, 10, True)
-    b = st.add_group(80, 10, True)
-    for g in (a, b):
-        st.configure_space(g, api.TAY_GPU_Z_GRID, 3, 50.0, 8)
+    a, b = _two_boids_groups(st)
+    ctx = M.boids_context()
+    st.add_see(a, a, "boids_see", 10.0, False, ctx)
+    st.add_see(a, b, "boids_see", 10.0, False, ctx)
+    st.add_act(a, "boids_act", ctx)
+    st.start()
+    assert _run_error(st) == "TAY_ERROR_DEVICE_MODEL"
+    assert "does not accumulate" in st.message()
+
+
+def test_pass_on_a_group_of_another_state(built):
+    st = api.State()
+    other = api.State()
+    a = st.add_group(M.TEST_RECORD.itemsize, 10, True)
+    st.configure_space(a, api.TAY_GPU_Z_GRID, 3, 50.0, 8)
+    b = other.add_group(M.TEST_RECORD.itemsize, 10, True)
     see, _ = M.test_contexts()
     st.add_see(a, b, "agent_see", 50.0, False, see)
     st.start()
-    assert _run_error(st) == "TAY_ERROR_NOT_IMPLEMENTED"
+    assert _run_error(st) == "TAY_ERROR_GROUP_INDEX_OUT_OF_RANGE"
+
+
+def test_state_pass_list_is_checked_before_device_work(built):
+    """tgpu_state_create refuses unknown functions, bad group indices and passes without
+    a standalone kernel before touching the device."""
+    import ctypes
+
+    L = api.lib()
+    gd = (api.TgpuGroup * 2)()
+    for g in gd:
+        g.agent_size = 80
+        g.count = 10
+        g.min_part_sizes[:] = [50.0] * 4
+        g.shared_megabytes = 1
+    sp = (api.TgpuStatePass * 2)()
+    sp[0].pass_.func_name = b"agent_see"
+    sp[0].pass_.is_see = 1
+    sp[0].seer_group, sp[0].seen_group = 0, 2
+    sp[1].pass_.func_name = b"agent_act"
+    sp[1].seer_group = 1
+    out = ctypes.c_void_p()
+    assert L.tgpu_state_create(gd, 2, sp, 2, ctypes.byref(out)) == 1  # TGPU_ERR_ARG
+    assert b"out of range" in L.tgpu_last_error()
+    sp[0].seen_group = 1
+    sp[1].pass_.func_name = b"sph_integrate"
+    assert L.tgpu_state_create(gd, 2, sp, 2, ctypes.byref(out)) == 2  # TGPU_ERR_UNKNOWN_FUNC
 
 
 def test_group_capacity_is_enforced(built):
@@ -116,8 +166,8 @@ def test_unsupported_pass_sequence_is_refused_before_device_work(built):
     import ctypes
 
     out = ctypes.c_void_p()
-    # agent_act alone is a supported sequence; boids_act alone is not
-    passes[0].func_name = b"boids_act"
-    gd[0].agent_size = 104
+    # agent_act alone is a supported sequence; sph_force alone is not
+    passes[0].func_name = b"sph_force"
+    gd[0].agent_size = 72
     assert L.tgpu_batch_create(gd, 1, ctypes.byref(out)) == 3  # TGPU_ERR_PROGRAM
     assert b"not supported" in L.tgpu_last_error()

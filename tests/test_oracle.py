@@ -108,3 +108,40 @@ def test_port_bit_exact_with_live_reference(port, model, space):
     a = port.run(model, space, rec, see, act, radius, radius, steps, mask, threads=3).records
     b = O.reference().run(model, space, rec, see, act, radius, radius, steps, mask, threads=3).records
     assert same_records(model, a, b)
+
+
+GOLDEN_GROUPS = os.path.join(os.path.dirname(__file__), "golden", "golden_groups.npz")
+GG = np.load(GOLDEN_GROUPS)
+GG_NAMES = sorted({k.split("__")[0] for k in GG.files})
+
+
+def group_passes(table):
+    """Pass tuples from the stored [is_see, seer, seen, self_see] rows."""
+    return [("see", int(s), int(t), bool(ss)) if see else ("act", int(s)) for see, s, t, ss in table]
+
+
+@pytest.mark.parametrize("name", GG_NAMES)
+def test_port_groups_bit_exact_with_golden(port, name):
+    """Two groups mixed by their see passes (the combination test's pass list)."""
+    model, space, steps, ngroups = (int(x) for x in GG[f"{name}__meta"])
+    radius, part = (float(x) for x in GG[f"{name}__params"])
+    recs = [GG[f"{name}__in{k}"] for k in range(ngroups)]
+    res = port.run_groups(model, SPACE_NAME[space], recs, group_passes(GG[f"{name}__passes"]), GG[f"{name}__see"],
+                          GG[f"{name}__act"], radius, part, steps, threads=3)
+    for k, r in enumerate(res):
+        assert same_records(model, r.records, GG[f"{name}__out{k}"]), (name, k)
+    if name.startswith("combo_see"):
+        assert res[0].records["b_buffer_count"].sum() > 0
+
+
+@pytest.mark.skipif(O.reference() is None, reason="reference source tree not built on this machine")
+def test_port_groups_bit_exact_with_live_reference(port):
+    a = W.basic_points(900, seed=31)
+    b = W.basic_points(1300, seed=32)
+    recs = [O.make_records(O.MODEL_TEST, a.p, a.v), O.make_records(O.MODEL_TEST, b.p, b.v)]
+    passes = [("see", 1, 0, False), ("see", 0, 0, True), ("act", 1), ("see", 0, 1, False), ("act", 0)]
+    see, act = np.array([60, 40, 50, 0], np.float32), O.test_act_context(np.float32)
+    x = port.run_groups(O.MODEL_TEST, "z_grid", recs, passes, see, act, 50.0, 50.0, 4, threads=3)
+    y = O.reference().run_groups(O.MODEL_TEST, "z_grid", recs, passes, see, act, 50.0, 50.0, 4, threads=3)
+    for r, s in zip(x, y):
+        assert same_records(O.MODEL_TEST, r.records, s.records)
