@@ -54,6 +54,9 @@ typedef struct TgpuGroup {
     float box_max[4];
     int pass_count;
     const TgpuPass *passes;
+    int dims;                 /* tay_configure_space dims: 1, 2 or 3 (0 means 3); the box test
+                                 and the grid use the first `dims` axes (min over seer and
+                                 seen group for a two-group pass), tay/space.c:62-68 */
 } TgpuGroup;
 
 /* Creates a batch of `group_count` groups; all must resolve to the same model and the

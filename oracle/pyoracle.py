@@ -112,10 +112,16 @@ def _bind_groups(lib, name, real_c):
 
 
 class _Impl:
-    def __init__(self, so, names, pair_fns=None, group_names=None):
+    def __init__(self, so, names, pair_fns=None, group_names=None, space_fns=None):
         if not os.path.exists(so):
             raise FileNotFoundError(so)
         self.lib = ctypes.CDLL(so)
+        self.space_fns = {}
+        for real, (nm, c) in (space_fns or {}).items():
+            f = getattr(self.lib, nm)
+            f.restype = None
+            f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+            self.space_fns[real] = (f, c)
         self.fns = {real: _bind(self.lib, nm, c) for real, (nm, c) in names.items()}
         self.group_fns = {real: _bind_groups(self.lib, nm, c) for real, (nm, c) in (group_names or {}).items()}
         self.pair_fns = {}
@@ -125,8 +131,16 @@ class _Impl:
             f.argtypes = []
             self.pair_fns[real] = f
 
+    def set_space(self, dims=3, box=None, real=np.float32):
+        """Space options of the following runs: dims (1..3) and a fixed box ((min3, max3))."""
+        f, _ = self.space_fns[real]
+        lo = np.zeros(3, real) if box is None else np.asarray(box[0], real)
+        hi = np.zeros(3, real) if box is None else np.asarray(box[1], real)
+        f(int(dims), 0 if box is None else 1, lo.ctypes.data, hi.ctypes.data)
+
     def run(self, model, space, records, see_ctx, act_ctx, radius, part_size, steps, pass_mask, threads=0, mb=250,
-            real=np.float32):
+            real=np.float32, dims=3, box=None):
+        self.set_space(dims, box, real)
         fn = self.fns[real]
         rec = np.ascontiguousarray(records.copy())
         see = np.ascontiguousarray(see_ctx) if see_ctx is not None else np.zeros(4, real)
@@ -141,10 +155,11 @@ class _Impl:
         return RunResult(rec, ms.value, pairs)
 
     def run_groups(self, model, space, groups, passes, see_ctx, act_ctx, radius, part_size, steps, threads=0, mb=250,
-                   real=np.float32):
+                   real=np.float32, dims=3, box=None):
         """Several groups of one model; `groups` is a list of record arrays (id order),
         `passes` a list of ("see", seer, seen, self_see) / ("act", group) tuples.
         Returns a list of RunResult (one per group; pairs summed over all passes)."""
+        self.set_space(dims, box, real)
         fn = self.group_fns[real]
         recs = [np.ascontiguousarray(r.copy()) for r in groups]
         counts = np.array([r.shape[0] for r in recs], np.int32)
@@ -179,7 +194,9 @@ def port():
                                 np.float64: ("oracle_run_f64", ctypes.c_double)},
                       {np.float32: "oracle_last_pairs_f32", np.float64: "oracle_last_pairs_f64"},
                       {np.float32: ("oracle_run_groups_f32", ctypes.c_float),
-                       np.float64: ("oracle_run_groups_f64", ctypes.c_double)})
+                       np.float64: ("oracle_run_groups_f64", ctypes.c_double)},
+                      {np.float32: ("oracle_set_space_f32", ctypes.c_float),
+                       np.float64: ("oracle_set_space_f64", ctypes.c_double)})
     return _port
 
 
@@ -190,7 +207,8 @@ def reference():
         if not os.path.exists(REF_SO):
             return None
         _ref = _Impl(REF_SO, {np.float32: ("ref_run", ctypes.c_float)}, None,
-                     {np.float32: ("ref_run_groups", ctypes.c_float)})
+                     {np.float32: ("ref_run_groups", ctypes.c_float)},
+                     {np.float32: ("ref_set_space", ctypes.c_float)})
     return _ref
 
 

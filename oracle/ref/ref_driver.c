@@ -29,6 +29,28 @@ enum { REF_PASS_SEE0 = 1, REF_PASS_ACT0 = 2, REF_PASS_SEE1 = 4, REF_PASS_ACT1 = 
 
 static unsigned ref_threads = 0;
 
+/* Space options of the following runs: tay_configure_space dims and tay_fix_space_box. */
+static int ref_dims = 3;
+static int ref_box_fixed = 0;
+static float4 ref_box_min, ref_box_max;
+
+void ref_set_space(int dims, int box_fixed, const float *box_min, const float *box_max) {
+    ref_dims = dims;
+    ref_box_fixed = box_fixed;
+    for (int i = 0; i < 3; ++i) {
+        ref_box_min.arr[i] = box_fixed ? box_min[i] : 0.0f;
+        ref_box_max.arr[i] = box_fixed ? box_max[i] : 0.0f;
+    }
+    ref_box_min.arr[3] = ref_box_max.arr[3] = 0.0f;
+}
+
+static void configure(TayState *tay, TayGroup *group, int space_type, float part_size, int mb) {
+    float4 part = {{{part_size, part_size, part_size, part_size}}};
+    tay_configure_space(tay, group, (TaySpaceType)space_type, ref_dims, part, mb);
+    if (ref_box_fixed)
+        tay_fix_space_box(tay, group, ref_box_min, ref_box_max);
+}
+
 static void ensure_threads(int threads) {
     if (threads <= 0)
         threads = 1;
@@ -77,8 +99,7 @@ int ref_run(int model, int space_type, int n, void *agents, const void *see_ctx,
 
     TayState *tay = tay_create_state();
     TayGroup *group = tay_add_group(tay, agent_size, (unsigned)n, TAY_TRUE);
-    float4 part = {{{part_size, part_size, part_size, part_size}}};
-    tay_configure_space(tay, group, (TaySpaceType)space_type, 3, part, mb);
+    configure(tay, group, space_type, part_size, mb);
 
     float4 radii = {{{radius, radius, radius, radius}}};
     if (model == REF_MODEL_TEST) {
@@ -160,10 +181,9 @@ int ref_run_groups(int model, int space_type, int ngroups, const int *counts, vo
 
     TayState *tay = tay_create_state();
     TayGroup *groups[kMaxGroups];
-    float4 part = {{{part_size, part_size, part_size, part_size}}};
     for (int g = 0; g < ngroups; ++g) {
         groups[g] = tay_add_group(tay, agent_size, (unsigned)counts[g], TAY_TRUE);
-        tay_configure_space(tay, groups[g], (TaySpaceType)space_type, 3, part, mb);
+        configure(tay, groups[g], space_type, part_size, mb);
     }
     float4 radii = {{{radius, radius, radius, radius}}};
     if (model == REF_MODEL_TEST) {

@@ -169,6 +169,9 @@ typedef struct {
     unsigned agent_size;
     unsigned count;
     int space;
+    int dims;                         /* tay_configure_space dims: 1..3 */
+    int box_fixed;                    /* tay_fix_space_box */
+    REAL fixed_min[3], fixed_max[3];
     REAL part[3];
     REAL box_min[3], box_max[3];
     /* grids */
@@ -199,15 +202,22 @@ static inline OTag *o_tag(const OGroup *g, unsigned i) {
     return (OTag *)(g->storage + (size_t)g->agent_size * i);
 }
 
-/* tay/space.c:9-48 */
+/* tay/space.c:9-48: the agents' box over the space's dims, unless the box is fixed */
 static void o_update_box(OGroup *g) {
+    if (g->box_fixed) {
+        for (int i = 0; i < 3; ++i) {
+            g->box_min[i] = g->fixed_min[i];
+            g->box_max[i] = g->fixed_max[i];
+        }
+        return;
+    }
     for (int i = 0; i < 3; ++i) {
         g->box_min[i] = O_BIG;
         g->box_max[i] = -O_BIG;
     }
     for (unsigned a = 0; a < g->count; ++a) {
         const REAL *p = o_pos(g, a);
-        for (int i = 0; i < 3; ++i) {
+        for (int i = 0; i < g->dims; ++i) {
             if (p[i] < g->box_min[i])
                 g->box_min[i] = p[i];
             if (p[i] > g->box_max[i])
@@ -238,9 +248,10 @@ static inline unsigned o_compact10(unsigned v) {
     return v;
 }
 
-static inline void o_cell_indices(const REAL *p, const REAL *o, const REAL *s, int *idx) {
+/* tay/cpu_z_grid.c:12-35, tay/cpu_grid.c:18-40: the first `dims` indices; the others 0 */
+static inline void o_cell_indices(const REAL *p, const REAL *o, const REAL *s, int *idx, int dims) {
     for (int i = 0; i < 3; ++i)
-        idx[i] = (int)O_FLOOR((p[i] - o[i]) / s[i]);
+        idx[i] = i < dims ? (int)O_FLOOR((p[i] - o[i]) / s[i]) : 0;
 }
 
 /* tay/cpu_z_grid.c:156-221 */
@@ -275,7 +286,7 @@ static void o_z_grid_sort(OGroup *g) {
 
     for (unsigned a = 0; a < g->count; ++a) {
         int idx[3];
-        o_cell_indices(o_pos(g, a), g->origin, g->cell_size, idx);
+        o_cell_indices(o_pos(g, a), g->origin, g->cell_size, idx, 3);
         unsigned cell_i = o_morton3(idx[0], idx[1], idx[2]);
         OTag *tag = o_tag(g, a);
         tag->part_i = cell_i;
@@ -303,6 +314,10 @@ static void o_grid_sort(OGroup *g) {
     unsigned long long cells_count = 1;
     for (int i = 0; i < 3; ++i) {
         g->origin[i] = g->box_min[i];
+        g->cell_counts[i] = 1;
+        g->cell_size[i] = 1;
+    }
+    for (int i = 0; i < g->dims; ++i) {
         REAL cs = g->part[i];
         REAL size = g->box_max[i] - g->box_min[i] + cs * (REAL)0.001;
         g->cell_counts[i] = (int)O_CEIL(size / cs);
@@ -311,8 +326,8 @@ static void o_grid_sort(OGroup *g) {
     }
     if (cells_count > g->max_cells) {
         REAL volume_ratio = (REAL)cells_count / (REAL)g->max_cells;
-        REAL ratio = O_POW(volume_ratio, (REAL)1 / (REAL)3);
-        for (int i = 0; i < 3; ++i) {
+        REAL ratio = O_POW(volume_ratio, (REAL)1 / (REAL)g->dims);
+        for (int i = 0; i < g->dims; ++i) {
             REAL cs = g->part[i];
             REAL size = g->box_max[i] - g->box_min[i] + cs * (REAL)0.001;
             g->cell_counts[i] = (int)O_CEIL(g->cell_counts[i] / ratio);
@@ -321,7 +336,7 @@ static void o_grid_sort(OGroup *g) {
     }
     for (unsigned a = 0; a < g->count; ++a) {
         int idx[3];
-        o_cell_indices(o_pos(g, a), g->origin, g->cell_size, idx);
+        o_cell_indices(o_pos(g, a), g->origin, g->cell_size, idx, g->dims);
         unsigned cell_i = (unsigned)(idx[2] * g->cell_counts[0] * g->cell_counts[1] + idx[1] * g->cell_counts[0] + idx[0]);
         OGCell *cell = g->gcells + cell_i;
         if (cell->count == 0) {
@@ -365,7 +380,7 @@ static void o_unsort(OGroup *g) {
 static unsigned long long O_NAME(pairs_by_thread)[64];
 
 static unsigned long long o_pair(const OGroup *g, const OGroup *h, const OPass *pass, unsigned seer_beg, unsigned seer_end,
-                                 unsigned seen_beg, unsigned seen_end, int skip_self) {
+                                 unsigned seen_beg, unsigned seen_end, int skip_self, int dims) {
     unsigned long long pairs = 0;
     for (unsigned s = seer_beg; s < seer_end; ++s) {
         char *seer = g->storage + (size_t)g->agent_size * s;
@@ -375,7 +390,7 @@ static unsigned long long o_pair(const OGroup *g, const OGroup *h, const OPass *
                 continue;
             const REAL *bp = o_pos(h, b);
             int skip = 0;
-            for (int i = 0; i < 3; ++i) {
+            for (int i = 0; i < dims; ++i) {
                 REAL d = sp[i] - bp[i];
                 if (d < -pass->radii[i] || d > pass->radii[i]) {
                     skip = 1;
@@ -392,10 +407,10 @@ static unsigned long long o_pair(const OGroup *g, const OGroup *h, const OPass *
 }
 
 /* neighbour cell index box for a seer box (tay/cpu_z_grid.c:232-247, tay/cpu_grid.c:158-174) */
-static void o_index_box(const OGroup *g, const REAL *bmin, const REAL *bmax, int *lo, int *hi) {
-    o_cell_indices(bmin, g->origin, g->cell_size, lo);
-    o_cell_indices(bmax, g->origin, g->cell_size, hi);
-    for (int i = 0; i < 3; ++i) {
+static void o_index_box(const OGroup *g, const REAL *bmin, const REAL *bmax, int *lo, int *hi, int dims) {
+    o_cell_indices(bmin, g->origin, g->cell_size, lo, dims);
+    o_cell_indices(bmax, g->origin, g->cell_size, hi, dims);
+    for (int i = 0; i < dims; ++i) {
         if (lo[i] < 0) lo[i] = 0;
         if (hi[i] < 0) hi[i] = 0;
         if (lo[i] >= g->cell_counts[i]) lo[i] = g->cell_counts[i] - 1;
@@ -421,12 +436,13 @@ static void o_see_task(OTask *task, int thread_i, int threads) {
     OGroup *h = arg->h;
     OPass *pass = arg->pass;
     int skip_self = arg->skip_self;
+    int dims = g->dims < h->dims ? g->dims : h->dims; /* min_dims, tay/cpu_z_grid.c:289-291 */
     unsigned beg, end;
     o_range(g->count, thread_i, threads, &beg, &end);
 
     unsigned long long pairs = 0;
     if (g->space == O_SPACE_SIMPLE || h->space == O_SPACE_SIMPLE) {
-        O_NAME(pairs_by_thread)[thread_i] += o_pair(g, h, pass, beg, end, 0, h->count, skip_self);
+        O_NAME(pairs_by_thread)[thread_i] += o_pair(g, h, pass, beg, end, 0, h->count, skip_self, dims);
         return;
     }
 
@@ -451,14 +467,14 @@ static void o_see_task(OTask *task, int thread_i, int threads) {
         }
         if (run_end > end)
             run_end = end;
-        REAL bmin[3], bmax[3];
-        for (int i = 0; i < 3; ++i) {
+        REAL bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
+        for (int i = 0; i < dims; ++i) {
             REAL m = g->origin[i] + idx[i] * g->cell_size[i];
             bmin[i] = m - pass->radii[i];
             bmax[i] = m + g->cell_size[i] + pass->radii[i];
         }
         int lo[3], hi[3];
-        o_index_box(h, bmin, bmax, lo, hi);
+        o_index_box(h, bmin, bmax, lo, hi, dims);
         for (int x = lo[0]; x <= hi[0]; ++x)
             for (int y = lo[1]; y <= hi[1]; ++y)
                 for (int z = lo[2]; z <= hi[2]; ++z) {
@@ -473,7 +489,7 @@ static void o_see_task(OTask *task, int thread_i, int threads) {
                         first = c->first;
                         count = c->count;
                     }
-                    pairs += o_pair(g, h, pass, s, run_end, first, first + count, skip_self);
+                    pairs += o_pair(g, h, pass, s, run_end, first, first + count, skip_self, dims);
                 }
         s = run_end;
     }
@@ -519,8 +535,29 @@ unsigned O_NAME(oracle_agent_size)(int model) {
     return o_agent_size(model);
 }
 
+/* Space options of the groups of the following runs (tay_configure_space dims,
+ * tay_fix_space_box): dims 3 and no fixed box unless set. */
+static int o_opt_dims = 3;
+static int o_opt_box_fixed = 0;
+static REAL o_opt_min[3], o_opt_max[3];
+
+void O_NAME(oracle_set_space)(int dims, int box_fixed, const REAL *box_min, const REAL *box_max) {
+    o_opt_dims = dims;
+    o_opt_box_fixed = box_fixed;
+    for (int i = 0; i < 3; ++i) {
+        o_opt_min[i] = box_fixed ? box_min[i] : 0;
+        o_opt_max[i] = box_fixed ? box_max[i] : 0;
+    }
+}
+
 static void o_group_init(OGroup *g, unsigned agent_size, int space, int n, const void *agents, REAL part_size, int mb) {
     memset(g, 0, sizeof(*g));
+    g->dims = o_opt_dims;
+    g->box_fixed = o_opt_box_fixed;
+    for (int i = 0; i < 3; ++i) {
+        g->fixed_min[i] = o_opt_min[i];
+        g->fixed_max[i] = o_opt_max[i];
+    }
     g->agent_size = agent_size;
     g->count = (unsigned)n;
     g->space = space;
@@ -580,6 +617,9 @@ int O_NAME(oracle_run)(int model, int space, int n, void *agents, const void *se
     if (!agent_size || n <= 0 || steps < 0)
         return 0;
     if (space != O_SPACE_SIMPLE && space != O_SPACE_GRID && space != O_SPACE_Z_GRID)
+        return 0;
+    /* the reference's Z-grid pairs nothing below 3 dims (tay/cpu_z_grid.c:254-260) */
+    if (o_opt_dims < 1 || o_opt_dims > 3 || (space == O_SPACE_Z_GRID && o_opt_dims != 3))
         return 0;
     O_NAME(pool_start)(threads);
 
@@ -656,6 +696,8 @@ int O_NAME(oracle_run_groups)(int model, int space, int ngroups, const int *coun
     if (model != O_MODEL_TEST && model != O_MODEL_BOIDS)
         return 0;
     if (space != O_SPACE_SIMPLE && space != O_SPACE_GRID && space != O_SPACE_Z_GRID)
+        return 0;
+    if (o_opt_dims < 1 || o_opt_dims > 3 || (space == O_SPACE_Z_GRID && o_opt_dims != 3))
         return 0;
     for (int k = 0; k < ngroups; ++k)
         if (counts[k] <= 0)

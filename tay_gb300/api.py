@@ -250,7 +250,7 @@ class TgpuGroup(ctypes.Structure):
     _fields_ = [("agent_size", ctypes.c_uint), ("count", ctypes.c_uint), ("min_part_sizes", ctypes.c_float * 4),
                 ("shared_megabytes", ctypes.c_int), ("box_fixed", ctypes.c_int), ("box_min", ctypes.c_float * 4),
                 ("box_max", ctypes.c_float * 4), ("pass_count", ctypes.c_int),
-                ("passes", ctypes.POINTER(TgpuPass))]
+                ("passes", ctypes.POINTER(TgpuPass)), ("dims", ctypes.c_int)]
 
 
 class TgpuStatePass(ctypes.Structure):
@@ -285,8 +285,13 @@ class Batch:
             d.min_part_sizes[:] = [setup.part] * 4
             d.shared_megabytes = setup.mb
             d.box_fixed = 0
+            if setup.fixed_box is not None:
+                d.box_fixed = 1
+                d.box_min[:3] = list(setup.fixed_box[0])
+                d.box_max[:3] = list(setup.fixed_box[1])
             d.pass_count = len(setup.passes)
             d.passes = passes
+            d.dims = setup.dims
         self._descs = descs
         self.ptr = ctypes.c_void_p()
         self._check(self.L.tgpu_batch_create(descs, len(groups), ctypes.byref(self.ptr)), "tgpu_batch_create")

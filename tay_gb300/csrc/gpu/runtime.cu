@@ -148,6 +148,13 @@ int pass_index(const TgpuGroup &g, const char *name, int from) {
     return -1;
 }
 
+// See radii of a pass as the kernels use them: the reference's box test skips the axes
+// beyond the space's dims (tay/space.c:62-68), here those radii are +inf.
+float4 pass_radii(const TgpuPass &tp, int dims) {
+    const float inf = INFINITY;
+    return make_float4(tp.radii[0], dims > 1 ? tp.radii[1] : inf, dims > 2 ? tp.radii[2] : inf, tp.radii[3]);
+}
+
 int upload_contexts(TgpuBatch *b, int seg) {
     std::vector<char> buf(b->ctx_stride);
     const HostSeg &h = b->hs[seg];
@@ -165,7 +172,7 @@ int upload_contexts(TgpuBatch *b, int seg) {
         }
         if (r.see_pass >= 0) {
             const TgpuPass &tp = h.passes[r.see_pass];
-            float4 rr = make_float4(tp.radii[0], tp.radii[1], tp.radii[2], tp.radii[3]);
+            float4 rr = pass_radii(tp, seg_dims(b->specs[seg]));
             CK(cudaMemcpyAsync(r.d_radii + seg, &rr, sizeof(float4), cudaMemcpyHostToDevice, b->st));
         }
     }
@@ -188,7 +195,7 @@ int tgpu::prepare_specs(TgpuBatch *b) {
         SegmentSpec &sp = next[s];
         const HostSeg &h = b->hs[s];
         uint32_t axis = 2;
-        for (int a = 0; a < 3; ++a) {
+        for (int a = 0; a < seg_dims(sp); ++a) {
             float lo = h.g.box_fixed ? h.g.box_min[a] : h.host_min[a];
             float hi = h.g.box_fixed ? h.g.box_max[a] : h.host_max[a];
             float ext = hi > lo ? hi - lo : 0.0f;
@@ -557,6 +564,7 @@ int add_segments(TgpuBatch *b, const TgpuGroup *groups, int group_count, const s
         sp.count = g.count;
         sp.fixed_box = g.box_fixed ? 1u : 0u;
         sp.order = b->cell_order;
+        sp.dims = (g.dims >= 1 && g.dims <= 3) ? (uint32_t)g.dims : 3u;
         for (int a = 0; a < 3; ++a) {
             float part = g.min_part_sizes[a] > 0.0f ? g.min_part_sizes[a] : 1.0f;
             sp.part[a] = part * g_tuning.cell_multiple;
@@ -673,7 +681,9 @@ int upload_state_contexts(TgpuBatch *b) {
         CK(cudaMemcpyAsync(dst + (size_t)r.seer_seg * b->ctx_stride, buf.data(), b->ctx_stride, cudaMemcpyHostToDevice,
                            b->st));
         if (r.k->see) {
-            float4 rr = make_float4(tp.radii[0], tp.radii[1], tp.radii[2], tp.radii[3]);
+            // the box test over min(seer dims, seen dims) axes (tay/cpu_z_grid.c:289-291)
+            const int dims = std::min(seg_dims(b->specs[r.seer_seg]), seg_dims(b->specs[r.seen_seg]));
+            float4 rr = pass_radii(tp, dims);
             CK(cudaMemcpyAsync(r.d_radii + r.seer_seg, &rr, sizeof(float4), cudaMemcpyHostToDevice, b->st));
         }
     }

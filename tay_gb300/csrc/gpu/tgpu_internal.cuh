@@ -40,6 +40,7 @@ struct SegmentSpec {
     uint32_t axis_cells_max; // power of two, <= 1024: bounds each grid axis (key bits)
     uint32_t fixed_box;      // 1: use box_min/box_max instead of the agents' bounding box
     uint32_t order;          // cell order of the keys and table layout: kOrderMorton / kOrderRows
+    uint32_t dims;           // tay_configure_space dims (1..3; 0 means 3): axes >= dims get one cell
     float part[3];           // minimum cell edge per axis
     float reach[3];          // largest see radius per axis over the segment's see passes
     float box_min[3];        // fixed space box (tay_fix_space_box)
@@ -96,6 +97,8 @@ TGPU_HD int clamp_cells(float cells, uint32_t axis_max) {
     return (int)cells;
 }
 
+TGPU_HD int seg_dims(const SegmentSpec &s) { return (s.dims >= 1u && s.dims <= 3u) ? (int)s.dims : 3; }
+
 TGPU_HD Grid derive_grid(const SegmentSpec &s, const float *mn, const float *mx) {
     Grid g;
     float cs[3], ext[3];
@@ -107,11 +110,16 @@ TGPU_HD Grid derive_grid(const SegmentSpec &s, const float *mn, const float *mx)
         float cells = floorf(ext[i] / cs[i]) + 1.0f;
         if (cells > (float)s.axis_cells_max) cs[i] = ext[i] / ((float)s.axis_cells_max - 0.5f);
         d[i] = clamp_cells(floorf(ext[i] / cs[i]) + 1.0f, s.axis_cells_max);
+        if (i >= seg_dims(s)) {
+            // an axis the space does not have: one cell spanning it
+            d[i] = 1;
+            cs[i] = ext[i] > cs[i] ? ext[i] : cs[i];
+        }
     }
     for (int iter = 0; iter < 64; ++iter) {
         unsigned long long total = (unsigned long long)d[0] * (unsigned long long)d[1] * (unsigned long long)d[2];
         if (total <= s.table_cap) break;
-        for (int i = 0; i < 3; ++i) {
+        for (int i = 0; i < seg_dims(s); ++i) {
             cs[i] *= 1.25f;
             d[i] = clamp_cells(floorf(ext[i] / cs[i]) + 1.0f, s.axis_cells_max);
         }

@@ -334,8 +334,8 @@ static int validate(TayState *state) {
             set_error(state, TAY_ERROR_POINT_NONPOINT_MISMATCH, "grid structure can only contain point agents");
             return 0;
         }
-        if (g->dims != 3) {
-            set_error(state, TAY_ERROR_NOT_IMPLEMENTED, "the GPU Z-grid supports 3 dimensions");
+        if (g->dims < 1 || g->dims > 3) {
+            set_error(state, TAY_ERROR_NOT_IMPLEMENTED, "the GPU Z-grid supports 1 to 3 dimensions");
             return 0;
         }
         g->slot = state->ngpu;
@@ -396,6 +396,7 @@ static int validate(TayState *state) {
         }
         tg->shared_megabytes = g->shared_mb;
         tg->box_fixed = g->box_fixed;
+        tg->dims = g->dims;
     }
     if (state->ngpu == 1) {
         state->gpu_group = state->gpu_slots[0];

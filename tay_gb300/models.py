@@ -88,6 +88,7 @@ class Setup:
     mb: int = 250
     fixed_box: tuple | None = None
     extra: dict = field(default_factory=dict)
+    dims: int = 3
 
 
 def test_setup(radius=50.0, part=50.0, passes=("agent_see", "agent_act"), mb=250):
@@ -119,7 +120,7 @@ def make_state(setup: Setup, recs: np.ndarray):
     """Creates a state with one TAY_GPU_Z_GRID group holding `recs`, passes registered."""
     st = api.State()
     g = st.add_group(setup.dtype.itemsize, max(1, recs.shape[0]), True)
-    st.configure_space(g, api.TAY_GPU_Z_GRID, 3, api.f4(setup.part), setup.mb)
+    st.configure_space(g, api.TAY_GPU_Z_GRID, setup.dims, api.f4(setup.part), setup.mb)
     if setup.fixed_box is not None:
         st.fix_space_box(g, api.f4(*setup.fixed_box[0]), api.f4(*setup.fixed_box[1]))
     for p in setup.passes:

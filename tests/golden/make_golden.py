@@ -24,6 +24,15 @@ Two-group cases (golden_groups.npz; the pass list of test/test_combo.c:114-119):
   combo_full_*   the same passes + act a, act b, 5 steps, CpuGrid / CpuZGrid
   boids_pair     boids groups of 1500 and 1000, see a->b, b->a, act a, act b, 3 steps,
                  CpuZGrid
+
+Space-option cases (golden_space.npz):
+  dims2_*        test model, 2000 agents, tay_configure_space dims 2 (box test and grid
+                 over x, y only), see + act, 3 steps, CpuSimple / CpuGrid
+  dims1_grid     the same with dims 1, CpuGrid
+  fixed_*        tay_fix_space_box [-10, 1010]^3 around the agents, see + act, 3 steps,
+                 CpuGrid / CpuZGrid
+  (the reference's CpuZGrid pairs nothing below 3 dims, tay/cpu_z_grid.c:254-260, so
+  dims < 3 is pinned on CpuSimple / CpuGrid)
 """
 import os
 import sys
@@ -81,6 +90,19 @@ def group_cases():
     yield "boids_pair", O.MODEL_BOIDS, "z_grid", brecs, BOIDS_PAIR, bctx, bctx, 10.0, 3
 
 
+def space_cases():
+    ps = W.basic_points(2000, seed=121)
+    rec = O.make_records(O.MODEL_TEST, ps.p, ps.v)
+    see, act = np.array([50, 50, 50, 0], np.float32), O.test_act_context(np.float32)
+    full = O.PASS_SEE0 | O.PASS_ACT0
+    for space in ("simple", "grid"):
+        yield f"dims2_{space}", space, rec, see, act, 3, full, 2, None
+    yield "dims1_grid", "grid", rec, see, act, 3, full, 1, None
+    box = ((-10.0, -10.0, -10.0), (1010.0, 1010.0, 1010.0))
+    for space in ("grid", "z_grid"):
+        yield f"fixed_{space}", space, rec, see, act, 3, full, 3, box
+
+
 def pass_table(passes):
     return np.array([[1 if p[0] == "see" else 0, p[1], p[2] if p[0] == "see" else p[1], int(p[3]) if p[0] == "see" else 0]
                      for p in passes], np.int64)
@@ -116,6 +138,19 @@ def main():
         out[f"{name}__act"] = act
         print(f"{name}: {[r.shape[0] for r in recs]} agents, {steps} steps")
     np.savez_compressed(os.path.join(HERE, "golden_groups.npz"), **out)
+    out = {}
+    for name, space, rec, see, act, steps, mask, dims, box in space_cases():
+        r = ref.run(O.MODEL_TEST, space, rec, see, act, 50.0, 50.0, steps, mask, threads=4, dims=dims, box=box)
+        out[f"{name}__in"] = rec
+        out[f"{name}__out"] = r.records
+        out[f"{name}__meta"] = np.array([O.MODEL_TEST, O.SPACE[space], steps, mask, dims], np.int64)
+        out[f"{name}__box"] = np.zeros((2, 3)) if box is None else np.array(box, np.float64)
+        out[f"{name}__fixed"] = np.array([0 if box is None else 1], np.int64)
+        out[f"{name}__see"] = see
+        out[f"{name}__act"] = act
+        print(f"{name}: {rec.shape[0]} agents, dims {dims}, fixed box {box is not None}")
+    ref.set_space()
+    np.savez_compressed(os.path.join(HERE, "golden_space.npz"), **out)
 
 
 if __name__ == "__main__":

@@ -145,3 +145,23 @@ def test_port_groups_bit_exact_with_live_reference(port):
     y = O.reference().run_groups(O.MODEL_TEST, "z_grid", recs, passes, see, act, 50.0, 50.0, 4, threads=3)
     for r, s in zip(x, y):
         assert same_records(O.MODEL_TEST, r.records, s.records)
+
+
+GS = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_space.npz"))
+GS_NAMES = sorted({k.split("__")[0] for k in GS.files})
+
+
+def space_case(name):
+    model, space, steps, mask, dims = (int(x) for x in GS[f"{name}__meta"])
+    box = tuple(map(tuple, GS[f"{name}__box"])) if int(GS[f"{name}__fixed"][0]) else None
+    return model, SPACE_NAME[space], steps, mask, dims, box
+
+
+@pytest.mark.parametrize("name", GS_NAMES)
+def test_port_space_options_bit_exact_with_golden(port, name):
+    """tay_configure_space dims 1 / 2 and tay_fix_space_box."""
+    model, space, steps, mask, dims, box = space_case(name)
+    r = port.run(model, space, GS[f"{name}__in"], GS[f"{name}__see"], GS[f"{name}__act"], 50.0, 50.0, steps, mask,
+                 threads=3, dims=dims, box=box)
+    port.set_space()
+    assert same_records(model, r.records, GS[f"{name}__out"]), name
