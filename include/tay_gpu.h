@@ -87,6 +87,10 @@ int tgpu_state_create(const TgpuGroup *groups, int group_count, const TgpuStateP
 /* Copies the contexts and radii of a state's passes again (same order as at create). */
 int tgpu_state_set_contexts(TgpuBatch *batch, const TgpuStatePass *passes, int pass_count);
 
+/* 1 when the device model providing `func_name` holds non-point (box) agents, 0 when it
+ * holds point agents, -1 when no model provides it. */
+int tgpu_model_nonpoint(const char *func_name);
+
 /* Copies the pass contexts of group `group` again (contexts are borrowed by the host
  * API and re-read at every tay_run, as tay/ocl.c:252-259 does). */
 int tgpu_batch_set_contexts(TgpuBatch *batch, int group, const TgpuGroup *desc);

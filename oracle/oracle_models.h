@@ -95,6 +95,67 @@ static inline void o_test_act(void *va, void *vc) {
 }
 
 /* ---------------------------------------------------------------------------------
+ * Box test model (non-point agents): restates the reference's box agent
+ * (test/agent.h:21-29, test/agent.c:57-118).
+ *   see: b_buffer += b.min - a.min (x, y, z), b_buffer_count += 1
+ *   act: fold the mean into f_buffer, move min and max by v, then at each wall in the
+ *        order min x, y, z, max x, y, z: clamp that corner to the wall, put the other
+ *        corner at the size's distance, reverse that velocity component.
+ * The reference's float4 helpers leave the w components of min, max, b_buffer and
+ * f_buffer undefined once written.
+ * --------------------------------------------------------------------------------- */
+typedef struct {
+    OTag tag;
+    REAL min[4];
+    REAL max[4];
+    REAL v[4];
+    REAL b_buffer[4];
+    int b_buffer_count;
+    REAL f_buffer[4];
+    int result_index;
+} OBoxAgent;
+
+static inline void o_box_see(void *va, void *vb, void *vc) {
+    OBoxAgent *a = (OBoxAgent *)va;
+    OBoxAgent *b = (OBoxAgent *)vb;
+    (void)vc;
+    for (int i = 0; i < 3; ++i)
+        a->b_buffer[i] = a->b_buffer[i] + (b->min[i] - a->min[i]);
+    a->b_buffer_count++;
+}
+
+static inline void o_box_act(void *va, void *vc) {
+    OBoxAgent *a = (OBoxAgent *)va;
+    const OTestActContext *c = (const OTestActContext *)vc;
+    if (a->b_buffer_count != 0) {
+        REAL n = (REAL)a->b_buffer_count;
+        for (int i = 0; i < 3; ++i) {
+            a->f_buffer[i] = a->f_buffer[i] + a->b_buffer[i] / n;
+            a->b_buffer[i] = 0;
+        }
+        a->b_buffer_count = 0;
+    }
+    REAL size[3];
+    for (int i = 0; i < 3; ++i) {
+        size[i] = a->max[i] - a->min[i];
+        a->min[i] = a->min[i] + a->v[i];
+        a->max[i] = a->max[i] + a->v[i];
+    }
+    for (int i = 0; i < 3; ++i)
+        if (a->min[i] < c->min[i]) {
+            a->min[i] = c->min[i];
+            a->max[i] = c->min[i] + size[i];
+            a->v[i] = -a->v[i];
+        }
+    for (int i = 0; i < 3; ++i)
+        if (a->max[i] > c->max[i]) {
+            a->max[i] = c->max[i];
+            a->min[i] = c->max[i] - size[i];
+            a->v[i] = -a->v[i];
+        }
+}
+
+/* ---------------------------------------------------------------------------------
  * Boids (Reynolds' rules in the steering form of Shiffman's "Nature of Code" flocking,
  * with its weights 1.5 / 1.0 / 1.0 and max speed 2): neighbours within radius r,
  * separation from neighbours within sep_r.

@@ -24,8 +24,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libtayref.so")
 
-MODEL_TEST, MODEL_BOIDS, MODEL_SPH = 0, 1, 2
-SPACE = {"simple": 1, "kd_tree": 2, "grid": 4, "z_grid": 5}
+MODEL_TEST, MODEL_BOIDS, MODEL_SPH, MODEL_BOX = 0, 1, 2, 3
+SPACE = {"simple": 1, "kd_tree": 2, "aabb_tree": 3, "grid": 4, "z_grid": 5}
 PASS_SEE0, PASS_ACT0, PASS_SEE1, PASS_ACT1 = 1, 2, 4, 8
 
 
@@ -37,13 +37,16 @@ def _rec(real):
                      ("count", "<i4"), ("sep_count", "<i4"), ("id", "<i4"), ("pad", "<i4")])
     sph = np.dtype([("tag", "<u4", 2), ("p", f, 4), ("v", f, 4), ("a", f, 4), ("rho", f), ("P", f), ("id", "<i4"),
                     ("pad", "<i4")])
-    return {MODEL_TEST: test, MODEL_BOIDS: boid, MODEL_SPH: sph}
+    box = np.dtype([("tag", "<u4", 2), ("min", f, 4), ("max", f, 4), ("v", f, 4), ("b_buffer", f, 4),
+                    ("b_buffer_count", "<i4"), ("f_buffer", f, 4), ("id", "<i4")])
+    return {MODEL_TEST: test, MODEL_BOIDS: boid, MODEL_SPH: sph, MODEL_BOX: box}
 
 
 RECORDS = {np.float32: _rec(np.float32), np.float64: _rec(np.float64)}
 assert RECORDS[np.float32][MODEL_TEST].itemsize == 80
 assert RECORDS[np.float32][MODEL_BOIDS].itemsize == 104
 assert RECORDS[np.float32][MODEL_SPH].itemsize == 72
+assert RECORDS[np.float32][MODEL_BOX].itemsize == 96
 
 
 def boids_context(real, r=10.0, sep_r=5.0, w_sep=1.5, w_ali=1.0, w_coh=1.0, max_speed=2.0, max_force=0.03, dt=1.0):
@@ -70,6 +73,17 @@ def make_records(model, p, v, real=np.float32):
     n = p.shape[0]
     rec = np.zeros(n, RECORDS[real][model])
     rec["p"] = p
+    rec["v"] = v
+    rec["id"] = np.arange(n, dtype=np.int32)
+    return rec
+
+
+def make_box_records(lo, hi, v, real=np.float32):
+    """Box-agent records from min / max corners and velocities ([N,4] arrays)."""
+    n = lo.shape[0]
+    rec = np.zeros(n, RECORDS[real][MODEL_BOX])
+    rec["min"] = lo
+    rec["max"] = hi
     rec["v"] = v
     rec["id"] = np.arange(n, dtype=np.int32)
     return rec

@@ -11,6 +11,8 @@
  *   REF_MODEL_TEST  - the reference's own test agent (test/agent.c agent_see/agent_act)
  *   REF_MODEL_BOIDS - oracle boids (oracle/oracle_models.h), run by the reference framework
  *   REF_MODEL_SPH   - oracle SPH, run by the reference framework
+ *   REF_MODEL_BOX   - the reference's own box agent (test/agent.c box_agent_see/act), a
+ *                     non-point group
  */
 #include "tay.h"
 #include "thread.h"
@@ -22,7 +24,7 @@
 #define REAL float
 #include "../oracle_models.h"
 
-enum { REF_MODEL_TEST = 0, REF_MODEL_BOIDS = 1, REF_MODEL_SPH = 2 };
+enum { REF_MODEL_TEST = 0, REF_MODEL_BOIDS = 1, REF_MODEL_SPH = 2, REF_MODEL_BOX = 3 };
 
 /* pass mask bits, in registration order */
 enum { REF_PASS_SEE0 = 1, REF_PASS_ACT0 = 2, REF_PASS_SEE1 = 4, REF_PASS_ACT1 = 8 };
@@ -67,6 +69,7 @@ unsigned ref_agent_size(int model) {
         case REF_MODEL_TEST: return (unsigned)sizeof(Agent);
         case REF_MODEL_BOIDS: return (unsigned)sizeof(OBoid);
         case REF_MODEL_SPH: return (unsigned)sizeof(OSphParticle);
+        case REF_MODEL_BOX: return (unsigned)sizeof(BoxAgent);
         default: return 0;
     }
 }
@@ -76,6 +79,7 @@ static int agent_id(int model, const char *agent) {
         case REF_MODEL_TEST: return ((const Agent *)agent)->result_index;
         case REF_MODEL_BOIDS: return ((const OBoid *)agent)->id;
         case REF_MODEL_SPH: return ((const OSphParticle *)agent)->id;
+        case REF_MODEL_BOX: return ((const BoxAgent *)agent)->result_index;
         default: return -1;
     }
 }
@@ -98,11 +102,22 @@ int ref_run(int model, int space_type, int n, void *agents, const void *see_ctx,
     static OSphContext sph_ctx;
 
     TayState *tay = tay_create_state();
-    TayGroup *group = tay_add_group(tay, agent_size, (unsigned)n, TAY_TRUE);
+    TayGroup *group = tay_add_group(tay, agent_size, (unsigned)n, model == REF_MODEL_BOX ? TAY_FALSE : TAY_TRUE);
     configure(tay, group, space_type, part_size, mb);
 
     float4 radii = {{{radius, radius, radius, radius}}};
-    if (model == REF_MODEL_TEST) {
+    if (model == REF_MODEL_BOX) {
+        memcpy(&test_see_ctx, see_ctx, sizeof(test_see_ctx));
+        memcpy(&test_act_ctx, act_ctx, sizeof(test_act_ctx));
+        radii.w = 0.0f;
+        if (pass_mask & REF_PASS_SEE0)
+            tay_add_see(tay, group, group, (void (*)(void *, void *, void *))box_agent_see, "box_agent_see", radii,
+                        TAY_FALSE, &test_see_ctx, sizeof(test_see_ctx));
+        if (pass_mask & REF_PASS_ACT0)
+            tay_add_act(tay, group, (void (*)(void *, void *))box_agent_act, "box_agent_act", &test_act_ctx,
+                        sizeof(test_act_ctx));
+    }
+    else if (model == REF_MODEL_TEST) {
         memcpy(&test_see_ctx, see_ctx, sizeof(test_see_ctx));
         memcpy(&test_act_ctx, act_ctx, sizeof(test_act_ctx));
         radii.w = 0.0f;

@@ -46,7 +46,7 @@
 #endif
 
 enum { O_SPACE_SIMPLE = 1, O_SPACE_GRID = 4, O_SPACE_Z_GRID = 5 };
-enum { O_MODEL_TEST = 0, O_MODEL_BOIDS = 1, O_MODEL_SPH = 2 };
+enum { O_MODEL_TEST = 0, O_MODEL_BOIDS = 1, O_MODEL_SPH = 2, O_MODEL_BOX = 3 };
 enum { O_PASS_SEE0 = 1, O_PASS_ACT0 = 2, O_PASS_SEE1 = 4, O_PASS_ACT1 = 8 };
 
 typedef void (*OSeeFn)(void *, void *, void *);
@@ -170,6 +170,7 @@ typedef struct {
     unsigned count;
     int space;
     int dims;                         /* tay_configure_space dims: 1..3 */
+    int is_point;                     /* 0: box agents, min at the position's offset, max after it */
     int box_fixed;                    /* tay_fix_space_box */
     REAL fixed_min[3], fixed_max[3];
     REAL part[3];
@@ -196,6 +197,11 @@ typedef struct {
 
 static inline REAL *o_pos(const OGroup *g, unsigned i) {
     return (REAL *)(g->storage + (size_t)g->agent_size * i + sizeof(OTag));
+}
+
+/* a box agent's max corner follows its min (the position), tay/state.h float4_agent_max */
+static inline REAL *o_max(const OGroup *g, unsigned i) {
+    return o_pos(g, i) + 4;
 }
 
 static inline OTag *o_tag(const OGroup *g, unsigned i) {
@@ -390,11 +396,23 @@ static unsigned long long o_pair(const OGroup *g, const OGroup *h, const OPass *
                 continue;
             const REAL *bp = o_pos(h, b);
             int skip = 0;
-            for (int i = 0; i < dims; ++i) {
-                REAL d = sp[i] - bp[i];
-                if (d < -pass->radii[i] || d > pass->radii[i]) {
-                    skip = 1;
-                    break;
+            if (g->is_point) {
+                for (int i = 0; i < dims; ++i) {
+                    REAL d = sp[i] - bp[i];
+                    if (d < -pass->radii[i] || d > pass->radii[i]) {
+                        skip = 1;
+                        break;
+                    }
+                }
+            }
+            else {
+                /* _NONPOINT_NONPOINT_NARROW_PHASE_TEST, tay/space.c:92-103 */
+                const REAL *smax = o_max(g, s), *bmax = o_max(h, b);
+                for (int i = 0; i < dims; ++i) {
+                    if (sp[i] - bmax[i] > pass->radii[i] || bp[i] - smax[i] > pass->radii[i]) {
+                        skip = 1;
+                        break;
+                    }
                 }
             }
             if (skip)
@@ -511,6 +529,7 @@ static unsigned o_agent_size(int model) {
         case O_MODEL_TEST: return (unsigned)sizeof(OTestAgent);
         case O_MODEL_BOIDS: return (unsigned)sizeof(OBoid);
         case O_MODEL_SPH: return (unsigned)sizeof(OSphParticle);
+        case O_MODEL_BOX: return (unsigned)sizeof(OBoxAgent);
         default: return 0;
     }
 }
@@ -519,6 +538,7 @@ static int o_agent_id(int model, const char *a) {
     switch (model) {
         case O_MODEL_TEST: return ((const OTestAgent *)a)->result_index;
         case O_MODEL_BOIDS: return ((const OBoid *)a)->id;
+        case O_MODEL_BOX: return ((const OBoxAgent *)a)->result_index;
         default: return ((const OSphParticle *)a)->id;
     }
 }
@@ -553,6 +573,7 @@ void O_NAME(oracle_set_space)(int dims, int box_fixed, const REAL *box_min, cons
 static void o_group_init(OGroup *g, unsigned agent_size, int space, int n, const void *agents, REAL part_size, int mb) {
     memset(g, 0, sizeof(*g));
     g->dims = o_opt_dims;
+    g->is_point = 1;
     g->box_fixed = o_opt_box_fixed;
     for (int i = 0; i < 3; ++i) {
         g->fixed_min[i] = o_opt_min[i];
@@ -621,10 +642,15 @@ int O_NAME(oracle_run)(int model, int space, int n, void *agents, const void *se
     /* the reference's Z-grid pairs nothing below 3 dims (tay/cpu_z_grid.c:254-260) */
     if (o_opt_dims < 1 || o_opt_dims > 3 || (space == O_SPACE_Z_GRID && o_opt_dims != 3))
         return 0;
+    /* grids hold point agents only (tay/state_compile.c: "grid structure can only contain
+     * point agents"); box agents run on CpuSimple */
+    if (model == O_MODEL_BOX && space != O_SPACE_SIMPLE)
+        return 0;
     O_NAME(pool_start)(threads);
 
     OGroup g;
     o_group_init(&g, agent_size, space, n, agents, part_size, mb);
+    g.is_point = model != O_MODEL_BOX;
 
     /* contexts are copied, as the OpenCL path copies them per run (tay/ocl.c:252-259) */
     OTestActContext test_act;
@@ -633,12 +659,14 @@ int O_NAME(oracle_run)(int model, int space, int n, void *agents, const void *se
     OPass passes[4];
     int passes_count = 0;
     REAL radii[3] = {radius, radius, radius};
-    if (model == O_MODEL_TEST) {
+    if (model == O_MODEL_TEST || model == O_MODEL_BOX) {
         memcpy(&test_act, act_ctx, sizeof(test_act));
+        OSeeFn see = model == O_MODEL_TEST ? o_test_see : o_box_see;
+        OActFn act = model == O_MODEL_TEST ? o_test_act : o_box_act;
         if (pass_mask & O_PASS_SEE0)
-            passes[passes_count++] = (OPass){1, o_test_see, 0, {radii[0], radii[1], radii[2]}, 0, 0};
+            passes[passes_count++] = (OPass){1, see, 0, {radii[0], radii[1], radii[2]}, 0, 0};
         if (pass_mask & O_PASS_ACT0)
-            passes[passes_count++] = (OPass){0, 0, o_test_act, {0, 0, 0}, 0, &test_act};
+            passes[passes_count++] = (OPass){0, 0, act, {0, 0, 0}, 0, &test_act};
     }
     else if (model == O_MODEL_BOIDS) {
         memcpy(&boids, see_ctx, sizeof(boids));
@@ -693,7 +721,9 @@ int O_NAME(oracle_run_groups)(int model, int space, int ngroups, const int *coun
     unsigned agent_size = o_agent_size(model);
     if (!agent_size || ngroups <= 0 || ngroups > kMaxGroups || npasses < 0 || npasses > kMaxPasses || steps < 0)
         return 0;
-    if (model != O_MODEL_TEST && model != O_MODEL_BOIDS)
+    if (model != O_MODEL_TEST && model != O_MODEL_BOIDS && model != O_MODEL_BOX)
+        return 0;
+    if (model == O_MODEL_BOX && space != O_SPACE_SIMPLE)
         return 0;
     if (space != O_SPACE_SIMPLE && space != O_SPACE_GRID && space != O_SPACE_Z_GRID)
         return 0;
@@ -708,20 +738,22 @@ int O_NAME(oracle_run_groups)(int model, int space, int ngroups, const int *coun
     O_NAME(pool_start)(threads);
 
     OGroup g[kMaxGroups];
-    for (int k = 0; k < ngroups; ++k)
+    for (int k = 0; k < ngroups; ++k) {
         o_group_init(g + k, agent_size, space, counts[k], agents[k], part_size, mb);
+        g[k].is_point = model != O_MODEL_BOX;
+    }
     OTestActContext test_act;
     OBoidsContext boids;
-    if (model == O_MODEL_TEST)
+    if (model == O_MODEL_TEST || model == O_MODEL_BOX)
         memcpy(&test_act, act_ctx, sizeof(test_act));
     else
         memcpy(&boids, see_ctx, sizeof(boids));
     OPass passes[kMaxPasses];
     for (int k = 0; k < npasses; ++k) {
         OPass p = {pass_is_see[k], 0, 0, {radius, radius, radius}, pass_self_see[k], 0};
-        if (model == O_MODEL_TEST) {
-            p.see = o_test_see;
-            p.act = o_test_act;
+        if (model == O_MODEL_TEST || model == O_MODEL_BOX) {
+            p.see = model == O_MODEL_TEST ? o_test_see : o_box_see;
+            p.act = model == O_MODEL_TEST ? o_test_act : o_box_act;
             p.ctx = pass_is_see[k] ? 0 : &test_act;
         }
         else {

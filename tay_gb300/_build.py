@@ -26,6 +26,7 @@ CU_SOURCES = [
     "gpu/sort.cu",
     "gpu/runtime.cu",
     "gpu/model_test_basic.cu",
+    "gpu/model_box.cu",
     "gpu/model_boids.cu",
     "gpu/model_sph.cu",
     "gpu/noalloc.cu",

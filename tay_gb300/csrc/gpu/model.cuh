@@ -58,6 +58,7 @@ struct ModelDesc {
     int nprograms;
     void (*pack)(const uint32_t *aos, uint32_t n, const PassIO &io, cudaStream_t st);
     void (*unpack)(uint32_t *aos, uint32_t n, const PassIO &io, uint32_t program, cudaStream_t st);
+    int nonpoint;  // 1: box agents, float4 stream 0 the min corner (the position), 1 the max
 };
 
 // The SPH model's adjoint kernels (used by adjoint.cu).
@@ -77,6 +78,7 @@ const SphAdjointKernels *sph_adjoint_kernels();
 const ModelDesc *model_test_basic();
 const ModelDesc *model_boids();
 const ModelDesc *model_sph();
+const ModelDesc *model_box();
 
 // helpers used by the model translation units
 template <class P>

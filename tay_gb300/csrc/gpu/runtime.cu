@@ -63,6 +63,7 @@ const ModelDesc *model_list(int i) {
         case 0: return model_test_basic();
         case 1: return model_boids();
         case 2: return model_sph();
+        case 3: return model_box();
         default: return nullptr;
     }
 }
@@ -268,6 +269,7 @@ SortLaunch tgpu::sort_launch(TgpuBatch *b) {
     L.tile_seg = b->d_tile_seg;
     L.box = b->d_box;
     L.pos = b->f4[0][b->cur_f4[0]];
+    L.pos_max = b->m->nonpoint ? b->f4[1][b->cur_f4[1]] : nullptr;
     L.keys[0] = b->keys[0];
     L.keys[1] = b->keys[1];
     L.vals[0] = b->vals[0];
@@ -527,6 +529,11 @@ void tgpu_get_tuning(TgpuTuning *t) {
 const char *tgpu_model_of(const char *func_name) {
     const ModelDesc *m = func_name ? find_model(func_name) : nullptr;
     return m ? m->name : nullptr;
+}
+
+int tgpu_model_nonpoint(const char *func_name) {
+    const ModelDesc *m = func_name ? find_model(func_name) : nullptr;
+    return m ? (m->nonpoint ? 1 : 0) : -1;
 }
 
 const char *tgpu_batch_model(const TgpuBatch *b) { return b && b->m ? b->m->name : nullptr; }

@@ -51,6 +51,33 @@ TGPU_D void axis_range(float p, float r, float origin, float inv_cs, int dim, fl
     hi = h < 0 ? 0 : (h >= dim ? dim - 1 : h);
 }
 
+// Cell range along one axis for the interval [lo_v, hi_v] (a seer's search interval over
+// the seen agents' positions), widened by `pad` cells as in axis_range.
+TGPU_D void axis_span(float lo_v, float hi_v, float origin, float inv_cs, int dim, float pad, int &lo, int &hi) {
+    float a = (lo_v - origin) * inv_cs - pad;
+    float b = (hi_v - origin) * inv_cs + pad;
+    int l = (int)floorf(a), h = (int)floorf(b);
+    lo = l < 0 ? 0 : (l >= dim ? dim - 1 : l);
+    hi = h < 0 ? 0 : (h >= dim ? dim - 1 : h);
+}
+
+// Non-point seer over non-point seen agents (tay/space.c:92-103): skipped when on any
+// axis seer_min - seen_max > r or seen_min - seer_max > r.
+TGPU_D bool boxes_hit(const float4 &amin, const float4 &amax, const float4 &bmin, const float4 &bmax, const float4 &r) {
+    return !(amin.x - bmax.x > r.x) && !(bmin.x - amax.x > r.x) && !(amin.y - bmax.y > r.y) &&
+           !(bmin.y - amax.y > r.y) && !(amin.z - bmax.z > r.z) && !(bmin.z - amax.z > r.z);
+}
+
+// Whether pass P runs over non-point (box) agents: P::kBox when it declares one.
+template <class P, class = void>
+struct BoxOf {
+    static constexpr bool value = false;
+};
+template <class P>
+struct BoxOf<P, decltype((void)P::kBox)> {
+    static constexpr bool value = P::kBox;
+};
+
 // Inclusive per-axis box test of the reference: a pair is skipped when any
 // d = seer - seen satisfies d < -r || d > r, i.e. |d| > r (NaN compares false both ways).
 TGPU_D bool box_hit(const float4 &a, const float4 &b, const float4 &r) {
@@ -150,6 +177,40 @@ TGPU_D void lane_run(typename P::Seer &s, const float4 &sp, const float4 &r4, ui
     }
 }
 
+// Per-lane walk of box agents over candidates [j0, j1): min corners from `pos`, max
+// corners from `pos_max`.
+template <class P, class Acc>
+TGPU_D void lane_run_boxes(typename P::Seer &s, const float4 &amin, const float4 &amax, const float4 &r4, uint32_t j0,
+                           uint32_t j1, uint32_t self, const float4 *pos, const float4 *pos_max, const Acc &acc,
+                           const typename P::SeeCtx &sctx, uint32_t &pairs, uint32_t &tested) {
+    tested += j1 - j0;
+    for (uint32_t j = j0; j < j1; ++j) {
+        const float4 bmin = __ldg(pos + j);
+        const float4 bmax = __ldg(pos_max + j);
+        if (j != self && boxes_hit(amin, amax, bmin, bmax, r4)) {
+            ++pairs;
+            P::see(s, amin, bmin, acc, j, sctx);
+        }
+    }
+}
+
+// The seer's cell box in the seen grid: its search interval p +- r per axis, for box
+// agents [min - r - S, max + r] with S the seen agents' largest edge on that axis.
+template <bool kBox>
+TGPU_D void seer_cells(const float4 &sp, const float4 &smax, const float4 &r4, const BoxAcc &B, const Grid &g, float pad,
+                       int *lo, int *hi) {
+    if (!kBox) {
+        axis_range(sp.x, r4.x, g.origin[0], g.inv_cs[0], g.dims[0], pad, lo[0], hi[0]);
+        axis_range(sp.y, r4.y, g.origin[1], g.inv_cs[1], g.dims[1], pad, lo[1], hi[1]);
+        axis_range(sp.z, r4.z, g.origin[2], g.inv_cs[2], g.dims[2], pad, lo[2], hi[2]);
+        return;
+    }
+    const float sx = ordered_to_float(B.size[0]), sy = ordered_to_float(B.size[1]), sz = ordered_to_float(B.size[2]);
+    axis_span((sp.x - r4.x) - sx, smax.x + r4.x, g.origin[0], g.inv_cs[0], g.dims[0], pad, lo[0], hi[0]);
+    axis_span((sp.y - r4.y) - sy, smax.y + r4.y, g.origin[1], g.inv_cs[1], g.dims[1], pad, lo[1], hi[1]);
+    axis_span((sp.z - r4.z) - sz, smax.z + r4.z, g.origin[2], g.inv_cs[2], g.dims[2], pad, lo[2], hi[2]);
+}
+
 }  // namespace see_detail
 
 template <class P>
@@ -179,15 +240,15 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
     const bool active = i < seg_end;
     const uint32_t lane = threadIdx.x & 31u;
 
-    float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
+    constexpr bool kBox = BoxOf<P>::value;
+    float4 sp = make_float4(0.f, 0.f, 0.f, 0.f), smax = sp;
     typename P::Seer s;
     int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
     if (active) {
         sp = L.io.in_f4[0][i];
+        if (kBox) smax = L.io.in_f4[1][i];
         P::load(s, L.io, i, sctx, actx);
-        axis_range(sp.x, r4.x, g.origin[0], g.inv_cs[0], g.dims[0], pad, lo[0], hi[0]);
-        axis_range(sp.y, r4.y, g.origin[1], g.inv_cs[1], g.dims[1], pad, lo[1], hi[1]);
-        axis_range(sp.z, r4.z, g.origin[2], g.inv_cs[2], g.dims[2], pad, lo[2], hi[2]);
+        seer_cells<kBox>(sp, smax, r4, B, g, pad, lo, hi);
     }
 
     // CTA halo box = union of the seers' cell boxes
@@ -209,7 +270,7 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
     const int H0x = hbox[0], H0y = hbox[1], H0z = hbox[2];
     const int hx = hbox[3] - H0x + 1, hy = hbox[4] - H0y + 1, hz = hbox[5] - H0z + 1;
     const long long V = (hx > 0 && hy > 0 && hz > 0) ? (long long)hx * hy * hz : 0;
-    bool staged = L.stage_cap > 0 && V > 0 && V <= (long long)L.stage_cells;
+    bool staged = !kBox && L.stage_cap > 0 && V > 0 && V <= (long long)L.stage_cells;
     const uint2 *table = L.table + T.table_base;
     const uint32_t dx0 = (uint32_t)g.dims[0], dy0 = (uint32_t)g.dims[1];
 
@@ -285,7 +346,7 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
         // regions, each lane walks its own box instead.
         const int lane_vol = active ? max(0, hi[0] - lo[0] + 1) * max(0, hi[1] - lo[1] + 1) * max(0, hi[2] - lo[2] + 1) : 0;
         const long long union_vol = (long long)(wh0 - wl0 + 1) * (wh1 - wl1 + 1) * (wh2 - wl2 + 1);
-        const bool union_mode = union_vol <= (long long)L.union_factor * warp_max_i(lane_vol);
+        const bool union_mode = !kBox && union_vol <= (long long)L.union_factor * warp_max_i(lane_vol);
         if (L.telemetry && lane == 0) atomicAdd(L.telemetry + (union_mode ? 3 : 4), 1ull);
         if (staged) {
             uint32_t self_slot = 0xFFFFFFFFu;
@@ -339,7 +400,11 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
                     for (int y = lo[1]; y <= hi[1]; ++y)
                         for (int x = lo[0]; x <= hi[0]; ++x) {
                             const uint2 e = table[((uint32_t)z * dy0 + (uint32_t)y) * dx0 + (uint32_t)x];
-                            lane_run<P>(s, sp, r4, e.x, e.y, self, pos, acc, sctx, pairs, tested);
+                            if (kBox)
+                                lane_run_boxes<P>(s, sp, smax, r4, e.x, e.y, self, pos, L.io.in_f4[1], acc, sctx,
+                                                  pairs, tested);
+                            else
+                                lane_run<P>(s, sp, r4, e.x, e.y, self, pos, acc, sctx, pairs, tested);
                         }
             }
         }
@@ -380,15 +445,15 @@ __global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
     const bool active = i < seg_end;
     const uint32_t lane = threadIdx.x & 31u;
 
-    float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
+    constexpr bool kBox = BoxOf<P>::value;
+    float4 sp = make_float4(0.f, 0.f, 0.f, 0.f), smax = sp;
     typename P::Seer s;
     int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
     if (active) {
         sp = L.io.in_f4[0][i];
+        if (kBox) smax = L.io.in_f4[1][i];
         P::load(s, L.io, i, sctx, actx);
-        axis_range(sp.x, r4.x, g.origin[0], g.inv_cs[0], g.dims[0], pad, lo[0], hi[0]);
-        axis_range(sp.y, r4.y, g.origin[1], g.inv_cs[1], g.dims[1], pad, lo[1], hi[1]);
-        axis_range(sp.z, r4.z, g.origin[2], g.inv_cs[2], g.dims[2], pad, lo[2], hi[2]);
+        seer_cells<kBox>(sp, smax, r4, B, g, pad, lo, hi);
     }
     const uint32_t *rows = reinterpret_cast<const uint32_t *>(L.table + T.table_base);
     const uint32_t rw = (uint32_t)g.dims[0] + 1u, dy0 = (uint32_t)g.dims[1];
@@ -406,7 +471,7 @@ __global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
     if (wl0 <= wh0) {
         const int lane_vol = active ? (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) * (hi[0] - lo[0] + 1) : 0;
         const long long union_vol = (long long)(wh0 - wl0 + 1) * (wh1 - wl1 + 1) * (wh2 - wl2 + 1);
-        const bool union_mode = union_vol <= (long long)L.union_factor * warp_max_i(lane_vol);
+        const bool union_mode = !kBox && union_vol <= (long long)L.union_factor * warp_max_i(lane_vol);
         if (L.telemetry && lane == 0) atomicAdd(L.telemetry + (union_mode ? 3 : 4), 1ull);
         if (union_mode) {
             for (int z = wl2; z <= wh2; ++z)
@@ -419,7 +484,12 @@ __global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
             for (int z = lo[2]; z <= hi[2]; ++z)
                 for (int y = lo[1]; y <= hi[1]; ++y) {
                     const uint32_t *r = rows + ((uint32_t)z * dy0 + (uint32_t)y) * rw;
-                    lane_run<P>(s, sp, r4, __ldg(r + lo[0]), __ldg(r + hi[0] + 1), self, pos, acc, sctx, pairs, tested);
+                    if (kBox)
+                        lane_run_boxes<P>(s, sp, smax, r4, __ldg(r + lo[0]), __ldg(r + hi[0] + 1), self, pos,
+                                          L.io.in_f4[1], acc, sctx, pairs, tested);
+                    else
+                        lane_run<P>(s, sp, r4, __ldg(r + lo[0]), __ldg(r + hi[0] + 1), self, pos, acc, sctx, pairs,
+                                    tested);
                 }
         }
     }

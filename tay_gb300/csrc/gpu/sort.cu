@@ -45,17 +45,22 @@ TGPU_D uint32_t warp_incl_scan(uint32_t v) {
 
 // ------------------------------------------------------------------ bounding box
 
+// Bounding box of the positions (the min corners of non-point agents) per segment, and
+// for non-point agents (pos_max != nullptr) the largest box edge per axis, which widens
+// every seer's search over the seen agents' min corners.
 __global__ void __launch_bounds__(kSortThreads) bbox_kernel(const SegmentSpec *__restrict__ specs,
                                                             const uint32_t *__restrict__ tile_seg,
-                                                            const float4 *__restrict__ pos, BoxAcc *box) {
+                                                            const float4 *__restrict__ pos,
+                                                            const float4 *__restrict__ pos_max, BoxAcc *box) {
     const uint32_t seg = tile_seg[blockIdx.x];
     const SegmentSpec s = specs[seg];
-    if (s.fixed_box) return;
+    if (s.fixed_box && !pos_max) return;
     const uint32_t t = blockIdx.x - s.tile_begin;
     const uint32_t beg = s.begin + t * kSortTile;
     const uint32_t end = min(beg + (uint32_t)kSortTile, s.begin + s.count);
     uint32_t lo[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
     uint32_t hi[3] = {0u, 0u, 0u};
+    uint32_t sz[3] = {0u, 0u, 0u};
     for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads) {
         float4 p = pos[i];
         float c[3] = {p.x, p.y, p.z};
@@ -64,6 +69,18 @@ __global__ void __launch_bounds__(kSortThreads) bbox_kernel(const SegmentSpec *_
             lo[a] = min(lo[a], o);
             hi[a] = max(hi[a], o);
         }
+        if (pos_max) {
+            const float4 q = pos_max[i];
+            const float d[3] = {q.x - p.x, q.y - p.y, q.z - p.z};
+            for (int a = 0; a < 3; ++a) sz[a] = max(sz[a], float_to_ordered(fmaxf(d[a], 0.0f)));
+        }
+    }
+    if (pos_max) {
+        for (int a = 0; a < 3; ++a) {
+            const uint32_t v = warp_max(sz[a]);
+            if (lane_id() == 0 && v) atomicMax(&box[seg].size[a], v);
+        }
+        if (s.fixed_box) return;
     }
     __shared__ uint32_t red[6][kSortThreads / 32];
     for (int a = 0; a < 3; ++a) {
@@ -117,6 +134,7 @@ __global__ void box_reset_kernel(BoxAcc *box, uint32_t segments) {
     for (int a = 0; a < 3; ++a) {
         box[s].lo[a] = 0xFFFFFFFFu;
         box[s].hi[a] = 0u;
+        box[s].size[a] = float_to_ordered(0.0f);
     }
 }
 
@@ -433,7 +451,7 @@ void launch_extent(const float4 *pos, uint32_t n, BoxAcc *out, cudaStream_t st) 
 
 void launch_box(const SortLaunch &L, cudaStream_t st) {
     box_reset_kernel<<<(L.segments + 127) / 128, 128, 0, st>>>(L.box, L.segments);
-    bbox_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.pos, L.box);
+    bbox_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.pos, L.pos_max, L.box);
 }
 
 static void launch_scan(const SortLaunch &L, cudaStream_t st) {

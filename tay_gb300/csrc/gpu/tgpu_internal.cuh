@@ -61,6 +61,7 @@ struct Grid {
 struct BoxAcc {
     uint32_t lo[3];
     uint32_t hi[3];
+    uint32_t size[3];  // non-point agents: largest max - min per axis (ordered encoding)
 };
 
 TGPU_HD uint32_t float_to_ordered(float f) {

@@ -11,6 +11,7 @@ struct SortLaunch {
     const uint32_t *tile_seg;  // [tiles] segment of each radix tile
     BoxAcc *box;               // [segments]
     const float4 *pos;         // positions, current order
+    const float4 *pos_max;     // non-point agents: max corners, current order (else null)
     uint32_t *keys[2];         // [n] ping-pong key buffers
     uint32_t *vals[2];         // [n] ping-pong permutation buffers
     uint32_t *counts;          // [256 * tiles]

@@ -330,10 +330,7 @@ static int validate(TayState *state) {
                       "group %d uses a CPU structure; this library runs TAY_GPU_Z_GRID groups only", i);
             return 0;
         }
-        if (!g->is_point) {
-            set_error(state, TAY_ERROR_POINT_NONPOINT_MISMATCH, "grid structure can only contain point agents");
-            return 0;
-        }
+
         if (g->dims < 1 || g->dims > 3) {
             set_error(state, TAY_ERROR_NOT_IMPLEMENTED, "the GPU Z-grid supports 1 to 3 dimensions");
             return 0;
@@ -382,6 +379,20 @@ static int validate(TayState *state) {
         sp->pass = *t;
         sp->seer_group = state->groups[seer].slot;
         sp->seen_group = p->is_see ? state->groups[seen].slot : sp->seer_group;
+    }
+    /* a group's shape must be the one its device model holds: the reference's grids take
+     * point agents only ("grid structure can only contain point agents"); here box
+     * agents have their own device model and the Z-grid keys them by their min corner */
+    for (unsigned k = 0; k < state->passes_count; ++k) {
+        const TayPass *p = state->passes + k;
+        int np = tgpu_model_nonpoint(p->func_name);
+        if (np < 0) continue;
+        if ((np == 1) == (p->seer_group->is_point != 0) ||
+            (p->is_see && (np == 1) == (p->seen_group->is_point != 0))) {
+            set_error(state, TAY_ERROR_POINT_NONPOINT_MISMATCH, "pass %u: '%s' takes %s agents", k, p->func_name,
+                      np ? "non-point" : "point");
+            return 0;
+        }
     }
     for (int s = 0; s < state->ngpu; ++s) {
         const TayGroup *g = state->groups + state->gpu_slots[s];

@@ -27,13 +27,28 @@ BOIDS_RECORD = np.dtype([("tag", "<u4", 2), ("p",) + F4, ("v",) + F4, ("coh",) +
                          ("sep",) + F4, ("count", "<i4"), ("sep_count", "<i4"), ("id", "<i4"), ("pad", "<i4")])
 SPH_RECORD = np.dtype([("tag", "<u4", 2), ("p",) + F4, ("v",) + F4, ("a",) + F4, ("rho", "<f4"), ("P", "<f4"),
                        ("id", "<i4"), ("pad", "<i4")])
+BOX_RECORD = np.dtype([("tag", "<u4", 2), ("min",) + F4, ("max",) + F4, ("v",) + F4, ("b_buffer",) + F4,
+                       ("b_buffer_count", "<i4"), ("f_buffer",) + F4, ("id", "<i4")])
 assert TEST_RECORD.itemsize == 80 and BOIDS_RECORD.itemsize == 104 and SPH_RECORD.itemsize == 72
+assert BOX_RECORD.itemsize == 96
 
 
 def records(dtype, p, v):
     n = p.shape[0]
     rec = np.zeros(n, dtype)
     rec["p"] = p
+    rec["v"] = v
+    rec["id"] = np.arange(n, dtype=np.int32)
+    return rec
+
+
+def box_records(lo, hi, v):
+    """Box-agent records (the reference's BoxAgent, test/agent.h:21-29) from min / max
+    corners and velocities ([N,4] arrays)."""
+    n = lo.shape[0]
+    rec = np.zeros(n, BOX_RECORD)
+    rec["min"] = lo
+    rec["max"] = hi
     rec["v"] = v
     rec["id"] = np.arange(n, dtype=np.int32)
     return rec
@@ -89,6 +104,7 @@ class Setup:
     fixed_box: tuple | None = None
     extra: dict = field(default_factory=dict)
     dims: int = 3
+    is_point: bool = True
 
 
 def test_setup(radius=50.0, part=50.0, passes=("agent_see", "agent_act"), mb=250):
@@ -100,6 +116,18 @@ def test_setup(radius=50.0, part=50.0, passes=("agent_see", "agent_act"), mb=250
         else:
             lst.append(Pass("agent_act", False, act))
     return Setup(TEST_RECORD, lst, part, mb)
+
+
+def box_setup(radius=50.0, part=50.0, passes=("box_agent_see", "box_agent_act"), mb=250):
+    """The reference's box agents: a non-point group."""
+    see, act = test_contexts(radius)
+    lst = []
+    for p in passes:
+        if p == "box_agent_see":
+            lst.append(Pass("box_agent_see", True, see, radius, False))
+        else:
+            lst.append(Pass("box_agent_act", False, act))
+    return Setup(BOX_RECORD, lst, part, mb, is_point=False)
 
 
 def boids_setup(r=10.0, part=10.0, passes=("boids_see", "boids_act"), mb=250):
@@ -119,7 +147,7 @@ def sph_setup(h=0.02, part=None, passes=("sph_density", "sph_pressure", "sph_for
 def make_state(setup: Setup, recs: np.ndarray):
     """Creates a state with one TAY_GPU_Z_GRID group holding `recs`, passes registered."""
     st = api.State()
-    g = st.add_group(setup.dtype.itemsize, max(1, recs.shape[0]), True)
+    g = st.add_group(setup.dtype.itemsize, max(1, recs.shape[0]), setup.is_point)
     st.configure_space(g, api.TAY_GPU_Z_GRID, setup.dims, api.f4(setup.part), setup.mb)
     if setup.fixed_box is not None:
         st.fix_space_box(g, api.f4(*setup.fixed_box[0]), api.f4(*setup.fixed_box[1]))
@@ -143,7 +171,7 @@ def run(setup: Setup, recs: np.ndarray, steps: int):
     return out
 
 
-def run_groups(dtype, funcs, groups, passes, see_ctx, act_ctx, radius, part, steps, mb=8):
+def run_groups(dtype, funcs, groups, passes, see_ctx, act_ctx, radius, part, steps, mb=8, is_point=True):
     """A state of several groups of one model mixed by its passes, through the C API.
     `funcs` = (see func name, act func name); `groups` = record arrays (id order);
     `passes` = ("see", seer, seen, self_see) / ("act", group) tuples in registration
@@ -153,7 +181,7 @@ def run_groups(dtype, funcs, groups, passes, see_ctx, act_ctx, radius, part, ste
     st = api.State()
     gs = []
     for recs in groups:
-        g = st.add_group(dtype.itemsize, recs.shape[0], True)
+        g = st.add_group(dtype.itemsize, recs.shape[0], is_point)
         st.configure_space(g, api.TAY_GPU_Z_GRID, 3, part, mb)
         gs.append(g)
     for p in passes:

@@ -101,6 +101,28 @@ def boids_points(n: int = 1 << 20, seed: int = 2, clusters: int = 64, sigma: flo
 
 
 @dataclass
+class BoxSet:
+    lo: np.ndarray   # [N, 4] float32 min corners
+    hi: np.ndarray   # [N, 4] float32 max corners
+    v: np.ndarray    # [N, 4] float32 velocities
+
+
+def box_agents(n: int = 10_000, seed: int = 3, side: float = 1000.0, min_size: float = 1.0,
+               max_size: float = 50.0, speed: float = 1.0) -> BoxSet:
+    """Cubes of edge U[min_size, max_size] placed inside [0, side]^3 with velocity of the given
+    speed in a uniform random direction (the reference's non-point test population,
+    test/test.c:133-170, with its sizes 1..50 and speed 1)."""
+    s = Stream(seed)
+    size = s.uniform(n, min_size, max_size)
+    u = s.uniform(3 * n, 0.0, 1.0).reshape(n, 3)
+    lo = u * (side - size[:, None])
+    hi = lo + size[:, None]
+    d = s.uniform(3 * n, -1.0, 1.0).reshape(n, 3)
+    d *= speed / np.maximum(np.linalg.norm(d, axis=1, keepdims=True), 1e-12)
+    return BoxSet(_pack4(lo), _pack4(hi), _pack4(d))
+
+
+@dataclass
 class SphSetup:
     points: PointSet
     tank_min: tuple

@@ -33,6 +33,9 @@ Space-option cases (golden_space.npz):
                  CpuGrid / CpuZGrid
   (the reference's CpuZGrid pairs nothing below 3 dims, tay/cpu_z_grid.c:254-260, so
   dims < 3 is pinned on CpuSimple / CpuGrid)
+  box_see_simple  the reference's box agents (non-point group), 2000 cubes of edge 1..50
+                  in [0,1000]^3, r = 50, see only, 1 step, CpuSimple
+  box_full_simple the same, see + act, 5 steps
 """
 import os
 import sys
@@ -103,6 +106,14 @@ def space_cases():
         yield f"fixed_{space}", space, rec, see, act, 3, full, 3, box
 
 
+def box_cases():
+    b = W.box_agents(2000, seed=122)
+    rec = O.make_box_records(b.lo, b.hi, b.v)
+    see, act = np.array([50, 50, 50, 0], np.float32), O.test_act_context(np.float32)
+    yield "box_see_simple", "simple", rec, see, act, 1, O.PASS_SEE0, 3, None
+    yield "box_full_simple", "simple", rec, see, act, 5, O.PASS_SEE0 | O.PASS_ACT0, 3, None
+
+
 def pass_table(passes):
     return np.array([[1 if p[0] == "see" else 0, p[1], p[2] if p[0] == "see" else p[1], int(p[3]) if p[0] == "see" else 0]
                      for p in passes], np.int64)
@@ -139,11 +150,12 @@ def main():
         print(f"{name}: {[r.shape[0] for r in recs]} agents, {steps} steps")
     np.savez_compressed(os.path.join(HERE, "golden_groups.npz"), **out)
     out = {}
-    for name, space, rec, see, act, steps, mask, dims, box in space_cases():
-        r = ref.run(O.MODEL_TEST, space, rec, see, act, 50.0, 50.0, steps, mask, threads=4, dims=dims, box=box)
+    opt_cases = [(O.MODEL_TEST,) + c for c in space_cases()] + [(O.MODEL_BOX,) + c for c in box_cases()]
+    for model, name, space, rec, see, act, steps, mask, dims, box in opt_cases:
+        r = ref.run(model, space, rec, see, act, 50.0, 50.0, steps, mask, threads=4, dims=dims, box=box)
         out[f"{name}__in"] = rec
         out[f"{name}__out"] = r.records
-        out[f"{name}__meta"] = np.array([O.MODEL_TEST, O.SPACE[space], steps, mask, dims], np.int64)
+        out[f"{name}__meta"] = np.array([model, O.SPACE[space], steps, mask, dims], np.int64)
         out[f"{name}__box"] = np.zeros((2, 3)) if box is None else np.array(box, np.float64)
         out[f"{name}__fixed"] = np.array([0 if box is None else 1], np.int64)
         out[f"{name}__see"] = see

@@ -27,13 +27,13 @@ GOLD, GOLD_NAMES = _golden()
 def same_records(model, a, b):
     """Bit-for-bit equality of every field the reference defines.  The reference's test
     model leaves the w components of b_buffer and f_buffer undefined (its float4 helpers
-    return structs whose w is never set, test/taystd.c:109-135), so those two floats are
-    excluded for that model."""
-    if model != O.MODEL_TEST:
+    return structs whose w is never set, test/taystd.c:109-135), and the box model also
+    those of min and max, so those floats are excluded for these models."""
+    if model not in (O.MODEL_TEST, O.MODEL_BOX):
         return a.tobytes() == b.tobytes()
     for f in a.dtype.names:
         x, y = a[f], b[f]
-        if f in ("b_buffer", "f_buffer"):
+        if f in ("b_buffer", "f_buffer", "min", "max"):
             x, y = x[:, :3], y[:, :3]
         if np.ascontiguousarray(x).tobytes() != np.ascontiguousarray(y).tobytes():
             return False
