@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--stage", type=int, default=None, help="see kernel: 1 = stage halos in shared memory")
     ap.add_argument("--union-factor", type=int, default=None, help="see kernel: union walk threshold")
     ap.add_argument("--cell-order", type=int, default=None, help="0 = Morton cells, 1 = x-rows")
+    ap.add_argument("--hit-masks", type=int, default=None, help="1 = see walk with hit masks (cell order 1)")
     ap.add_argument("--cell-multiple", type=float, default=None, help="grid cell edge / min part size")
     return ap.parse_args()
 
@@ -360,7 +361,8 @@ def run_gb300(args, rank, world, D):
 
     api.set_tuning()  # library defaults, then the autotuner's choice or command-line overrides
     over = {k: v for k, v in (("stage", args.stage), ("union_factor", args.union_factor),
-                              ("cell_multiple", args.cell_multiple), ("cell_order", args.cell_order)) if v is not None}
+                              ("cell_multiple", args.cell_multiple), ("cell_order", args.cell_order),
+                              ("hit_masks", args.hit_masks)) if v is not None}
     tuned = None
     if over:
         api.set_tuning(**over)
@@ -426,14 +428,19 @@ def run_gb300(args, rank, world, D):
     see_bytes = N_BOIDS * 64
     achieved = see_bytes / (see_ms / 1000.0) / 1e9
     step_ms = sum(prof) / prof_steps
-    # whole-step algorithmic bytes (key from position 16 B, key+index write 8 B, reorder of
-    # the 36 B state read+write, see+act 64 B)
-    step_bytes = N_BOIDS * (16 + 8 + 2 * 36 + 64)
+    # whole-step algorithmic bytes, counted as if see and act were separate passes (the
+    # accumulators written and read back): per agent, key from position 16 B, key + index
+    # write 8 B, reorder of the 36 B state read + write, see 32 B seen + 40 B accumulators,
+    # act 2 x 36 B state + 40 B accumulators = 280 B
+    step_bytes = N_BOIDS * (16 + 8 + 2 * 36 + (32 + 40) + (2 * 36 + 40))
+    see_name = "see_rows_kernel<boids::SeeAct>" if api.get_tuning().get("cell_order") == 1 else "see_kernel<boids::SeeAct>"
     traffic = None
     tp = os.path.join(ROOT, "profiles", "see_boids_traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+            tj = json.load(f)
+        if tj.get("kernel", see_name) == see_name:
+            traffic = tj.get("dram_bytes_per_launch")
     if rank == 0:
         line = {
             "metric": "pair-interactions/s", "value": all_pairs / secs, "unit": "pair-interactions/s",
@@ -448,7 +455,7 @@ def run_gb300(args, rank, world, D):
                     "d2h_bytes_per_step": N_BOIDS * BOIDS_RECORD_BYTES, "steps": e2e_steps,
                     "ms_per_step": 1000.0 * e2e_s / e2e_steps},
             "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "kernel": "see_kernel<boids::SeeAct>", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": see_name, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": see_bytes, "launch_ms": see_ms},
             "step_roofline": {"achieved": step_bytes / (step_ms / 1000.0) / 1e9, "unit": "GB/s",

@@ -160,7 +160,9 @@ int tgpu_batch_program(const TgpuBatch *batch);
  *   use_graphs     capture each step in a CUDA graph and replay it
  *   cell_order     0: cells in 3-D Morton order, a {first, end} table entry per cell;
  *                  1: x-rows (x fastest inside (y, z) rows, rows in 2-D Morton order),
- *                  a seer's box is one candidate range per row (no staging) */
+ *                  a seer's box is one candidate range per row (no staging)
+ *   hit_masks      cell order 1: each lane box-tests up to 32 candidates into a mask
+ *                  before the lanes run the see function over their hits together */
 typedef struct TgpuTuning {
     int stage;
     unsigned stage_cap;
@@ -169,6 +171,7 @@ typedef struct TgpuTuning {
     unsigned union_factor;
     int use_graphs;
     unsigned cell_order;
+    unsigned hit_masks;
 } TgpuTuning;
 
 void tgpu_set_tuning(const TgpuTuning *tuning);  /* NULL restores the defaults */

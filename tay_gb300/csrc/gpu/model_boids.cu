@@ -122,6 +122,7 @@ struct SeeOnly {
     using ActCtx = Ctx;
     using Seer = boids::Seer;
     static constexpr int kSeenF4 = 2;
+    static constexpr int kLaneUnroll = 4;
     TGPU_D static int seen_stream(int k) { return k == 0 ? POS : VEL; }
     TGPU_D static void load(Seer &s, const PassIO &, uint32_t, const Ctx &, const Ctx &) { zero(s); }
     template <class Acc>
@@ -140,6 +141,7 @@ struct SeeAct {
     using ActCtx = Ctx;
     using Seer = boids::Seer;
     static constexpr int kSeenF4 = 2;
+    static constexpr int kLaneUnroll = 4;
     TGPU_D static int seen_stream(int k) { return k == 0 ? POS : VEL; }
     TGPU_D static void load(Seer &s, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {
         zero(s);

@@ -54,6 +54,7 @@ TgpuTuning default_tuning() {
     t.union_factor = 1;
     t.use_graphs = 1;
     t.cell_order = 0;
+    t.hit_masks = 0;
     return t;
 }
 TgpuTuning g_tuning = default_tuning();
@@ -210,7 +211,12 @@ int tgpu::prepare_specs(TgpuBatch *b) {
         uint64_t cap_axis = (uint64_t)axis * axis * axis;
         uint64_t cap = std::min(cap_mem, cap_axis);
         cap = std::max<uint64_t>(cap, 8);
-        cap = std::min<uint64_t>(cap, 0x7FFFFFFFull);
+        cap = std::min<uint64_t>(cap, 0x7FFFFFFEull);
+        cap = (cap + 1) & ~1ull;  // even: every segment's table starts 16-byte aligned (row headers)
+        // row order: headers for up to axis^2 rows, at most a quarter of the table
+        sp.row_cap = b->cell_order == kOrderRows
+                         ? (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)axis * axis, cap / 4))
+                         : 0u;
         sp.table_base = (uint32_t)table_total;
         sp.table_cap = (uint32_t)cap;
         table_total += cap;
@@ -347,6 +353,7 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E) {
             S.stage_cells = r.stage_cells;
             S.union_factor = r.union_factor;
             S.rows = b->cell_order == kOrderRows ? 1u : 0u;
+            S.hit_masks = b->hit_masks;
             if (r.seer_seg >= 0) {
                 // one seer segment; the seen agents are another segment's (or its own)
                 S.cta_offset = b->cta_begin[r.seer_seg];
@@ -732,6 +739,7 @@ int tgpu_batch_create(const TgpuGroup *groups, int group_count, TgpuBatch **out)
     b->nseg = group_count;
     b->use_graphs = g_tuning.use_graphs != 0;
     b->cell_order = g_tuning.cell_order == kOrderRows ? kOrderRows : kOrderMorton;
+    b->hit_masks = g_tuning.hit_masks ? 1u : 0u;
     int rc = add_segments(b, groups, group_count, reach);
     if (!rc) rc = alloc_batch(b);
     const ProgramDesc &pd = m->programs[program];
@@ -797,6 +805,7 @@ int tgpu_state_create(const TgpuGroup *groups, int group_count, const TgpuStateP
     b->nseg = group_count;
     b->use_graphs = g_tuning.use_graphs != 0;
     b->cell_order = g_tuning.cell_order == kOrderRows ? kOrderRows : kOrderMorton;
+    b->hit_masks = g_tuning.hit_masks ? 1u : 0u;
     b->state_passes.assign(passes, passes + pass_count);
     int rc = add_segments(b, groups, group_count, reach);
     if (!rc) rc = alloc_batch(b);

@@ -82,6 +82,7 @@ struct TgpuBatch {
     bool use_graphs = true;
     uint32_t cell_order = kOrderMorton;  // key order and table layout of every segment
     BoxAcc *d_extent = nullptr;          // pushed extent of one group
+    uint32_t hit_masks = 0;              // see walk: hit masks (row order)
     std::map<uint64_t, cudaGraphExec_t> graphs;
 };
 

@@ -147,32 +147,89 @@ TGPU_D void union_batches(typename P::Seer &s, const float4 &sp, const float4 &r
     }
 }
 
-// Per-lane walk over candidates [j0, j1): two candidates per iteration for independent
-// loads in flight.
+// Candidates a lane loads per iteration of its walk: P::kLaneUnroll when the pass
+// declares one (light see bodies gain from more loads in flight), else 2.
+template <class P, class = void>
+struct UnrollOf {
+    static constexpr int value = 2;
+};
+template <class P>
+struct UnrollOf<P, decltype((void)P::kLaneUnroll)> {
+    static constexpr int value = P::kLaneUnroll;
+};
+
+// Per-lane walk over candidates [j0, j1): UnrollOf<P> candidates per iteration for
+// independent loads in flight.
 template <class P, class Acc>
 TGPU_D void lane_run(typename P::Seer &s, const float4 &sp, const float4 &r4, uint32_t j0, uint32_t j1, uint32_t self,
                      const float4 *src, const Acc &acc, const typename P::SeeCtx &sctx, uint32_t &pairs,
                      uint32_t &tested) {
     constexpr bool kGlobal = Acc::kGlobal;
+    constexpr int U = UnrollOf<P>::value;
     tested += j1 - j0;
     uint32_t j = j0;
-    for (; j + 1 < j1; j += 2) {
+    for (; j + (U - 1) < j1; j += U) {
+        float4 b[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) b[u] = load_pos(src, j + u, kGlobal);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (j + u != self && box_hit(sp, b[u], r4)) {
+                ++pairs;
+                P::see(s, sp, b[u], acc, j + u, sctx);
+            }
+    }
+    for (; j < j1; ++j) {
         const float4 b0 = load_pos(src, j, kGlobal);
-        const float4 b1 = load_pos(src, j + 1, kGlobal);
         if (j != self && box_hit(sp, b0, r4)) {
             ++pairs;
             P::see(s, sp, b0, acc, j, sctx);
-        }
-        if (j + 1 != self && box_hit(sp, b1, r4)) {
-            ++pairs;
-            P::see(s, sp, b1, acc, j + 1, sctx);
         }
     }
-    if (j < j1) {
-        const float4 b0 = load_pos(src, j, kGlobal);
-        if (j != self && box_hit(sp, b0, r4)) {
-            ++pairs;
-            P::see(s, sp, b0, acc, j, sctx);
+}
+
+// Candidate range of cells [x0, x1] of one row of a row-order table: the header and the
+// two start entries are loaded together; an entry is used only inside the row's occupied
+// span (x_first, x_last], where it is valid for this step.
+TGPU_D uint2 row_range(const uint32_t *words, const uint4 *hdr, uint32_t row, uint32_t dx, int x0, int x1) {
+    const uint4 h = __ldg(hdr + row);
+    const uint32_t e0 = __ldg(words + row * dx + (uint32_t)x0);
+    const uint32_t e1 = __ldg(words + row * dx + min((uint32_t)x1 + 1u, dx - 1u));
+    if ((uint32_t)x0 > h.y || (uint32_t)x1 < h.x) return make_uint2(0u, 0u);
+    return make_uint2((uint32_t)x0 <= h.x ? h.z : e0, (uint32_t)x1 >= h.y ? h.w : e1);
+}
+
+// Per-lane candidates [j0, j1) in batches of 32, the see function run over hit masks:
+// every lane box-tests its own next (up to) 32 candidates into a mask, then the lanes
+// with hits run the see function together, one hit each per round, so the see body runs
+// for all lanes that have hits instead of for the few whose current candidate passed.
+// All 32 lanes of the warp must call it (lanes with an empty range pass j0 = j1).
+template <class P, class Acc>
+TGPU_D void lane_run_masked(typename P::Seer &s, const float4 &sp, const float4 &r4, uint32_t j0, uint32_t j1,
+                            uint32_t self, const float4 *pos, const Acc &acc, const typename P::SeeCtx &sctx,
+                            uint32_t &pairs, uint32_t &tested) {
+    tested += j1 - j0;
+    for (uint32_t jb = j0; __any_sync(0xffffffffu, jb < j1); jb += 32u) {
+        const uint32_t nb = jb < j1 ? min(32u, j1 - jb) : 0u;
+        uint32_t hits = 0;
+        uint32_t k = 0;
+        for (; k + 1 < nb; k += 2) {
+            const float4 b0 = __ldg(pos + jb + k);
+            const float4 b1 = __ldg(pos + jb + k + 1);
+            hits |= (uint32_t)(box_hit(sp, b0, r4) && jb + k != self) << k;
+            hits |= (uint32_t)(box_hit(sp, b1, r4) && jb + k + 1 != self) << (k + 1);
+        }
+        if (k < nb) {
+            const float4 b0 = __ldg(pos + jb + k);
+            hits |= (uint32_t)(box_hit(sp, b0, r4) && jb + k != self) << k;
+        }
+        pairs += __popc(hits);
+        while (__any_sync(0xffffffffu, hits != 0u)) {
+            if (hits) {
+                const uint32_t j = jb + (uint32_t)(__ffs(hits) - 1);
+                hits &= hits - 1u;
+                P::see(s, sp, __ldg(pos + j), acc, j, sctx);
+            }
         }
     }
 }
@@ -455,8 +512,9 @@ __global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
         P::load(s, L.io, i, sctx, actx);
         seer_cells<kBox>(sp, smax, r4, B, g, pad, lo, hi);
     }
-    const uint32_t *rows = reinterpret_cast<const uint32_t *>(L.table + T.table_base);
-    const uint32_t rw = (uint32_t)g.dims[0] + 1u, dy0 = (uint32_t)g.dims[1];
+    const uint4 *hdr = reinterpret_cast<const uint4 *>(L.table + T.table_base);
+    const uint32_t *words = reinterpret_cast<const uint32_t *>(L.table + T.table_base) + row_entry_word(T);
+    const uint32_t dx0 = (uint32_t)g.dims[0], dy0 = (uint32_t)g.dims[1];
     GlobalSeen<P::kSeenF4> acc;
 #pragma unroll
     for (int k = 0; k < P::kSeenF4; ++k) acc.s[k] = L.io.in_f4[P::seen_stream(k)];
@@ -476,20 +534,27 @@ __global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
         if (union_mode) {
             for (int z = wl2; z <= wh2; ++z)
                 for (int y = wl1; y <= wh1; ++y) {
-                    const uint32_t *r = rows + ((uint32_t)z * dy0 + (uint32_t)y) * rw;
-                    union_batches<P>(s, sp, r4, active, __ldg(r + wl0), __ldg(r + wh0 + 1), self, pos, acc, sctx, pairs,
-                                     tested);
+                    const uint2 jr = row_range(words, hdr, (uint32_t)z * dy0 + (uint32_t)y, dx0, wl0, wh0);
+                    union_batches<P>(s, sp, r4, active, jr.x, jr.y, self, pos, acc, sctx, pairs, tested);
+                }
+        } else if (!kBox && L.hit_masks) {
+            // rows of the warp's union box (a warp-uniform loop), each lane's own x range
+            for (int z = wl2; z <= wh2; ++z)
+                for (int y = wl1; y <= wh1; ++y) {
+                    uint2 jr = make_uint2(0u, 0u);
+                    if (active && z >= lo[2] && z <= hi[2] && y >= lo[1] && y <= hi[1])
+                        jr = row_range(words, hdr, (uint32_t)z * dy0 + (uint32_t)y, dx0, lo[0], hi[0]);
+                    lane_run_masked<P>(s, sp, r4, jr.x, jr.y, self, pos, acc, sctx, pairs, tested);
                 }
         } else if (active) {
             for (int z = lo[2]; z <= hi[2]; ++z)
                 for (int y = lo[1]; y <= hi[1]; ++y) {
-                    const uint32_t *r = rows + ((uint32_t)z * dy0 + (uint32_t)y) * rw;
+                    const uint2 jr = row_range(words, hdr, (uint32_t)z * dy0 + (uint32_t)y, dx0, lo[0], hi[0]);
                     if (kBox)
-                        lane_run_boxes<P>(s, sp, smax, r4, __ldg(r + lo[0]), __ldg(r + hi[0] + 1), self, pos,
-                                          L.io.in_f4[1], acc, sctx, pairs, tested);
+                        lane_run_boxes<P>(s, sp, smax, r4, jr.x, jr.y, self, pos, L.io.in_f4[1], acc, sctx, pairs,
+                                          tested);
                     else
-                        lane_run<P>(s, sp, r4, __ldg(r + lo[0]), __ldg(r + hi[0] + 1), self, pos, acc, sctx, pairs,
-                                    tested);
+                        lane_run<P>(s, sp, r4, jr.x, jr.y, self, pos, acc, sctx, pairs, tested);
                 }
         }
     }

@@ -360,55 +360,52 @@ __global__ void __launch_bounds__(kSortThreads) cell_table_kernel(const SegmentS
     const uint32_t seg_end = s.begin + s.count;
     const uint32_t end = min(beg + (uint32_t)kSortTile, seg_end);
     if (s.order == kOrderRows) {
-        // Each lane derives up to two fills (an entry range of one row and its value);
-        // the warp then writes every lane's fills together, 32 consecutive entries per
-        // store, since the head and tail fills of a row span most of it.
-        uint32_t *rows = reinterpret_cast<uint32_t *>(table + s.table_base);
+        // The first agent of a row writes its header's x_first / first, the last agent
+        // x_last / end, and the first agent of every other cell the start entries of the
+        // cells after the previous occupied one up to its own; the clear zeroes headers.
+        // Gap fills are written by the warp together, 32 consecutive entries per store.
+        uint4 *hdr = reinterpret_cast<uint4 *>(table + s.table_base);
+        uint32_t *words = reinterpret_cast<uint32_t *>(table + s.table_base) + row_entry_word(s);
         const uint32_t b = axis_bits(s);
         const uint32_t xmask = (1u << b) - 1u;
-        const uint32_t dx = (uint32_t)g.dims[0], rw = dx + 1u;
+        const uint32_t dx = (uint32_t)g.dims[0];
         const uint32_t lane = threadIdx.x & 31u;
         for (uint32_t base = beg; base < end; base += kSortThreads) {
             const uint32_t i = base + threadIdx.x;
-            uint32_t off[2] = {0u, 0u}, len[2] = {0u, 0u}, val[2] = {0u, 0u};
+            uint32_t off = 0u, len = 0u;
             if (i < end) {
                 const uint32_t k = keys[i];
                 const uint32_t row = k >> b, x = k & xmask;
                 const bool row_first = (i == s.begin) || (keys[i - 1] >> b) != row;
                 const bool row_last = (i + 1 == seg_end) || (keys[i + 1] >> b) != row;
-                const bool first = row_first || keys[i - 1] != k;
                 const uint32_t y = compact2_10(row), z = compact2_10(row >> 1);
-                const uint32_t r0 = (z * (uint32_t)g.dims[1] + y) * rw;
+                const uint32_t r = z * (uint32_t)g.dims[1] + y;
                 if (!write_runs) {
-                    if (row_first) {
-                        off[0] = r0;
-                        len[0] = rw;
-                    }
+                    if (row_first) hdr[r] = make_uint4(0u, 0u, 0u, 0u);
                 } else {
-                    if (first) {
-                        const uint32_t x0 = row_first ? 0u : (keys[i - 1] & xmask) + 1u;
-                        off[0] = r0 + x0;
-                        len[0] = x + 1u - x0;
-                        val[0] = i;
+                    uint32_t *h = reinterpret_cast<uint32_t *>(hdr + r);
+                    if (row_first) {
+                        h[0] = x;
+                        h[2] = i;
+                    } else if (keys[i - 1] != k) {
+                        const uint32_t x0 = (keys[i - 1] & xmask) + 1u;
+                        off = r * dx + x0;
+                        len = x + 1u - x0;
                     }
                     if (row_last) {
-                        off[1] = r0 + x + 1u;
-                        len[1] = dx - x;
-                        val[1] = i + 1u;
+                        h[1] = x;
+                        h[3] = i + 1u;
                     }
                 }
             }
-#pragma unroll
-            for (int t = 0; t < 2; ++t) {
-                uint32_t m = __ballot_sync(0xffffffffu, len[t] > 0u);
-                while (m) {
-                    const int l = __ffs(m) - 1;
-                    m &= m - 1u;
-                    const uint32_t o = __shfl_sync(0xffffffffu, off[t], l);
-                    const uint32_t n = __shfl_sync(0xffffffffu, len[t], l);
-                    const uint32_t v = __shfl_sync(0xffffffffu, val[t], l);
-                    for (uint32_t c = lane; c < n; c += 32u) rows[o + c] = v;
-                }
+            uint32_t m = __ballot_sync(0xffffffffu, len > 0u);
+            while (m) {
+                const int l = __ffs(m) - 1;
+                m &= m - 1u;
+                const uint32_t o = __shfl_sync(0xffffffffu, off, l);
+                const uint32_t n = __shfl_sync(0xffffffffu, len, l);
+                const uint32_t v = __shfl_sync(0xffffffffu, i, l);
+                for (uint32_t c = lane; c < n; c += 32u) words[o + c] = v;
             }
         }
         return;

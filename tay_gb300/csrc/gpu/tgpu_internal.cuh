@@ -41,6 +41,7 @@ struct SegmentSpec {
     uint32_t fixed_box;      // 1: use box_min/box_max instead of the agents' bounding box
     uint32_t order;          // cell order of the keys and table layout: kOrderMorton / kOrderRows
     uint32_t dims;           // tay_configure_space dims (1..3; 0 means 3): axes >= dims get one cell
+    uint32_t row_cap;        // row order: (y, z) rows the table's header region holds
     float part[3];           // minimum cell edge per axis
     float reach[3];          // largest see radius per axis over the segment's see passes
     float box_min[3];        // fixed space box (tay_fix_space_box)
@@ -100,6 +101,32 @@ TGPU_HD int clamp_cells(float cells, uint32_t axis_max) {
 
 TGPU_HD int seg_dims(const SegmentSpec &s) { return (s.dims >= 1u && s.dims <= 3u) ? (int)s.dims : 3; }
 
+// Two cell orders.  kOrderMorton: the 3-D Morton key, a table entry {first, end} per
+// cell.  kOrderRows: x fastest inside rows of constant (y, z), the rows in 2-D Morton
+// order of (y, z): key = (morton2(y, z) << b) | x with b = log2(axis_cells_max), so the
+// agents of x-adjacent cells are contiguous and a seer's box is one candidate range per
+// row.  Its table holds, per row, a 16-byte header {x_first, x_last, first, end} (the
+// occupied cells and the row's agent range; zero for an empty row) and, per cell x in
+// (x_first, x_last], the first agent of the row in a cell >= x; entries outside that span
+// are never read.  Both orders give the same neighbour sets; only the order in which a
+// seer meets its neighbours differs.
+enum CellOrder : uint32_t { kOrderMorton = 0, kOrderRows = 1 };
+
+// Row-order table layout (u32 words from the segment's table base): the row headers
+// (uint4, 16-byte aligned) at word 0 for up to row_cap rows, then the start entries at
+// word 4 * row_cap + row * dims[0] + x.  The header region's place does not depend on the
+// step's grid, so a header is never a stale entry of an earlier step: every step's clear
+// leaves all headers zero.
+TGPU_HD uint32_t row_entry_word(const SegmentSpec &s) { return 4u * s.row_cap; }
+
+// Whether a grid fits the segment's table.
+TGPU_HD bool table_fits(const SegmentSpec &s, const int *d) {
+    const unsigned long long cells = (unsigned long long)d[0] * (unsigned long long)d[1] * (unsigned long long)d[2];
+    if (s.order != kOrderRows) return cells <= s.table_cap;
+    const unsigned long long rows = (unsigned long long)d[1] * (unsigned long long)d[2];
+    return rows <= s.row_cap && 4ull * s.row_cap + cells <= 2ull * s.table_cap;
+}
+
 TGPU_HD Grid derive_grid(const SegmentSpec &s, const float *mn, const float *mx) {
     Grid g;
     float cs[3], ext[3];
@@ -118,14 +145,13 @@ TGPU_HD Grid derive_grid(const SegmentSpec &s, const float *mn, const float *mx)
         }
     }
     for (int iter = 0; iter < 64; ++iter) {
-        unsigned long long total = (unsigned long long)d[0] * (unsigned long long)d[1] * (unsigned long long)d[2];
-        if (total <= s.table_cap) break;
+        if (table_fits(s, d)) break;
         for (int i = 0; i < seg_dims(s); ++i) {
             cs[i] *= 1.25f;
             d[i] = clamp_cells(floorf(ext[i] / cs[i]) + 1.0f, s.axis_cells_max);
         }
     }
-    if ((unsigned long long)d[0] * (unsigned long long)d[1] * (unsigned long long)d[2] > s.table_cap) {
+    if (!table_fits(s, d)) {
         for (int i = 0; i < 3; ++i) {
             d[i] = 1;
             cs[i] = ext[i] > cs[i] ? ext[i] : cs[i];
@@ -188,14 +214,6 @@ TGPU_HD uint32_t compact2_10(uint32_t v) {
     return v & 0x3FFu;
 }
 
-// Two cell orders.  kOrderMorton: the 3-D Morton key above, table of {first, end} per
-// cell.  kOrderRows: x fastest inside rows of constant (y, z), the rows in 2-D Morton
-// order of (y, z): key = (morton2(y, z) << b) | x with b = log2(axis_cells_max), so the
-// agents of x-adjacent cells are contiguous and a seer's box is one candidate range per
-// row.  Its table holds per row dims[0] + 1 start offsets: entry x is the first agent of
-// the row in a cell >= x, entry dims[0] the row's end.  Both orders give the same
-// neighbour sets; only the order in which a seer meets its neighbours differs.
-enum CellOrder : uint32_t { kOrderMorton = 0, kOrderRows = 1 };
 
 TGPU_HD uint32_t axis_bits(const SegmentSpec &s) {
 #ifdef __CUDA_ARCH__
