@@ -353,6 +353,7 @@ int tgpu_adjoint_forward(TgpuAdjoint *a) {
     cudaError_t e = cudaStreamSynchronize(b->st);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return fail(TGPU_ERR_CUDA, "adjoint forward: %s", cudaGetErrorString(e));
+    if (int rc = check_device_error(b)) return rc;
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, a->e0, a->e1);
     a->fwd_ms = ms;
@@ -399,6 +400,7 @@ int tgpu_adjoint_backward(TgpuAdjoint *a, const float *dl_dpos, const float *dl_
     cudaError_t e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return fail(TGPU_ERR_CUDA, "adjoint backward: %s", cudaGetErrorString(e));
+    if (int rc = check_device_error(b)) return rc;
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, a->e0, a->e1);
     a->bwd_ms = ms;

@@ -48,9 +48,9 @@ constexpr size_t kOffKeys0 = align256(kOffCta + sizeof(uint2) * kNoallocCtas);
 constexpr size_t kOffKeys1 = align256(kOffKeys0 + sizeof(uint32_t) * kNoallocMaxAgents);
 constexpr size_t kOffVals0 = align256(kOffKeys1 + sizeof(uint32_t) * kNoallocMaxAgents);
 constexpr size_t kOffVals1 = align256(kOffVals0 + sizeof(uint32_t) * kNoallocMaxAgents);
-constexpr size_t kOffCounts = align256(kOffVals1 + sizeof(uint32_t) * kNoallocMaxAgents);
-constexpr size_t kOffPartials = align256(kOffCounts + sizeof(uint32_t) * 256 * kNoallocTiles);
-constexpr size_t kOffTable = align256(kOffPartials + sizeof(uint32_t) * 8);
+constexpr size_t kOffSortScratch = align256(kOffVals1 + sizeof(uint32_t) * kNoallocMaxAgents);
+constexpr size_t kOffErr = align256(kOffSortScratch + sort_scratch_bytes(1, kNoallocTiles));
+constexpr size_t kOffTable = align256(kOffErr + sizeof(uint32_t));
 constexpr size_t kOffPos = align256(kOffTable + sizeof(uint2) * kNoallocTable);
 constexpr size_t kOffAcc = align256(kOffPos + sizeof(float4) * kNoallocMaxAgents);
 constexpr size_t kNoallocBytes = align256(kOffAcc + sizeof(float4) * kNoallocMaxAgents);
@@ -167,8 +167,8 @@ extern "C" int tgpu_see_noalloc(const float *positions, unsigned n, const float 
     L.keys[1] = reinterpret_cast<uint32_t *>(scratch + kOffKeys1);
     L.vals[0] = reinterpret_cast<uint32_t *>(scratch + kOffVals0);
     L.vals[1] = reinterpret_cast<uint32_t *>(scratch + kOffVals1);
-    L.counts = reinterpret_cast<uint32_t *>(scratch + kOffCounts);
-    L.partials = reinterpret_cast<uint32_t *>(scratch + kOffPartials);
+    L.sort_scratch = reinterpret_cast<uint32_t *>(scratch + kOffSortScratch);
+    L.err = reinterpret_cast<uint32_t *>(scratch + kOffErr);
     L.table = reinterpret_cast<uint2 *>(scratch + kOffTable);
     L.segments = 1;
     L.tiles = spec.tile_count;
@@ -218,6 +218,12 @@ extern "C" int tgpu_see_noalloc(const float *positions, unsigned n, const float 
         char msg[200];
         snprintf(msg, sizeof(msg), "tgpu_see_noalloc: %s", cudaGetErrorString(e));
         return noalloc_fail(TGPU_ERR_CUDA, msg);
+    }
+    uint32_t err = 0;
+    e = cudaMemcpy(&err, scratch + kOffErr, sizeof(err), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && err) {
+        cudaMemset(scratch + kOffErr, 0, sizeof(err));
+        return noalloc_fail(TGPU_ERR_DEVICE, "tgpu_see_noalloc: radix sort look-back wait ran out");
     }
     return TGPU_OK;
 }

@@ -115,8 +115,8 @@ void free_batch(TgpuBatch *b) {
         cudaFree(b->keys[k]);
         cudaFree(b->vals[k]);
     }
-    cudaFree(b->counts);
-    cudaFree(b->partials);
+    cudaFree(b->sort_scratch);
+    cudaFree(b->d_err);
     cudaFree(b->table);
     cudaFree(b->d_aos);
     cudaFree(b->d_pairs);
@@ -156,6 +156,20 @@ float4 pass_radii(const TgpuPass &tp, int dims) {
     const float inf = INFINITY;
     return make_float4(tp.radii[0], dims > 1 ? tp.radii[1] : inf, dims > 2 ? tp.radii[2] : inf, tp.radii[3]);
 }
+
+}  // namespace
+
+// Reads and clears the device error word; kernels never trap, they record failures there.
+int tgpu::check_device_error(TgpuBatch *b) {
+    uint32_t err = 0;
+    CK(cudaMemcpy(&err, b->d_err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (!err) return TGPU_OK;
+    CK(cudaMemset(b->d_err, 0, sizeof(err)));
+    return fail(TGPU_ERR_DEVICE, "device error 0x%x%s", err,
+                (err & kErrSortLookback) ? " (radix sort look-back wait ran out)" : "");
+}
+
+namespace {
 
 int upload_contexts(TgpuBatch *b, int seg) {
     std::vector<char> buf(b->ctx_stride);
@@ -280,8 +294,8 @@ SortLaunch tgpu::sort_launch(TgpuBatch *b) {
     L.keys[1] = b->keys[1];
     L.vals[0] = b->vals[0];
     L.vals[1] = b->vals[1];
-    L.counts = b->counts;
-    L.partials = b->partials;
+    L.sort_scratch = b->sort_scratch;
+    L.err = b->d_err;
     L.table = b->table;
     L.segments = (uint32_t)b->nseg;
     L.tiles = b->tiles;
@@ -637,10 +651,9 @@ int alloc_batch(TgpuBatch *b) {
         CKR(cudaMalloc(&b->keys[k], sizeof(uint32_t) * n));
         CKR(cudaMalloc(&b->vals[k], sizeof(uint32_t) * n));
     }
-    const size_t ncounts = 256ull * std::max<uint32_t>(b->tiles, 1);
-    if ((ncounts + 4095) / 4096 > 4096) return fail(TGPU_ERR_ARG, "batch too large for the scan spine (%u tiles)", b->tiles);
-    CKR(cudaMalloc(&b->counts, sizeof(uint32_t) * ncounts));
-    CKR(cudaMalloc(&b->partials, sizeof(uint32_t) * ((ncounts + 4095) / 4096 + 1)));
+    CKR(cudaMalloc(&b->sort_scratch, sort_scratch_bytes((uint32_t)b->nseg, std::max<uint32_t>(b->tiles, 1))));
+    CKR(cudaMalloc(&b->d_err, sizeof(uint32_t)));
+    CKR(cudaMemset(b->d_err, 0, sizeof(uint32_t)));
     CKR(cudaMalloc(&b->d_aos, (size_t)m->agent_bytes * n));
     CKR(cudaMalloc(&b->d_pairs, sizeof(unsigned long long)));
     CKR(cudaMalloc(&b->d_telemetry, sizeof(unsigned long long) * 8));
@@ -938,7 +951,7 @@ int tgpu_batch_sync(TgpuBatch *b) {
     b->last_ms = ms;
     CK(cudaMemcpy(&b->last_pairs, b->d_pairs, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(b->last_telemetry, b->d_telemetry, sizeof(b->last_telemetry), cudaMemcpyDeviceToHost));
-    return TGPU_OK;
+    return check_device_error(b);
 }
 
 int tgpu_batch_run(TgpuBatch *b, int steps) {

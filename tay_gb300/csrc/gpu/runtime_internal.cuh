@@ -38,6 +38,8 @@ struct StepEvents {
     cudaEvent_t *ev2;
 };
 
+int check_device_error(TgpuBatch *b);
+
 }  // namespace tgpu
 
 using namespace tgpu;
@@ -64,7 +66,8 @@ struct TgpuBatch {
     uint32_t *u32[kMaxU32][2] = {};
     int cur_f4[kMaxF4] = {};
     int cur_u32[kMaxU32] = {};
-    uint32_t *keys[2] = {}, *vals[2] = {}, *counts = nullptr, *partials = nullptr;
+    uint32_t *keys[2] = {}, *vals[2] = {}, *sort_scratch = nullptr;
+    uint32_t *d_err = nullptr;  // device error word (DeviceError bits), read at every sync
     uint2 *table = nullptr;
     size_t table_entries = 0;
     uint32_t *d_aos = nullptr;

@@ -33,6 +33,11 @@ TGPU_D T warp_max(T v) {
     return v;
 }
 
+TGPU_D uint32_t digit_mask(uint32_t key_bits, int pass) {
+    const int bits = min(8, (int)key_bits - 8 * pass);
+    return bits >= 8 ? 0xFFu : ((1u << bits) - 1u);
+}
+
 TGPU_D uint32_t warp_incl_scan(uint32_t v) {
     for (int o = 1; o < 32; o <<= 1) {
         uint32_t w = __shfl_up_sync(0xffffffffu, v, o);
@@ -147,163 +152,136 @@ TGPU_D uint32_t count_index(const SegmentSpec &s, uint32_t digit, uint32_t local
     return 256u * s.tile_begin + digit * s.tile_count + local_tile;
 }
 
-__global__ void __launch_bounds__(kSortThreads) key_histogram_kernel(const SegmentSpec *__restrict__ specs,
-                                                                     const uint32_t *__restrict__ tile_seg,
-                                                                     const BoxAcc *__restrict__ box,
-                                                                     const float4 *__restrict__ pos,
-                                                                     uint32_t *__restrict__ keys,
-                                                                     uint32_t *__restrict__ counts, uint32_t mask) {
-    __shared__ uint32_t hist[256];
+// One pass over the positions: the grid from the box, the cell key of every agent, and
+// per-segment histograms of every 8-bit digit of the keys (order-independent, so all
+// passes' digit offsets are known before the first scatter).  hist layout:
+// [segment][pass][256].
+__global__ void __launch_bounds__(kSortThreads) keys_hist_kernel(const SegmentSpec *__restrict__ specs,
+                                                                 const uint32_t *__restrict__ tile_seg,
+                                                                 const BoxAcc *__restrict__ box,
+                                                                 const float4 *__restrict__ pos,
+                                                                 uint32_t *__restrict__ keys,
+                                                                 uint32_t *__restrict__ hist, int passes,
+                                                                 uint32_t key_bits) {
+    __shared__ uint32_t h[kMaxSortPasses][256];
     const uint32_t seg = tile_seg[blockIdx.x];
     const SegmentSpec s = specs[seg];
     const Grid g = segment_grid(s, box[seg]);
     const uint32_t t = blockIdx.x - s.tile_begin;
     const uint32_t beg = s.begin + t * kSortTile;
     const uint32_t end = min(beg + (uint32_t)kSortTile, s.begin + s.count);
-    hist[threadIdx.x] = 0;
+    for (int p = 0; p < passes; ++p) h[p][threadIdx.x] = 0;
     __syncthreads();
     for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads) {
-        float4 p = pos[i];
-        uint32_t cx = (uint32_t)cell_coord(p.x, g.origin[0], g.inv_cs[0], g.dims[0]);
-        uint32_t cy = (uint32_t)cell_coord(p.y, g.origin[1], g.inv_cs[1], g.dims[1]);
-        uint32_t cz = (uint32_t)cell_coord(p.z, g.origin[2], g.inv_cs[2], g.dims[2]);
+        float4 q = pos[i];
+        uint32_t cx = (uint32_t)cell_coord(q.x, g.origin[0], g.inv_cs[0], g.dims[0]);
+        uint32_t cy = (uint32_t)cell_coord(q.y, g.origin[1], g.inv_cs[1], g.dims[1]);
+        uint32_t cz = (uint32_t)cell_coord(q.z, g.origin[2], g.inv_cs[2], g.dims[2]);
         uint32_t k = cell_key(s, cx, cy, cz);
         keys[i] = k;
-        atomicAdd(&hist[k & mask], 1u);
+        for (int p = 0; p < passes; ++p) atomicAdd(&h[p][(k >> (8 * p)) & digit_mask(key_bits, p)], 1u);
     }
     __syncthreads();
-    counts[count_index(s, threadIdx.x, t)] = hist[threadIdx.x];
-}
-
-__global__ void __launch_bounds__(kSortThreads) digit_histogram_kernel(const SegmentSpec *__restrict__ specs,
-                                                                       const uint32_t *__restrict__ tile_seg,
-                                                                       const uint32_t *__restrict__ keys,
-                                                                       uint32_t *__restrict__ counts, int shift,
-                                                                       uint32_t mask) {
-    __shared__ uint32_t hist[256];
-    const uint32_t seg = tile_seg[blockIdx.x];
-    const SegmentSpec s = specs[seg];
-    const uint32_t t = blockIdx.x - s.tile_begin;
-    const uint32_t beg = s.begin + t * kSortTile;
-    const uint32_t end = min(beg + (uint32_t)kSortTile, s.begin + s.count);
-    hist[threadIdx.x] = 0;
-    __syncthreads();
-    for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads)
-        atomicAdd(&hist[(keys[i] >> shift) & mask], 1u);
-    __syncthreads();
-    counts[count_index(s, threadIdx.x, t)] = hist[threadIdx.x];
-}
-
-// ------------------------------------------------------------------ device-wide exclusive scan
-
-constexpr int kScanThreads = 1024;
-constexpr int kScanItems = 4;
-constexpr int kScanChunk = kScanThreads * kScanItems;
-
-// Block-wide exclusive scan of one value per thread; returns the exclusive prefix and
-// writes the block total.
-TGPU_D uint32_t block_excl_scan(uint32_t v, uint32_t *warp_sums, uint32_t *total) {
-    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
-    const uint32_t nwarps = blockDim.x >> 5;
-    uint32_t incl = warp_incl_scan(v);
-    if (lane == 31) warp_sums[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t w = lane < nwarps ? warp_sums[lane] : 0u;
-        uint32_t wi = warp_incl_scan(w);
-        if (lane < nwarps) warp_sums[lane] = wi - w;
-        if (lane == 31) *total = wi;
+    for (int p = 0; p < passes; ++p) {
+        const uint32_t c = h[p][threadIdx.x];
+        if (c) atomicAdd(&hist[((size_t)seg * kMaxSortPasses + p) * 256u + threadIdx.x], c);
     }
-    __syncthreads();
-    uint32_t r = warp_sums[warp] + incl - v;
-    __syncthreads();
-    return r;
 }
 
-__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const uint32_t *__restrict__ data,
-                                                                   uint32_t *__restrict__ partials, uint32_t n) {
-    __shared__ uint32_t warp_sums[32];
+// Per segment and pass: the histogram becomes each digit's first output slot (the
+// segment's begin plus the exclusive prefix over digits).  One 256-thread block per segment.
+__global__ void __launch_bounds__(256) digit_offsets_kernel(const SegmentSpec *__restrict__ specs,
+                                                            uint32_t *__restrict__ hist, int passes) {
+    __shared__ uint32_t warp_sums[8];
     __shared__ uint32_t total;
-    const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * kScanItems;
-    uint32_t sum = 0;
-    for (int k = 0; k < kScanItems; ++k)
-        if (base + k < n) sum += data[base + k];
-    block_excl_scan(sum, warp_sums, &total);
-    if (threadIdx.x == 0) partials[blockIdx.x] = total;
-}
-
-__global__ void __launch_bounds__(kScanThreads) scan_spine_kernel(uint32_t *__restrict__ partials, uint32_t n) {
-    __shared__ uint32_t warp_sums[32];
-    __shared__ uint32_t total;
-    const uint32_t base = threadIdx.x * kScanItems;
-    uint32_t v[kScanItems];
-    uint32_t sum = 0;
-    for (int k = 0; k < kScanItems; ++k) {
-        v[k] = base + k < n ? partials[base + k] : 0u;
-        sum += v[k];
-    }
-    uint32_t run = block_excl_scan(sum, warp_sums, &total);
-    for (int k = 0; k < kScanItems; ++k) {
-        if (base + k < n) partials[base + k] = run;
-        run += v[k];
+    const SegmentSpec s = specs[blockIdx.x];
+    for (int p = 0; p < passes; ++p) {
+        uint32_t *h = hist + ((size_t)blockIdx.x * kMaxSortPasses + p) * 256u;
+        const uint32_t v = h[threadIdx.x];
+        const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+        uint32_t incl = warp_incl_scan(v);
+        if (lane == 31) warp_sums[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = lane < 8 ? warp_sums[lane] : 0u;
+            uint32_t wi = warp_incl_scan(w);
+            if (lane < 8) warp_sums[lane] = wi - w;
+            if (lane == 7) total = wi;
+        }
+        __syncthreads();
+        h[threadIdx.x] = s.begin + warp_sums[warp] + incl - v;
+        __syncthreads();
     }
 }
 
-__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(uint32_t *__restrict__ data,
-                                                                  const uint32_t *__restrict__ partials, uint32_t n) {
-    __shared__ uint32_t warp_sums[32];
-    __shared__ uint32_t total;
-    const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * kScanItems;
-    uint32_t v[kScanItems];
-    uint32_t sum = 0;
-    for (int k = 0; k < kScanItems; ++k) {
-        v[k] = base + k < n ? data[base + k] : 0u;
-        sum += v[k];
-    }
-    uint32_t run = block_excl_scan(sum, warp_sums, &total) + partials[blockIdx.x];
-    for (int k = 0; k < kScanItems; ++k) {
-        if (base + k < n) data[base + k] = run;
-        run += v[k];
-    }
-}
+// Decoupled look-back words: a tile's count for one digit (kLookAgg) or its inclusive
+// prefix (kLookPrefix), with the flag in the top two bits.
+constexpr uint32_t kLookAgg = 1u << 30;
+constexpr uint32_t kLookPrefix = 2u << 30;
+constexpr uint32_t kLookValue = (1u << 30) - 1u;
+constexpr uint32_t kLookSpinLimit = 1u << 20;  // polls of one predecessor word before giving up
 
-// ------------------------------------------------------------------ stable scatter
-
-// One tile per block: 8 warps, each warp owns 256 consecutive items and walks them in 8
-// rounds of 32, so (warp, round, lane) is the item order.  Ranks within a round come
-// from __match_any_sync; per-warp running counts per digit live in shared memory; a
-// per-digit prefix over warps and the scanned global counts give each item its output
-// slot.  Items with equal digits therefore keep their input order (stable).
-__global__ void __launch_bounds__(kSortThreads) scatter_kernel(const SegmentSpec *__restrict__ specs,
-                                                               const uint32_t *__restrict__ tile_seg,
-                                                               const uint32_t *__restrict__ keys_in,
-                                                               const uint32_t *__restrict__ vals_in,
-                                                               uint32_t *__restrict__ keys_out,
-                                                               uint32_t *__restrict__ vals_out,
-                                                               const uint32_t *__restrict__ offsets, int shift,
-                                                               uint32_t mask) {
+// One radix pass as a single kernel (the "onesweep" scheme): a block takes the next tile in
+// input order from an atomic counter, ranks its 2048 keys stably (8 warps, each owning 256
+// consecutive items in 8 rounds of 32: __match_any_sync ranks and per-warp running digit
+// counts), publishes its per-digit counts, and finds its per-digit output offsets by looking
+// back over the earlier tiles of its segment (a tile's first tile starts from the segment's
+// digit offsets).  Tiles take ids in order, so every tile a block waits for is already
+// running; each wait is bounded and reports kErrSortLookback through *err when it runs out.
+__global__ void __launch_bounds__(kSortThreads) onesweep_kernel(const SegmentSpec *__restrict__ specs,
+                                                                const uint32_t *__restrict__ tile_seg,
+                                                                const uint32_t *__restrict__ keys_in,
+                                                                const uint32_t *__restrict__ vals_in,
+                                                                uint32_t *__restrict__ keys_out,
+                                                                uint32_t *__restrict__ vals_out,
+                                                                const uint32_t *__restrict__ hist,
+                                                                uint32_t *__restrict__ look, uint32_t *tile_ctr,
+                                                                uint32_t *err, int pass, uint32_t mask) {
     constexpr int kWarps = kSortThreads / 32;
     constexpr int kRounds = kSortTile / kSortThreads;
     __shared__ uint32_t warp_hist[kWarps][256];
     __shared__ uint32_t digit_base[256];
-    const uint32_t seg = tile_seg[blockIdx.x];
+    __shared__ uint32_t local_start[256];
+    __shared__ uint32_t warp_sums[kWarps];
+    __shared__ uint32_t keys_s[kSortTile], vals_s[kSortTile];
+    __shared__ uint32_t tile_hist[256];
+    __shared__ uint32_t s_tile;
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr + pass, 1u);
+    for (int i = threadIdx.x; i < kWarps * 256; i += kSortThreads) (&warp_hist[0][0])[i] = 0;
+    tile_hist[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t seg = tile_seg[tile];
     const SegmentSpec s = specs[seg];
-    const uint32_t t = blockIdx.x - s.tile_begin;
+    const uint32_t t = tile - s.tile_begin;
     const uint32_t beg = s.begin + t * kSortTile;
     const uint32_t end = min(beg + (uint32_t)kSortTile, s.begin + s.count);
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
-
-    for (int i = threadIdx.x; i < kWarps * 256; i += kSortThreads) (&warp_hist[0][0])[i] = 0;
-    digit_base[threadIdx.x] = offsets[count_index(s, threadIdx.x, t)];
-    __syncthreads();
+    const int shift = 8 * pass;
 
     uint32_t key[kRounds], val[kRounds], rank[kRounds], dig[kRounds];
+    // the tile's digit counts first, published before the ranking so that later tiles
+    // find them when they look back
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+        const uint32_t i = beg + warp * (kSortTile / kWarps) + r * 32 + lane;
+        key[r] = i < end ? keys_in[i] : 0u;
+        dig[r] = i < end ? ((key[r] >> shift) & mask) : 256u;
+        if (dig[r] < 256u) atomicAdd(&tile_hist[dig[r]], 1u);
+    }
+    __syncthreads();
+    volatile uint32_t *mine = look + ((size_t)pass * gridDim.x + tile) * 256u + threadIdx.x;
+    if (t == 0)
+        *mine = kLookPrefix | ((hist[((size_t)seg * kMaxSortPasses + pass) * 256u + threadIdx.x] + tile_hist[threadIdx.x]) &
+                               kLookValue);
+    else
+        *mine = kLookAgg | tile_hist[threadIdx.x];
 #pragma unroll
     for (int r = 0; r < kRounds; ++r) {
         const uint32_t i = beg + warp * (kSortTile / kWarps) + r * 32 + lane;
         const bool valid = i < end;
-        const uint32_t k = valid ? keys_in[i] : 0u;
-        const uint32_t d = valid ? ((k >> shift) & mask) : 256u;
+        const uint32_t k = key[r];
+        const uint32_t d = dig[r];
         const uint32_t peers = __match_any_sync(0xffffffffu, d);
         const uint32_t below = __popc(peers & ((1u << lane) - 1u));
         const uint32_t before = valid ? warp_hist[warp][d] : 0u;
@@ -317,20 +295,84 @@ __global__ void __launch_bounds__(kSortThreads) scatter_kernel(const SegmentSpec
     }
     __syncthreads();
     {
+        // per digit (one thread each): prefix over warps, the tile's count, the look-back
+        const uint32_t d = threadIdx.x;
         uint32_t run = 0;
         for (int w = 0; w < kWarps; ++w) {
-            uint32_t c = warp_hist[w][threadIdx.x];
-            warp_hist[w][threadIdx.x] = run;
+            const uint32_t c = warp_hist[w][d];
+            warp_hist[w][d] = run;
             run += c;
         }
+        uint32_t excl;
+        if (t == 0) {
+            excl = hist[((size_t)seg * kMaxSortPasses + pass) * 256u + d];
+        } else {
+            // windows of up to 8 predecessors, loaded together: add counts back to the
+            // nearest inclusive prefix; spin (bounded) only on a word not yet published
+            excl = 0;
+            uint32_t next = tile;  // predecessors still to add: [tile_begin, next)
+            bool done = false;
+            while (!done) {
+                const uint32_t n = min(8u, next - s.tile_begin);
+                uint32_t v[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    v[k] = (uint32_t)k < n ? *(const volatile uint32_t *)(look + ((size_t)pass * gridDim.x + next - 1 - k) * 256u + d)
+                                           : 0u;
+                for (uint32_t k = 0; k < n && !done; ++k) {
+                    const volatile uint32_t *w = look + ((size_t)pass * gridDim.x + next - 1 - k) * 256u + d;
+                    uint32_t x = v[k];
+                    for (uint32_t spin = 0; (x >> 30) == 0u; ++spin) {
+                        if (spin == kLookSpinLimit) {
+                            atomicOr(err, kErrSortLookback);
+                            break;
+                        }
+                        __nanosleep(32);
+                        x = *w;
+                    }
+                    excl += x & kLookValue;
+                    if ((x >> 30) != 1u) done = true;  // an inclusive prefix (or a wait that ran out)
+                }
+                next -= n;
+                if (!done && next == s.tile_begin) {
+                    // only counts down to the segment's first tile: start from its digit offsets
+                    excl += hist[((size_t)seg * kMaxSortPasses + pass) * 256u + d];
+                    done = true;
+                }
+            }
+            *mine = kLookPrefix | ((excl + run) & kLookValue);
+        }
+        digit_base[d] = excl;
+        // the tile's own digit-sorted layout: exclusive scan of its digit counts
+        const uint32_t incl = warp_incl_scan(run);
+        if (lane == 31) warp_sums[warp] = incl;
+        __syncthreads();
+        uint32_t before = 0;
+        for (uint32_t w = 0; w < warp; ++w) before += warp_sums[w];
+        local_start[d] = before + incl - run;
     }
     __syncthreads();
+    // stage the tile in digit order, then write runs of equal digits to consecutive
+    // global slots (coalesced), not one sector per key
 #pragma unroll
     for (int r = 0; r < kRounds; ++r) {
         if (dig[r] < 256u) {
-            const uint32_t p = digit_base[dig[r]] + warp_hist[warp][dig[r]] + rank[r];
-            keys_out[p] = key[r];
-            vals_out[p] = val[r];
+            const uint32_t j = local_start[dig[r]] + warp_hist[warp][dig[r]] + rank[r];
+            keys_s[j] = key[r];
+            vals_s[j] = val[r];
+        }
+    }
+    __syncthreads();
+    const uint32_t count = end - beg;
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+        const uint32_t j = (uint32_t)r * kSortThreads + threadIdx.x;
+        if (j < count) {
+            const uint32_t k = keys_s[j];
+            const uint32_t dd = (k >> shift) & mask;
+            const uint32_t p = digit_base[dd] + (j - local_start[dd]);
+            keys_out[p] = k;
+            vals_out[p] = vals_s[j];
         }
     }
 }
@@ -451,32 +493,26 @@ void launch_box(const SortLaunch &L, cudaStream_t st) {
     bbox_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.pos, L.pos_max, L.box);
 }
 
-static void launch_scan(const SortLaunch &L, cudaStream_t st) {
-    const uint32_t n = 256u * L.tiles;
-    const uint32_t blocks = (n + kScanChunk - 1) / kScanChunk;
-    scan_reduce_kernel<<<blocks, kScanThreads, 0, st>>>(L.counts, L.partials, n);
-    scan_spine_kernel<<<1, kScanThreads, 0, st>>>(L.partials, blocks);
-    scan_apply_kernel<<<blocks, kScanThreads, 0, st>>>(L.counts, L.partials, n);
-}
-
 // Sorts the keys of every segment; on return *sorted_keys / *perm point at the buffers
 // holding the sorted keys and the permutation (sorted slot -> previous slot).
 void launch_sort(const SortLaunch &L, cudaStream_t st, uint32_t **sorted_keys, uint32_t **perm) {
     uint32_t *kin = L.keys[0], *kout = L.keys[1];
     uint32_t *vin = nullptr, *vout = L.vals[1];
-    const int passes = (int)((L.key_bits + 7) / 8);
+    const int passes = sort_passes(L.key_bits);
+    // zero the histograms, the tile counters and the look-back words of the passes used
+    cudaMemsetAsync(L.sort_scratch, 0,
+                    sizeof(uint32_t) * ((size_t)L.segments * kMaxSortPasses * 256u + kMaxSortPasses +
+                                        (size_t)passes * L.tiles * 256u),
+                    st);
+    uint32_t *hist = L.sort_scratch;
+    uint32_t *tile_ctr = hist + (size_t)L.segments * kMaxSortPasses * 256u;
+    uint32_t *look = tile_ctr + kMaxSortPasses;
+    keys_hist_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.box, L.pos, kin, hist, passes, L.key_bits);
+    digit_offsets_kernel<<<L.segments, 256, 0, st>>>(L.specs, hist, passes);
     for (int p = 0; p < passes; ++p) {
-        const int shift = 8 * p;
-        const int bits = min(8, (int)L.key_bits - shift);
-        const uint32_t mask = (1u << bits) - 1u;
-        if (p == 0)
-            key_histogram_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.box, L.pos, kin, L.counts,
-                                                                   mask);
-        else
-            digit_histogram_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, kin, L.counts, shift, mask);
-        launch_scan(L, st);
-        scatter_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, kin, vin, kout, vout, L.counts, shift,
-                                                         mask);
+        const int bits = std::min(8, (int)L.key_bits - 8 * p);
+        onesweep_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, kin, vin, kout, vout, hist, look,
+                                                          tile_ctr, L.err, p, (1u << bits) - 1u);
         // ping-pong: the next pass reads what this one wrote
         uint32_t *tk = kin;
         kin = kout;

@@ -246,6 +246,7 @@ TGPU_HD Grid segment_grid(const SegmentSpec &s, const BoxAcc &b) {
 enum DeviceError : uint32_t {
     kErrNone = 0,
     kErrTableOverflow = 1,
+    kErrSortLookback = 2,  // a radix pass's look-back wait ran out (a tile never published)
 };
 
 }  // namespace tgpu

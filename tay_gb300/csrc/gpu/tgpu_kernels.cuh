@@ -14,8 +14,9 @@ struct SortLaunch {
     const float4 *pos_max;     // non-point agents: max corners, current order (else null)
     uint32_t *keys[2];         // [n] ping-pong key buffers
     uint32_t *vals[2];         // [n] ping-pong permutation buffers
-    uint32_t *counts;          // [256 * tiles]
-    uint32_t *partials;        // [ceil(256 * tiles / 4096)]
+    uint32_t *sort_scratch;    // sort_scratch_bytes(segments, tiles): digit histograms, tile
+                               // counters and look-back words, zeroed by every sort
+    uint32_t *err;             // device error word (DeviceError bits)
     uint2 *table;              // dense cell tables of all segments
     uint32_t segments;
     uint32_t tiles;
@@ -80,6 +81,17 @@ struct ActLaunch {
 };
 
 void launch_box(const SortLaunch &L, cudaStream_t st);
+constexpr int kMaxSortPasses = 4;  // 32-bit keys in 8-bit digits
+
+constexpr int sort_passes(uint32_t key_bits) { return (int)((key_bits + 7u) / 8u); }
+
+// Bytes of the sort's scratch: per-segment histograms of every digit, one tile counter per
+// pass, and the look-back words of every (pass, tile, digit).
+constexpr size_t sort_scratch_bytes(uint32_t segments, uint32_t tiles) {
+    return sizeof(uint32_t) * ((size_t)segments * kMaxSortPasses * 256u + kMaxSortPasses +
+                               (size_t)kMaxSortPasses * tiles * 256u);
+}
+
 // Bounding box of n positions into *out (reset first), for the pushed extent.
 void launch_extent(const float4 *pos, uint32_t n, BoxAcc *out, cudaStream_t st);
 void launch_sort(const SortLaunch &L, cudaStream_t st, uint32_t **sorted_keys, uint32_t **perm);
