@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--union-factor", type=int, default=None, help="see kernel: union walk threshold")
     ap.add_argument("--cell-order", type=int, default=None, help="0 = Morton cells, 1 = x-rows")
     ap.add_argument("--hit-masks", type=int, default=None, help="1 = see walk with hit masks (cell order 1)")
+    ap.add_argument("--x-cell-factor", type=float, default=None, help="cell order 1: x cell / y,z cell")
     ap.add_argument("--cell-multiple", type=float, default=None, help="grid cell edge / min part size")
     return ap.parse_args()
 
@@ -362,7 +363,7 @@ def run_gb300(args, rank, world, D):
     api.set_tuning()  # library defaults, then the autotuner's choice or command-line overrides
     over = {k: v for k, v in (("stage", args.stage), ("union_factor", args.union_factor),
                               ("cell_multiple", args.cell_multiple), ("cell_order", args.cell_order),
-                              ("hit_masks", args.hit_masks)) if v is not None}
+                              ("hit_masks", args.hit_masks), ("x_cell_factor", args.x_cell_factor)) if v is not None}
     tuned = None
     if over:
         api.set_tuning(**over)
@@ -475,7 +476,7 @@ def run_gb300(args, rank, world, D):
             line["sph"] = sph_leg(min(args.steps, 20), not args.no_autotune)
         if args.adjoint:
             tune = not args.no_autotune
-            line["adjoint"] = adjoint_leg(keep=3, tune=tune)
+            line["adjoint"] = adjoint_leg(keep=4, tune=tune)
             line["adjoint_keep1"] = adjoint_leg(keep=1, tune=tune)
             line["adjoint_record_all"] = adjoint_leg(every=0, tune=tune)
         if not args.no_cpu_baseline and world == 1:

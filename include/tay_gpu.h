@@ -162,7 +162,9 @@ int tgpu_batch_program(const TgpuBatch *batch);
  *                  1: x-rows (x fastest inside (y, z) rows, rows in 2-D Morton order),
  *                  a seer's box is one candidate range per row (no staging)
  *   hit_masks      cell order 1: each lane box-tests up to 32 candidates into a mask
- *                  before the lanes run the see function over their hits together */
+ *                  before the lanes run the see function over their hits together
+ *   x_cell_factor  cell order 1: x cells are this fraction of the y / z cells (finer x
+ *                  cells tighten each row's candidate range without adding rows) */
 typedef struct TgpuTuning {
     int stage;
     unsigned stage_cap;
@@ -172,6 +174,7 @@ typedef struct TgpuTuning {
     int use_graphs;
     unsigned cell_order;
     unsigned hit_masks;
+    float x_cell_factor;
 } TgpuTuning;
 
 void tgpu_set_tuning(const TgpuTuning *tuning);  /* NULL restores the defaults */

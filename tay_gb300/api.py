@@ -362,7 +362,7 @@ def run_batch(states, steps):
 class TgpuTuning(ctypes.Structure):
     _fields_ = [("stage", ctypes.c_int), ("stage_cap", ctypes.c_uint), ("stage_cells", ctypes.c_uint),
                 ("cell_multiple", ctypes.c_float), ("union_factor", ctypes.c_uint), ("use_graphs", ctypes.c_int),
-                ("cell_order", ctypes.c_uint), ("hit_masks", ctypes.c_uint)]
+                ("cell_order", ctypes.c_uint), ("hit_masks", ctypes.c_uint), ("x_cell_factor", ctypes.c_float)]
 
 
 def get_tuning() -> dict:
@@ -373,11 +373,11 @@ def get_tuning() -> dict:
 
 def set_tuning(**kw):
     """Sets tuning fields (stage, stage_cap, stage_cells, cell_multiple, union_factor,
-    use_graphs, cell_order, hit_masks) for batches created afterwards; no arguments restores the defaults."""
+    use_graphs, cell_order, hit_masks, x_cell_factor) for batches created afterwards; no arguments restores the defaults."""
     if not kw:
         lib().tgpu_set_tuning(None)
         return
     cur = get_tuning()
     cur.update(kw)
-    t = TgpuTuning(**{k: (int(v) if k != "cell_multiple" else float(v)) for k, v in cur.items()})
+    t = TgpuTuning(**{k: (float(v) if k in ("cell_multiple", "x_cell_factor") else int(v)) for k, v in cur.items()})
     lib().tgpu_set_tuning(ctypes.byref(t))

@@ -1,8 +1,9 @@
 """Autotuner for the Z-grid engine's knobs.
 
 Picks, by measurement on the GPU, the grid cell-size multiple (cell edge relative to the
-configured minimum part size), the cell order (3-D Morton cells or x-rows), the warp
-walk (union walk threshold) and whether see CTAs stage their halos in shared memory.  Each candidate runs a few steps on a throwaway batch
+configured minimum part size), the cell order (3-D Morton cells or x-rows) with the x cell
+factor of row order, the warp walk (union walk threshold) and whether see CTAs stage their
+halos in shared memory.  Each candidate runs a few steps on a throwaway batch
 built from the same groups (the caller's state is not advanced); the fastest candidate is
 set as the library's tuning and cached per shape class (model, pass sequence, agent-count
 bucket, segment-count bucket, radius / part-size ratio) in a JSON file, so later runs of the
@@ -17,18 +18,14 @@ import os
 
 from . import api
 
-DEFAULT_CANDIDATES = [
-    {"cell_multiple": 1.0, "union_factor": 1, "stage": 0, "cell_order": 0},
-    {"cell_multiple": 0.5, "union_factor": 1, "stage": 0, "cell_order": 0},
-    {"cell_multiple": 0.75, "union_factor": 1, "stage": 0, "cell_order": 0},
-    {"cell_multiple": 1.5, "union_factor": 1, "stage": 0, "cell_order": 0},
-    {"cell_multiple": 1.0, "union_factor": 1, "stage": 0, "cell_order": 1},
-    {"cell_multiple": 0.5, "union_factor": 1, "stage": 0, "cell_order": 1},
-    {"cell_multiple": 0.75, "union_factor": 1, "stage": 0, "cell_order": 1},
-    {"cell_multiple": 0.34, "union_factor": 1, "stage": 0, "cell_order": 1},
-    {"cell_multiple": 1.0, "union_factor": 2, "stage": 0, "cell_order": 0},
-    {"cell_multiple": 1.0, "union_factor": 2, "stage": 1, "cell_order": 0},
-]
+DEFAULT_CANDIDATES = (
+    [{"cell_multiple": cm, "union_factor": 1, "stage": 0, "cell_order": 0, "x_cell_factor": 1.0}
+     for cm in (1.0, 0.5)]
+    + [{"cell_multiple": cm, "union_factor": 1, "stage": 0, "cell_order": 1, "x_cell_factor": xf}
+       for cm in (1.0, 0.5, 0.34, 0.25) for xf in (1.0, 0.5, 0.25)]
+    + [{"cell_multiple": 1.0, "union_factor": 2, "stage": 0, "cell_order": 0, "x_cell_factor": 1.0},
+       {"cell_multiple": 1.0, "union_factor": 2, "stage": 1, "cell_order": 0, "x_cell_factor": 1.0}]
+)
 
 
 def cache_path() -> str:

@@ -55,6 +55,7 @@ TgpuTuning default_tuning() {
     t.use_graphs = 1;
     t.cell_order = 0;
     t.hit_masks = 0;
+    t.x_cell_factor = 1.0f;
     return t;
 }
 TgpuTuning g_tuning = default_tuning();
@@ -206,39 +207,42 @@ int tgpu::prepare_specs(TgpuBatch *b) {
     b->specs_dirty = false;
     std::vector<SegmentSpec> next = b->specs;
     uint64_t table_total = 0;
-    uint32_t max_axis = 2;
+    uint32_t max_key_bits = 3;
     for (int s = 0; s < b->nseg; ++s) {
         SegmentSpec &sp = next[s];
         const HostSeg &h = b->hs[s];
-        uint32_t axis = 2;
+        uint32_t want[3] = {2, 2, 2};
         for (int a = 0; a < seg_dims(sp); ++a) {
             float lo = h.g.box_fixed ? h.g.box_min[a] : h.host_min[a];
             float hi = h.g.box_fixed ? h.g.box_max[a] : h.host_max[a];
             float ext = hi > lo ? hi - lo : 0.0f;
             double cells = floor((double)ext / (double)sp.part[a]) + 1.0;
-            uint32_t want = (uint32_t)std::min(1024.0, std::max(2.0, ceil(cells * 1.1)));
-            axis = std::max(axis, next_pow2(want));
+            want[a] = std::min(1024u, next_pow2((uint32_t)std::min(1024.0, std::max(2.0, ceil(cells * 1.1)))));
         }
-        axis = std::min(axis, 1024u);
+        // Morton order: one bound for all axes; row order: x and (y, z) bounded separately
+        const uint32_t ayz = std::max(want[1], want[2]);
+        const uint32_t axis = b->cell_order == kOrderRows ? want[0] : std::max(want[0], ayz);
         sp.axis_cells_max = axis;
+        sp.axis_cells_yz = b->cell_order == kOrderRows ? ayz : axis;
+        const uint32_t seg_key_bits = log2u(axis) + 2 * log2u(sp.axis_cells_yz);
         uint64_t cap_mem = ((uint64_t)std::max(h.g.shared_megabytes, 1) << 20) / sizeof(uint2);
-        uint64_t cap_axis = (uint64_t)axis * axis * axis;
+        uint64_t cap_axis = (uint64_t)axis * sp.axis_cells_yz * sp.axis_cells_yz;
         uint64_t cap = std::min(cap_mem, cap_axis);
         cap = std::max<uint64_t>(cap, 8);
         cap = std::min<uint64_t>(cap, 0x7FFFFFFEull);
         cap = (cap + 1) & ~1ull;  // even: every segment's table starts 16-byte aligned (row headers)
         // row order: headers for up to axis^2 rows, at most a quarter of the table
         sp.row_cap = b->cell_order == kOrderRows
-                         ? (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)axis * axis, cap / 4))
+                         ? (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)ayz * ayz, cap / 4))
                          : 0u;
         sp.table_base = (uint32_t)table_total;
         sp.table_cap = (uint32_t)cap;
         table_total += cap;
-        max_axis = std::max(max_axis, axis);
+        max_key_bits = std::max(max_key_bits, seg_key_bits);
     }
     if (table_total > 0xFFFFFFFFull)
         return fail(TGPU_ERR_ARG, "cell tables too large (%llu entries)", (unsigned long long)table_total);
-    const uint32_t key_bits = 3 * log2u(max_axis);
+    const uint32_t key_bits = max_key_bits;
     const bool same = b->table && key_bits == b->key_bits &&
                       !memcmp(next.data(), b->specs.data(), sizeof(SegmentSpec) * b->nseg);
     if (same) return TGPU_OK;  // the table is left clean by every completed step
@@ -540,6 +544,7 @@ int tgpu_device_count(void) {
 void tgpu_set_tuning(const TgpuTuning *t) {
     g_tuning = t ? *t : default_tuning();
     if (!(g_tuning.cell_multiple > 0.0f)) g_tuning.cell_multiple = 1.0f;
+    if (!(g_tuning.x_cell_factor > 0.0f)) g_tuning.x_cell_factor = 1.0f;
     if (!g_tuning.union_factor) g_tuning.union_factor = 1;
 }
 
@@ -596,6 +601,8 @@ int add_segments(TgpuBatch *b, const TgpuGroup *groups, int group_count, const s
         for (int a = 0; a < 3; ++a) {
             float part = g.min_part_sizes[a] > 0.0f ? g.min_part_sizes[a] : 1.0f;
             sp.part[a] = part * g_tuning.cell_multiple;
+            // row order: x cells only tighten each row's range, so they may be finer
+            if (a == 0 && b->cell_order == kOrderRows) sp.part[a] *= g_tuning.x_cell_factor;
             sp.box_min[a] = g.box_min[a];
             sp.box_max[a] = g.box_max[a];
             sp.reach[a] = reach[s][a];

@@ -42,6 +42,7 @@ struct SegmentSpec {
     uint32_t order;          // cell order of the keys and table layout: kOrderMorton / kOrderRows
     uint32_t dims;           // tay_configure_space dims (1..3; 0 means 3): axes >= dims get one cell
     uint32_t row_cap;        // row order: (y, z) rows the table's header region holds
+    uint32_t axis_cells_yz;  // row order: power-of-two bound of the y and z axes (x: axis_cells_max)
     float part[3];           // minimum cell edge per axis
     float reach[3];          // largest see radius per axis over the segment's see passes
     float box_min[3];        // fixed space box (tay_fix_space_box)
@@ -127,6 +128,12 @@ TGPU_HD bool table_fits(const SegmentSpec &s, const int *d) {
     return rows <= s.row_cap && 4ull * s.row_cap + cells <= 2ull * s.table_cap;
 }
 
+// Cell budget of axis i: in row order the x axis (whose cells only tighten each row's
+// candidate range) and the y / z axes (whose cells make the rows) have their own bounds.
+TGPU_HD uint32_t axis_max(const SegmentSpec &s, int i) {
+    return (i > 0 && s.order == kOrderRows && s.axis_cells_yz) ? s.axis_cells_yz : s.axis_cells_max;
+}
+
 TGPU_HD Grid derive_grid(const SegmentSpec &s, const float *mn, const float *mx) {
     Grid g;
     float cs[3], ext[3];
@@ -136,8 +143,8 @@ TGPU_HD Grid derive_grid(const SegmentSpec &s, const float *mn, const float *mx)
         if (!(ext[i] >= 0.0f) || ext[i] > 3.0e38f) ext[i] = 0.0f;
         cs[i] = s.part[i] > 0.0f ? s.part[i] : 1.0f;
         float cells = floorf(ext[i] / cs[i]) + 1.0f;
-        if (cells > (float)s.axis_cells_max) cs[i] = ext[i] / ((float)s.axis_cells_max - 0.5f);
-        d[i] = clamp_cells(floorf(ext[i] / cs[i]) + 1.0f, s.axis_cells_max);
+        if (cells > (float)axis_max(s, i)) cs[i] = ext[i] / ((float)axis_max(s, i) - 0.5f);
+        d[i] = clamp_cells(floorf(ext[i] / cs[i]) + 1.0f, axis_max(s, i));
         if (i >= seg_dims(s)) {
             // an axis the space does not have: one cell spanning it
             d[i] = 1;
@@ -148,7 +155,7 @@ TGPU_HD Grid derive_grid(const SegmentSpec &s, const float *mn, const float *mx)
         if (table_fits(s, d)) break;
         for (int i = 0; i < seg_dims(s); ++i) {
             cs[i] *= 1.25f;
-            d[i] = clamp_cells(floorf(ext[i] / cs[i]) + 1.0f, s.axis_cells_max);
+            d[i] = clamp_cells(floorf(ext[i] / cs[i]) + 1.0f, axis_max(s, i));
         }
     }
     if (!table_fits(s, d)) {

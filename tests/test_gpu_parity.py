@@ -110,6 +110,7 @@ def test_batch_matches_individual_runs(gpu):
 @pytest.mark.parametrize("tuning", [
     {"cell_order": 1}, {"cell_order": 1, "cell_multiple": 0.34}, {"cell_order": 1, "union_factor": 2},
     {"cell_order": 1, "hit_masks": 1}, {"cell_order": 1, "hit_masks": 1, "cell_multiple": 0.5},
+    {"cell_order": 1, "x_cell_factor": 0.25}, {"cell_order": 1, "cell_multiple": 0.5, "x_cell_factor": 0.5},
     {"union_factor": 2}, {"stage": 1}, {"cell_multiple": 0.5}, {"cell_multiple": 1.5},
 ])
 def test_walk_tunings_match_oracle(gpu, port, tuning):
