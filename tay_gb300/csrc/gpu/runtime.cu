@@ -172,6 +172,18 @@ int tgpu::check_device_error(TgpuBatch *b) {
 
 namespace {
 
+// Device address of page-locked host memory (the kernels then read or write the records
+// in place, one pass over the host link instead of a copy plus a pass), or nullptr for
+// pageable memory, which goes through the device staging buffer.
+void *pinned_device_ptr(const void *host) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int upload_contexts(TgpuBatch *b, int seg) {
     std::vector<char> buf(b->ctx_stride);
     const HostSeg &h = b->hs[seg];
@@ -887,8 +899,11 @@ int tgpu_batch_push(TgpuBatch *b, int group, const void *host) {
         for (int a = 0; a < 3; ++a) h.host_min[a] = h.host_max[a] = 0.0f;
         return TGPU_OK;
     }
-    uint32_t *aos = b->d_aos + (size_t)sp.begin * (b->m->agent_bytes / 4);
-    CK(cudaMemcpyAsync(aos, host, (size_t)n * b->m->agent_bytes, cudaMemcpyHostToDevice, b->st));
+    uint32_t *aos = static_cast<uint32_t *>(pinned_device_ptr(host));
+    if (!aos) {
+        aos = b->d_aos + (size_t)sp.begin * (b->m->agent_bytes / 4);
+        CK(cudaMemcpyAsync(aos, host, (size_t)n * b->m->agent_bytes, cudaMemcpyHostToDevice, b->st));
+    }
     // pack into the current buffers of every stream
     PassIO io{};
     for (int c = 0; c < b->m->nf4; ++c) {
@@ -971,7 +986,8 @@ int tgpu_batch_fetch(TgpuBatch *b, int group, void *host) {
     if (!b || group < 0 || group >= b->nseg || !host) return fail(TGPU_ERR_ARG, "bad fetch");
     const SegmentSpec &sp = b->specs[group];
     if (!sp.count) return TGPU_OK;
-    uint32_t *aos = b->d_aos + (size_t)sp.begin * (b->m->agent_bytes / 4);
+    uint32_t *pinned = static_cast<uint32_t *>(pinned_device_ptr(host));
+    uint32_t *aos = pinned ? pinned : b->d_aos + (size_t)sp.begin * (b->m->agent_bytes / 4);
     PassIO io = make_io(b, nullptr, false, sp.begin);
     // state batches: accumulators are visible when no act pass consumed them
     uint32_t program = (uint32_t)b->program;
@@ -982,7 +998,8 @@ int tgpu_batch_fetch(TgpuBatch *b, int group, void *host) {
     }
     b->m->unpack(aos, sp.count, io, program, b->st);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(host, aos, (size_t)sp.count * b->m->agent_bytes, cudaMemcpyDeviceToHost, b->st));
+    if (!pinned)
+        CK(cudaMemcpyAsync(host, aos, (size_t)sp.count * b->m->agent_bytes, cudaMemcpyDeviceToHost, b->st));
     CK(cudaStreamSynchronize(b->st));
     return TGPU_OK;
 }

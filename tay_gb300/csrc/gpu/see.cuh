@@ -584,16 +584,49 @@ __global__ void __launch_bounds__(kSortThreads) act_kernel(ActLaunch L) {
 // AoS <-> SoA conversion for push and fetch (replaces the OpenCL path's whole-buffer
 // copies, tay/ocl.c:238-272).  `aos` is the record array in device memory.
 template <class M>
+// AoS records <-> SoA streams, 256 records per block staged in shared memory, so the
+// records are read (pack) or written (unpack) as one contiguous run of words per block:
+// coalesced in device memory, and large requests when `aos` is page-locked host memory
+// the kernel reads or writes in place (no separate copy).
 __global__ void __launch_bounds__(256) pack_kernel(const uint32_t *__restrict__ aos, uint32_t n, PassIO io) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) M::pack(aos + (size_t)i * (M::kAgentBytes / 4), io, i);
+    constexpr uint32_t W = M::kAgentBytes / 4;
+    __shared__ __align__(16) uint32_t sm[256 * W];
+    const uint32_t first = blockIdx.x * 256u;
+    const uint32_t cnt = min(256u, n - first);
+    const uint32_t *src = aos + (size_t)first * W;
+    const uint32_t words = cnt * W;
+    uint32_t w0 = 0;
+    if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+        // 16-byte loads for the aligned bulk, words for the tail
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+        uint4 *d4 = reinterpret_cast<uint4 *>(sm);
+        for (uint32_t v = threadIdx.x; v < words / 4u; v += 256u) d4[v] = s4[v];
+        w0 = words & ~3u;
+    }
+    for (uint32_t w = w0 + threadIdx.x; w < words; w += 256u) sm[w] = src[w];
+    __syncthreads();
+    if (threadIdx.x < cnt) M::pack(sm + threadIdx.x * W, io, first + threadIdx.x);
 }
 
 template <class M>
 __global__ void __launch_bounds__(256) unpack_kernel(uint32_t *__restrict__ aos, uint32_t n, PassIO io,
                                                      uint32_t program) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) M::unpack(aos + (size_t)i * (M::kAgentBytes / 4), io, i, program);
+    constexpr uint32_t W = M::kAgentBytes / 4;
+    __shared__ __align__(16) uint32_t sm[256 * W];
+    const uint32_t first = blockIdx.x * 256u;
+    const uint32_t cnt = min(256u, n - first);
+    if (threadIdx.x < cnt) M::unpack(sm + threadIdx.x * W, io, first + threadIdx.x, program);
+    __syncthreads();
+    uint32_t *dst = aos + (size_t)first * W;
+    const uint32_t words = cnt * W;
+    uint32_t w0 = 0;
+    if ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(sm);
+        uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+        for (uint32_t v = threadIdx.x; v < words / 4u; v += 256u) d4[v] = s4[v];
+        w0 = words & ~3u;
+    }
+    for (uint32_t w = w0 + threadIdx.x; w < words; w += 256u) dst[w] = sm[w];
 }
 
 }  // namespace tgpu
