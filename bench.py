@@ -368,7 +368,7 @@ def run_gb300(args, rank, world, D):
     if over:
         api.set_tuning(**over)
     elif not args.no_autotune:
-        tuned = autotune.autotune([(setup, recs)], use_cache=False)
+        tuned = autotune.autotune([(setup, recs)], use_cache=False, evolve_steps=args.warmup + args.steps)
     B = api.Batch([(setup, recs)])
     B.push()
     for _ in range(args.warmup):
