@@ -87,6 +87,13 @@ int tgpu_state_create(const TgpuGroup *groups, int group_count, const TgpuStateP
 /* Copies the contexts and radii of a state's passes again (same order as at create). */
 int tgpu_state_set_contexts(TgpuBatch *batch, const TgpuStatePass *passes, int pass_count);
 
+/* Failure-path self-test of the radix sort's bounded waits: runs one tile of a radix pass
+ * whose predecessor never publishes its counts, so its look-back waits run out (each in
+ * well under a second) and the kernel returns after recording the failure.  Stores the
+ * device error word it read back (2 = look-back wait ran out) and returns TGPU_OK, or
+ * TGPU_ERR_CUDA.  The context stays usable. */
+int tgpu_selftest_sort_wait(unsigned *device_error);
+
 /* 1 when the device model providing `func_name` holds non-point (box) agents, 0 when it
  * holds point agents, -1 when no model provides it. */
 int tgpu_model_nonpoint(const char *func_name);

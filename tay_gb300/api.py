@@ -82,6 +82,7 @@ TGPU_SYMBOLS = [
     ("tgpu_state_create", ctypes.c_int, [_VP, ctypes.c_int, _VP, ctypes.c_int, ctypes.POINTER(_VP)]),
     ("tgpu_state_set_contexts", ctypes.c_int, [_VP, _VP, ctypes.c_int]),
     ("tgpu_model_nonpoint", ctypes.c_int, [ctypes.c_char_p]),
+    ("tgpu_selftest_sort_wait", ctypes.c_int, [ctypes.POINTER(ctypes.c_uint)]),
     ("tgpu_batch_set_contexts", ctypes.c_int, [_VP, ctypes.c_int, _VP]),
     ("tgpu_batch_push", ctypes.c_int, [_VP, ctypes.c_int, _VP]),
     ("tgpu_batch_run", ctypes.c_int, [_VP, ctypes.c_int]),

@@ -569,6 +569,15 @@ const char *tgpu_model_of(const char *func_name) {
     return m ? m->name : nullptr;
 }
 
+int tgpu_selftest_sort_wait(unsigned *device_error) {
+    if (!device_error) return fail(TGPU_ERR_ARG, "null output");
+    uint32_t err = 0;
+    cudaError_t e = selftest_sort_wait(&err);
+    if (e != cudaSuccess) return fail(TGPU_ERR_CUDA, "sort wait self-test: %s", cudaGetErrorString(e));
+    *device_error = err;
+    return TGPU_OK;
+}
+
 int tgpu_model_nonpoint(const char *func_name) {
     const ModelDesc *m = func_name ? find_model(func_name) : nullptr;
     return m ? (m->nonpoint ? 1 : 0) : -1;

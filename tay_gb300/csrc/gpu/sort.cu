@@ -530,6 +530,58 @@ void launch_sort(const SortLaunch &L, cudaStream_t st, uint32_t **sorted_keys, u
     *perm = vin;
 }
 
+// Self-test of the look-back's bounded wait: one block takes tile 1 of a two-tile segment
+// whose tile 0 never publishes, so every digit's wait runs out (each after kLookSpinLimit
+// polls, well under a second) and the kernel reports kErrSortLookback in *err and returns.
+// All accesses stay inside the buffers given (2 tiles of keys, values and look-back words).
+cudaError_t selftest_sort_wait(uint32_t *err_host) {
+    SegmentSpec spec{};
+    spec.begin = 0;
+    spec.count = 2u * kSortTile;
+    spec.tile_begin = 0;
+    spec.tile_count = 2;
+    const uint32_t tile_seg[2] = {0u, 0u};
+    const size_t hist_words = (size_t)kMaxSortPasses * 256u;
+    SegmentSpec *d_spec = nullptr;
+    uint32_t *d_tile_seg = nullptr, *d_keys = nullptr, *d_out = nullptr, *d_hist = nullptr, *d_look = nullptr,
+             *d_ctr = nullptr, *d_err = nullptr;
+    cudaError_t e = cudaMalloc(&d_spec, sizeof(spec));
+    if (e == cudaSuccess) e = cudaMalloc(&d_tile_seg, sizeof(tile_seg));
+    if (e == cudaSuccess) e = cudaMalloc(&d_keys, sizeof(uint32_t) * 2 * kSortTile);
+    if (e == cudaSuccess) e = cudaMalloc(&d_out, sizeof(uint32_t) * 4 * kSortTile);
+    if (e == cudaSuccess) e = cudaMalloc(&d_hist, sizeof(uint32_t) * hist_words);
+    if (e == cudaSuccess) e = cudaMalloc(&d_look, sizeof(uint32_t) * 2 * 256u);
+    if (e == cudaSuccess) e = cudaMalloc(&d_ctr, sizeof(uint32_t) * kMaxSortPasses);
+    if (e == cudaSuccess) e = cudaMalloc(&d_err, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemcpy(d_spec, &spec, sizeof(spec), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_tile_seg, tile_seg, sizeof(tile_seg), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(d_keys, 0, sizeof(uint32_t) * 2 * kSortTile);
+    if (e == cudaSuccess) e = cudaMemset(d_hist, 0, sizeof(uint32_t) * hist_words);
+    if (e == cudaSuccess) e = cudaMemset(d_look, 0, sizeof(uint32_t) * 2 * 256u);
+    if (e == cudaSuccess) e = cudaMemset(d_err, 0, sizeof(uint32_t));
+    // the tile counter starts at 1: the single block is tile 1 and waits for tile 0
+    const uint32_t ctr[kMaxSortPasses] = {1u, 0u, 0u, 0u};
+    if (e == cudaSuccess) e = cudaMemcpy(d_ctr, ctr, sizeof(ctr), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        // gridDim.x = 1 but tile = 1: the look-back words of tile t sit at t * 256 (two
+        // tiles' worth allocated), keys and values out of tile 1 land in [0, 2 * kSortTile)
+        onesweep_kernel<<<1, kSortThreads>>>(d_spec, d_tile_seg, d_keys, nullptr, d_out, d_out + 2 * kSortTile, d_hist,
+                                             d_look, d_ctr, d_err, 0, 0xFFu);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(err_host, d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaFree(d_spec);
+    cudaFree(d_tile_seg);
+    cudaFree(d_keys);
+    cudaFree(d_out);
+    cudaFree(d_hist);
+    cudaFree(d_look);
+    cudaFree(d_ctr);
+    cudaFree(d_err);
+    return e;
+}
+
 void launch_cell_table(const SortLaunch &L, const uint32_t *sorted_keys, int write_runs, cudaStream_t st) {
     cell_table_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.box, sorted_keys, L.table, write_runs);
 }
