@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batched-states", type=int, default=512, help="states of the batched leg (0 = skip)")
     ap.add_argument("--sph", type=int, default=1, help="1 = add the 524,288-particle SPH leg")
+    ap.add_argument("--features", type=int, default=1, help="1 = add the two-group / resident / dims-2 / box legs")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--adjoint", type=int, default=1, help="1 = add the differentiable SPH leg")
     ap.add_argument("--stage", type=int, default=None, help="see kernel: 1 = stage halos in shared memory")
@@ -319,6 +320,110 @@ def adjoint_leg(steps=200, every=20, instances=32, keep=1, tune=True):
             "dloss_dalpha_mean": float(dp[:, 0].mean()), "dloss_dc0_mean": float(dp[:, 1].mean())}
 
 
+def features_leg(setup, recs, steps=20):
+    """The hot path's other shapes (the rows after the headline), each timed through the C
+    API: a two-group state with the combination test's passes, the device-resident loop
+    (tay_run(state, 1) with no host copies) beside the e2e loop, a 2-D space, a fixed space
+    box, and non-point (box) agents.  Device time per step from the engine's events."""
+    import time
+
+    from tay_gb300 import api
+    from tay_gb300 import models as M
+    from tay_gb300 import workloads as W
+
+    out = {}
+    see, act = M.test_contexts(radius=10.0, hi=500.0)
+
+    # two groups of 262,144, see a->a, a->b, b->b, b->a, act a, act b (test/test_combo.c)
+    st = api.State()
+    gs = []
+    for k in range(2):
+        ps = W.basic_points(1 << 18, seed=300 + k, side=500.0)
+        g = st.add_group(M.TEST_RECORD.itemsize, 1 << 18, True)
+        st.configure_space(g, api.TAY_GPU_Z_GRID, 3, 10.0, 64)
+        st.commit(g, M.records(M.TEST_RECORD, ps.p, ps.v))
+        gs.append(g)
+    for a, b in ((0, 0), (0, 1), (1, 1), (1, 0)):
+        st.add_see(gs[a], gs[b], "agent_see", 10.0, False, see)
+    for a in (0, 1):
+        st.add_act(gs[a], "agent_act", act)
+    st.start()
+    st.run(3)
+    st.run(steps)
+    dev = st.L.tay_get_device_ms_for_last_run(st.ptr) / steps
+    pairs = st.pairs() / steps
+    out["two_groups"] = {"agents": 2 << 18, "passes": "4 see + 2 act", "ms_per_step": dev,
+                         "pair_interactions_per_s": pairs / (dev / 1000.0), "pairs_per_step": pairs}
+    st.end()
+    st.close()
+
+    # device-resident loop vs the loop that copies the records both ways every step
+    st, g = M.make_state(setup, recs)
+    st.start()
+    st.run(3)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        st.run(1)
+    resident = 1000.0 * (time.perf_counter() - t0) / steps
+    st.agent_ptr(g, 0)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        st.mark_changed(g)
+        st.run(1)
+        st.agent_ptr(g, 0)
+    copying = 1000.0 * (time.perf_counter() - t0) / steps
+    out["device_resident"] = {"agents": int(recs.shape[0]), "tay_run_1_ms": resident, "with_push_fetch_ms": copying}
+    st.end()
+    st.close()
+
+    # 2-D space (dims 2): 1M agents on a 2000 x 2000 plane, radius 5
+    ps = W.basic_points(1 << 20, seed=310, side=2000.0)
+    ps.p[:, 2] = 0.0
+    rec2 = M.records(M.TEST_RECORD, ps.p, ps.v)
+    s2 = M.test_setup(radius=5.0, part=5.0, passes=("agent_see", "agent_act"), mb=64)
+    s2.passes[-1].ctx[4:7] = 2000.0
+    s2.dims = 2
+    st, g = M.make_state(s2, rec2)
+    st.start()
+    st.run(3)
+    st.run(steps)
+    dev = st.L.tay_get_device_ms_for_last_run(st.ptr) / steps
+    out["dims2"] = {"agents": 1 << 20, "ms_per_step": dev, "pair_interactions_per_s": st.pairs() / steps / (dev / 1000.0)}
+    st.end()
+    st.close()
+
+    # fixed space box around the test model's walls
+    ps = W.basic_points(1 << 20, seed=311, side=1000.0)
+    rec3 = M.records(M.TEST_RECORD, ps.p, ps.v)
+    s3 = M.test_setup(radius=10.0, part=10.0, mb=128)
+    s3.fixed_box = ((0.0, 0.0, 0.0), (1000.0, 1000.0, 1000.0))
+    st, g = M.make_state(s3, rec3)
+    st.start()
+    st.run(3)
+    st.run(steps)
+    dev = st.L.tay_get_device_ms_for_last_run(st.ptr) / steps
+    out["fixed_box"] = {"agents": 1 << 20, "ms_per_step": dev,
+                        "pair_interactions_per_s": st.pairs() / steps / (dev / 1000.0)}
+    st.end()
+    st.close()
+
+    # non-point agents: 524,288 cubes of edge 1..5 in [0, 500]^3, radius 5
+    bx = W.box_agents(1 << 19, seed=312, side=500.0, min_size=1.0, max_size=5.0)
+    rec4 = M.box_records(bx.lo, bx.hi, bx.v)
+    s4 = M.box_setup(radius=5.0, part=5.0, mb=64)
+    s4.passes[-1].ctx[4:7] = 500.0
+    st, g = M.make_state(s4, rec4)
+    st.start()
+    st.run(3)
+    st.run(steps)
+    dev = st.L.tay_get_device_ms_for_last_run(st.ptr) / steps
+    out["box_agents"] = {"agents": 1 << 19, "ms_per_step": dev,
+                         "pair_interactions_per_s": st.pairs() / steps / (dev / 1000.0)}
+    st.end()
+    st.close()
+    return out
+
+
 def cpu_baseline(setup, recs, steps):
     """Oracle restatement of the reference CpuZGrid step, all host threads, `steps` steps."""
     from oracle import pyoracle as O
@@ -479,6 +584,8 @@ def run_gb300(args, rank, world, D):
             line["adjoint"] = adjoint_leg(keep=4, tune=tune)
             line["adjoint_keep1"] = adjoint_leg(keep=1, tune=tune)
             line["adjoint_record_all"] = adjoint_leg(every=0, tune=tune)
+        if args.features:
+            line["features"] = features_leg(setup, recs)
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(setup, recs, args.cpu_steps)
         print(json.dumps(line), flush=True)
