@@ -8,6 +8,8 @@
     x_final = SphRolloutFunction.apply(v0, params, roll)   # torch; gradients flow to v0 and
                                                            # params = [instances, 2] (alpha, c0)
 
+    history = fit_parameters(roll, target_x, iters=20)     # (alpha, c0) fitted to a target
+
 `instances` is a list of (PointSet, alpha, c0, tank_min, tank_max); every instance runs the
 full SPH pass sequence (density, pressure, force, integrate) as one segment of one batch.
 Rows of the per-particle arrays are the particles in instance order, each instance's
@@ -129,3 +131,35 @@ def make_function():
             return torch.from_numpy(dv0.copy()), torch.from_numpy(dp.copy()), None
 
     return SphRolloutFunction
+
+
+def fit_parameters(roll: SphRollout, target, iters: int = 20, lr: float = 0.05, scale=(0.05, 20.0)):
+    """Fits every instance's (alpha, c0) to a target rollout: minimises each instance's mean
+    squared distance of final positions to `target` ([N, 3], instances concatenated) with
+    Adam on the parameters divided by `scale`, gradients from the adjoint.  Updates
+    roll.params in place; returns the history [(loss summed over instances, params copy)]."""
+    scale = np.asarray(scale, np.float64)
+    z = roll.params / scale
+    m = np.zeros_like(z)
+    v = np.zeros_like(z)
+    b1, b2, eps = 0.9, 0.999, 1e-12
+    history = []
+    target = np.asarray(target, np.float64)
+    for it in range(1, iters + 1):
+        roll.params = z * scale
+        x, _ = roll.forward()
+        g = np.zeros((roll.n, 3), np.float64)
+        loss = 0.0
+        for k in range(len(roll.instances)):
+            a, b = roll.offsets[k], roll.offsets[k + 1]
+            d = x[a:b].astype(np.float64) - target[a:b]
+            loss += float(np.mean(np.sum(d * d, axis=1)))
+            g[a:b] = 2.0 * d / (b - a)
+        history.append((loss, roll.params.copy()))
+        _, _, dp = roll.backward(g)
+        gz = dp * scale
+        m = b1 * m + (1 - b1) * gz
+        v = b2 * v + (1 - b2) * gz * gz
+        z = z - lr * (m / (1 - b1 ** it)) / (np.sqrt(v / (1 - b2 ** it)) + eps)
+    roll.params = z * scale
+    return history

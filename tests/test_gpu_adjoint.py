@@ -144,3 +144,23 @@ def test_adjoint_row_order(gpu_grads):
     np.testing.assert_allclose(dp, gpu_grads["dp"], rtol=TOL)
     assert normwise(dx0, gpu_grads["dx0"]) < TOL
     assert normwise(dv0, gpu_grads["dv0"]) < TOL
+
+
+def test_fit_viscosity_and_sound_speed_to_a_target_rollout(gpu):
+    """The adjoint used as intended: two instances starting at (alpha, c0) = (0.05, 20) and
+    (0.12, 18) fitted with Adam to a target rollout made with (0.08, 22), 100 steps."""
+    from tay_gb300.adjoint import fit_parameters
+
+    tank = (0.16, 0.12, 0.12)
+    s = W.sph_dam(10, 10, 8, tank=tank)
+    tgt = SphRollout([(s.points, 0.08, 22.0, (0.0, 0.0, 0.0), tank)] * 2, 100)
+    target, _ = tgt.forward()
+    tgt.close()
+    roll = SphRollout([(s.points, 0.05, 20.0, (0.0, 0.0, 0.0), tank), (s.points, 0.12, 18.0, (0.0, 0.0, 0.0), tank)],
+                      100, checkpoint_every=20)
+    hist = fit_parameters(roll, target, iters=25, lr=0.05)
+    roll.close()
+    losses = [l for l, _ in hist]
+    assert min(losses[-5:]) < 0.1 * losses[0], losses
+    assert np.all(np.abs(roll.params[:, 0] - 0.08) < 0.012), roll.params
+    assert np.all(np.abs(roll.params[:, 1] - 22.0) < 2.0), roll.params
