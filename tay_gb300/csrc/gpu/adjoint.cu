@@ -163,6 +163,7 @@ SeeLaunch see_launch(TgpuBatch *b, const KernelRun &r, const PassIO &io) {
     S.union_factor = r.union_factor;
     S.rows = b->cell_order == kOrderRows ? 1u : 0u;
     S.hit_masks = b->hit_masks;
+    S.err = b->d_err;
     S.pairs = b->d_pairs;
     S.telemetry = nullptr;
     S.io = io;

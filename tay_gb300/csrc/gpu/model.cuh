@@ -84,7 +84,9 @@ const ModelDesc *model_box();
 template <class P>
 void launch_see_t(const SeeLaunch &L, size_t smem, cudaStream_t st) {
     if (!L.ctas) return;
-    if (L.rows)
+    if (L.rows && L.stage_cap)
+        see_rows_kernel<P, true><<<L.ctas, kSeeThreads, smem, st>>>(L);
+    else if (L.rows)
         see_rows_kernel<P><<<L.ctas, kSeeThreads, 0, st>>>(L);
     else
         see_kernel<P><<<L.ctas, kSeeThreads, smem, st>>>(L);
@@ -95,7 +97,9 @@ void launch_act_t(const ActLaunch &L, cudaStream_t st) {
 }
 template <class P>
 cudaError_t prepare_see_t(size_t smem) {
-    return cudaFuncSetAttribute(see_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(see_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(see_rows_kernel<P, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 template <class M>
 void pack_t(const uint32_t *aos, uint32_t n, const PassIO &io, cudaStream_t st) {

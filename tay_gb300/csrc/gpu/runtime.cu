@@ -167,7 +167,9 @@ int tgpu::check_device_error(TgpuBatch *b) {
     if (!err) return TGPU_OK;
     CK(cudaMemset(b->d_err, 0, sizeof(err)));
     return fail(TGPU_ERR_DEVICE, "device error 0x%x%s", err,
-                (err & kErrSortLookback) ? " (radix sort look-back wait ran out)" : "");
+                (err & kErrSortLookback) ? " (radix sort look-back wait ran out)"
+        : (err & kErrStageWait) ? " (a see CTA's wait for its bulk copies ran out)"
+        : (err & kErrStageRange) ? " (a see lane's row range fell outside the staged run)" : "");
 }
 
 namespace {
@@ -384,6 +386,7 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E) {
             S.union_factor = r.union_factor;
             S.rows = b->cell_order == kOrderRows ? 1u : 0u;
             S.hit_masks = b->hit_masks;
+            S.err = b->d_err;
             if (r.seer_seg >= 0) {
                 // one seer segment; the seen agents are another segment's (or its own)
                 S.cta_offset = b->cta_begin[r.seer_seg];
@@ -698,7 +701,13 @@ int setup_see_run(TgpuBatch *b, KernelRun &r, int self_see) {
     CKR(cudaMemset(r.d_see_ctx, 0, b->ctx_stride * b->nseg));
     const uint32_t cap_default = r.k->staged_f4 <= 1 ? 1024u : 768u;
     r.union_factor = g_tuning.union_factor;
-    if (g_tuning.stage && g_tuning.cell_order != kOrderRows) {
+    if (g_tuning.stage && g_tuning.cell_order == kOrderRows) {
+        // row order: bulk-copied union rows; stage_cells bounds the rows per CTA
+        r.stage_cap = g_tuning.stage_cap ? g_tuning.stage_cap : cap_default;
+        r.stage_cells = g_tuning.stage_cells ? g_tuning.stage_cells : 64u;
+        r.smem = (size_t)r.k->staged_f4 * r.stage_cap * sizeof(float4) + (2ull * r.stage_cells + 2) * sizeof(uint32_t) +
+                 sizeof(uint64_t);
+    } else if (g_tuning.stage) {
         r.stage_cap = g_tuning.stage_cap ? g_tuning.stage_cap : cap_default;
         r.stage_cells = g_tuning.stage_cells ? g_tuning.stage_cells : 512u;
         r.smem = (size_t)r.k->staged_f4 * r.stage_cap * sizeof(float4) + (2ull * r.stage_cells + 1) * sizeof(uint32_t);

@@ -166,9 +166,12 @@ TGPU_D void lane_run(typename P::Seer &s, const float4 &sp, const float4 &r4, ui
                      uint32_t &tested) {
     constexpr bool kGlobal = Acc::kGlobal;
     constexpr int U = UnrollOf<P>::value;
+    if (j1 <= j0) return;
     tested += j1 - j0;
     uint32_t j = j0;
-    for (; j + (U - 1) < j1; j += U) {
+    // counted on the remaining length, not on j + U - 1, which can wrap for indices
+    // near 2^32 (ranges translated into staged slots)
+    for (; j1 - j >= (uint32_t)U; j += U) {
         float4 b[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) b[u] = load_pos(src, j + u, kGlobal);
@@ -197,6 +200,42 @@ TGPU_D uint2 row_range(const uint32_t *words, const uint4 *hdr, uint32_t row, ui
     const uint32_t e1 = __ldg(words + row * dx + min((uint32_t)x1 + 1u, dx - 1u));
     if ((uint32_t)x0 > h.y || (uint32_t)x1 < h.x) return make_uint2(0u, 0u);
     return make_uint2((uint32_t)x0 <= h.x ? h.z : e0, (uint32_t)x1 >= h.y ? h.w : e1);
+}
+
+// ---- bulk copies (TMA, non-tensor) into shared memory, completed on an mbarrier ----
+TGPU_D uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+TGPU_D void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+TGPU_D void fence_mbar_init() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+TGPU_D void mbar_inval(uint64_t *bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+TGPU_D void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+// one contiguous run of bytes (16-byte aligned, a multiple of 16) global -> shared
+TGPU_D void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+TGPU_D bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for phase 0 of a one-shot barrier; false when the bound ran out.
+constexpr uint32_t kStageSpinLimit = 1u << 22;
+TGPU_D bool mbar_wait_bounded(uint64_t *bar) {
+    for (uint32_t it = 0; it < kStageSpinLimit; ++it)
+        if (mbar_try_wait(bar, 0)) return true;
+    return false;
 }
 
 // Per-lane candidates [j0, j1) in batches of 32, the see function run over hit masks:
@@ -483,7 +522,7 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
 // ranges are nearly the same length and their candidate loads fall on neighbouring
 // addresses.  No staging; a warp whose union box is compact walks the union's row
 // ranges with the two-phase batches instead.
-template <class P>
+template <class P, bool kStage = false>
 __global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
     using namespace see_detail;
     const uint2 cta = L.cta_table[L.cta_offset + blockIdx.x];
@@ -522,11 +561,118 @@ __global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
     const uint32_t self = (active && L.skip_self) ? i : 0xFFFFFFFFu;
     uint32_t pairs = 0;
     uint32_t tested = 0;
-    if (L.telemetry && threadIdx.x == 0) atomicAdd(L.telemetry + 2, 1ull);
+
+    // Optional staging (stage_cap > 0, point agents): the rows of the union of the CTA's
+    // seer boxes are contiguous runs of agents, each copied into shared memory by one bulk
+    // copy (TMA) per seen stream, completed on an mbarrier; the lanes then walk their rows
+    // there.  CTAs whose halo does not fit fall back to the walk through L1.
+    bool staged = false;
+    if constexpr (kStage && !kBox) {
+        extern __shared__ __align__(16) unsigned char smem_raw[];
+        float4 *stage = reinterpret_cast<float4 *>(smem_raw);
+        uint32_t *row_off = reinterpret_cast<uint32_t *>(stage + (size_t)P::kSeenF4 * L.stage_cap);
+        uint32_t *row_j0 = row_off + L.stage_cells;
+        // row_off starts 16-byte aligned and the two tables hold 2 * stage_cells words,
+        // so the barrier after them is 8-byte aligned
+        uint64_t *bar = reinterpret_cast<uint64_t *>(row_off + 2u * L.stage_cells);
+        __shared__ int hb[6];
+        __shared__ uint32_t s_total;
+        if (threadIdx.x < 6) hb[threadIdx.x] = threadIdx.x < 3 ? INT_MAX : INT_MIN;
+        __syncthreads();
+        {
+            const int l0 = warp_min_i(lo[0]), l1 = warp_min_i(lo[1]), l2 = warp_min_i(lo[2]);
+            const int h0 = warp_max_i(hi[0]), h1 = warp_max_i(hi[1]), h2 = warp_max_i(hi[2]);
+            if (lane == 0 && l0 <= h0) {
+                atomicMin(&hb[0], l0);
+                atomicMin(&hb[1], l1);
+                atomicMin(&hb[2], l2);
+                atomicMax(&hb[3], h0);
+                atomicMax(&hb[4], h1);
+                atomicMax(&hb[5], h2);
+            }
+        }
+        __syncthreads();
+        const int X0 = hb[0], Y0 = hb[1], Z0 = hb[2];
+        const int ny = hb[4] - Y0 + 1, nz = hb[5] - Z0 + 1;
+        const long long nrows = (hb[3] >= X0 && ny > 0 && nz > 0) ? (long long)ny * nz : 0;
+        if (nrows > 0 && nrows <= (long long)L.stage_cells) {
+            // each union row's candidate range over the union's x cells
+            for (uint32_t t = threadIdx.x; t < (uint32_t)nrows; t += kSeeThreads) {
+                const uint32_t z = (uint32_t)Z0 + t / (uint32_t)ny, y = (uint32_t)Y0 + t % (uint32_t)ny;
+                const uint2 jr = row_range(words, hdr, z * dy0 + y, dx0, X0, hb[3]);
+                row_j0[t] = jr.x;
+                row_off[t] = jr.y - jr.x;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                uint32_t run = 0;
+                for (uint32_t t = 0; t < (uint32_t)nrows; ++t) {
+                    const uint32_t c = row_off[t];
+                    row_off[t] = run;
+                    run += c;
+                }
+                s_total = run;
+                if (run > 0 && run <= L.stage_cap) {
+                    mbar_init(bar, 1);
+                    fence_mbar_init();
+                }
+            }
+            __syncthreads();
+            const uint32_t total = s_total;
+            if (total > 0 && total <= L.stage_cap) {
+                if (threadIdx.x == 0) {
+                    mbar_arrive_expect_tx(bar, total * (uint32_t)sizeof(float4) * (uint32_t)P::kSeenF4);
+                    for (uint32_t t = 0; t < (uint32_t)nrows; ++t) {
+                        const uint32_t c = (t + 1 < (uint32_t)nrows ? row_off[t + 1] : total) - row_off[t];
+                        if (!c) continue;
+#pragma unroll
+                        for (int k = 0; k < P::kSeenF4; ++k)
+                            bulk_copy_g2s(stage + (size_t)k * L.stage_cap + row_off[t],
+                                          L.io.in_f4[P::seen_stream(k)] + row_j0[t], c * (uint32_t)sizeof(float4),
+                                          bar);
+                    }
+                }
+                staged = mbar_wait_bounded(bar);
+                if (!staged) {
+                    // a wait that ran out: report it, and let the copies in flight land
+                    // before this CTA's shared memory can be given to another CTA
+                    if (threadIdx.x == 0 && L.err) atomicOr(L.err, kErrStageWait);
+                    mbar_wait_bounded(bar);
+                }
+                staged = __syncthreads_and(staged);
+                if (threadIdx.x == 0) mbar_inval(bar);  // every thread has left the wait
+                if (staged) {
+                    const SmemSeen sacc{stage, L.stage_cap};
+                    if (active) {
+                        for (int z = lo[2]; z <= hi[2]; ++z)
+                            for (int y = lo[1]; y <= hi[1]; ++y) {
+                                const uint32_t t = (uint32_t)(z - Z0) * (uint32_t)ny + (uint32_t)(y - Y0);
+                                const uint2 jr = row_range(words, hdr, (uint32_t)z * dy0 + (uint32_t)y, dx0, lo[0], hi[0]);
+                                if (jr.y <= jr.x) continue;  // an empty row is never translated
+                                const uint32_t shift = row_off[t] - row_j0[t];  // global index -> staged slot
+                                const uint32_t cnt = (t + 1 < (uint32_t)nrows ? row_off[t + 1] : total) - row_off[t];
+                                // the lane's x range lies inside the union's, so its run lies
+                                // inside the staged one; checked, reported and skipped if not
+                                if (jr.x < row_j0[t] || jr.y - row_j0[t] > cnt) {
+                                    if (L.err) atomicOr(L.err, kErrStageRange);
+                                    continue;
+                                }
+                                // the seer's own slot, only when it sits in this row's staged run
+                                const uint32_t self_s =
+                                    (self >= row_j0[t] && self - row_j0[t] < cnt) ? self + shift : 0xFFFFFFFFu;
+                                lane_run<P>(s, sp, r4, jr.x + shift, jr.y + shift, self_s, stage, sacc, sctx, pairs,
+                                            tested);
+                            }
+                    }
+                }
+            }
+        }
+    }
+    if (L.telemetry && threadIdx.x == 0) atomicAdd(L.telemetry + (staged ? 1 : 2), 1ull);
 
     const int wl0 = warp_min_i(lo[0]), wl1 = warp_min_i(lo[1]), wl2 = warp_min_i(lo[2]);
     const int wh0 = warp_max_i(hi[0]), wh1 = warp_max_i(hi[1]), wh2 = warp_max_i(hi[2]);
-    if (wl0 <= wh0) {
+    if (!staged && wl0 <= wh0) {
         const int lane_vol = active ? (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) * (hi[0] - lo[0] + 1) : 0;
         const long long union_vol = (long long)(wh0 - wl0 + 1) * (wh1 - wl1 + 1) * (wh2 - wl2 + 1);
         const bool union_mode = !kBox && union_vol <= (long long)L.union_factor * warp_max_i(lane_vol);

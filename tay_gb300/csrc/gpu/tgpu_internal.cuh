@@ -254,6 +254,8 @@ enum DeviceError : uint32_t {
     kErrNone = 0,
     kErrTableOverflow = 1,
     kErrSortLookback = 2,  // a radix pass's look-back wait ran out (a tile never published)
+    kErrStageWait = 4,     // a see CTA's wait for its bulk copies ran out
+    kErrStageRange = 8,    // a lane's row range fell outside its row's staged run (skipped)
 };
 
 }  // namespace tgpu

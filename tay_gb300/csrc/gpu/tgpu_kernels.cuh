@@ -58,6 +58,7 @@ struct SeeLaunch {
     uint32_t union_factor;    // a warp walks its union box when union <= factor x lane box
     uint32_t rows;            // 1: the table is in row order (see_rows_kernel)
     uint32_t hit_masks;       // row order: lanes collect box-test hits in 32-bit masks first
+    uint32_t *err;            // device error word (DeviceError bits)
     uint32_t cta_offset;      // first entry of cta_table this launch covers
     uint32_t cross;           // 1: the seen agents are segment seen_seg (a two-group pass)
     uint32_t seen_seg;

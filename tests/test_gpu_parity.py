@@ -111,6 +111,7 @@ def test_batch_matches_individual_runs(gpu):
     {"cell_order": 1}, {"cell_order": 1, "cell_multiple": 0.34}, {"cell_order": 1, "union_factor": 2},
     {"cell_order": 1, "hit_masks": 1}, {"cell_order": 1, "hit_masks": 1, "cell_multiple": 0.5},
     {"cell_order": 1, "x_cell_factor": 0.25}, {"cell_order": 1, "cell_multiple": 0.5, "x_cell_factor": 0.5},
+    {"cell_order": 1, "stage": 1}, {"cell_order": 1, "stage": 1, "x_cell_factor": 0.5, "stage_cap": 256},
     {"union_factor": 2}, {"stage": 1}, {"cell_multiple": 0.5}, {"cell_multiple": 1.5},
 ])
 def test_walk_tunings_match_oracle(gpu, port, tuning):
@@ -131,7 +132,7 @@ def test_walk_tunings_match_oracle(gpu, port, tuning):
         assert normwise(g[f][:, :3], o[f][:, :3]) < TOL_1STEP, f
 
 
-@pytest.mark.parametrize("order", [0, 1])
+@pytest.mark.parametrize("order", [0, 1, "rows_staged"])
 def test_cell_orders_many_steps(gpu, port, order):
     """Both cell orders over 20 see+act steps of boids and 5 SPH steps (all four passes)."""
     ps = W.boids_points(20000, seed=13, clusters=4, side=300.0)
@@ -140,8 +141,9 @@ def test_cell_orders_many_steps(gpu, port, order):
     sph = W.sph_dam(16, 24, 16)
     srecs = M.records(M.SPH_RECORD, sph.points.p, sph.points.v)
     ssetup = M.sph_setup()
+    tuning = {"cell_order": 1, "stage": 1, "cell_multiple": 0.5} if order == "rows_staged" else {"cell_order": order}
     try:
-        api.set_tuning(cell_order=order)
+        api.set_tuning(**tuning)
         g = M.run(setup, recs, 20)
         gs = M.run(ssetup, srecs, 5)
     finally:
@@ -152,3 +154,36 @@ def test_cell_orders_many_steps(gpu, port, order):
     os_ = oracle_run(port, O.MODEL_SPH, ssetup, srecs, 5)
     assert normwise(gs["p"][:, :3], os_["p"][:, :3]) < TOL_1STEP
     assert normwise(gs["v"][:, :3], os_["v"][:, :3]) < TOL_MANY
+
+
+@pytest.mark.parametrize("tuning", [
+    {"cell_multiple": 1.0, "x_cell_factor": 0.5},
+    {"cell_multiple": 0.5, "x_cell_factor": 0.5},
+    {"cell_multiple": 0.25, "x_cell_factor": 1.0, "stage_cap": 512, "stage_cells": 256},
+])
+def test_staged_rows_bit_identical_full_size(gpu, tuning):
+    """At the full benchmark size (2^20 boids, 64 clusters, r = cell = 10) the row walk that
+    bulk-copies its union rows into shared memory visits the same candidates in the same
+    order as the walk through L1, so the records after 5 see+act steps are bit-identical
+    and the pair counts equal; some CTAs must have been staged."""
+    ps = W.boids_points(1 << 20, seed=2)
+    recs = M.records(M.BOIDS_RECORD, ps.p, ps.v)
+    setup = M.boids_setup(r=10.0, part=10.0, mb=256)
+    out = {}
+    try:
+        for st in (0, 1):
+            api.set_tuning(cell_order=1, stage=st, **tuning)
+            b = api.Batch([(setup, recs)])
+            try:
+                b.push()
+                pairs = [b.run(1)[1] for _ in range(5)]
+                tel = b.telemetry()
+                out[st] = (b.fetch(0), pairs, tel)
+            finally:
+                b.close()
+    finally:
+        api.set_tuning()
+    (r0, p0, _), (r1, p1, t1) = out[0], out[1]
+    assert p0 == p1
+    assert r0.tobytes() == r1.tobytes()
+    assert t1["staged_ctas"] > 0
