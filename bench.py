@@ -505,8 +505,10 @@ def run_gb300(args, rank, world, D):
     # e2e through the C API with host buffers (push + step + fetch every step)
     st, g = M.make_state(setup, recs)
     st.start()
-    for _ in range(max(1, args.warmup // 2)):
+    for _ in range(max(3, args.warmup // 2)):  # the same loop as timed (its step graphs exist)
+        st.mark_changed(g)
         st.run(1)
+        st.agent_ptr(g, 0)
     e2e_steps = min(args.steps, 50)
     D.barrier()
     t0 = time.perf_counter()

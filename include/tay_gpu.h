@@ -116,6 +116,15 @@ int tgpu_batch_sync(TgpuBatch *batch);
  * tay_get_agent exposes them (tay/state.c:178-181). */
 int tgpu_batch_fetch(TgpuBatch *batch, int group, void *host_records);
 
+/* Write-through fetch of group `group` into page-locked `host_records` (from
+ * tgpu_host_alloc or cudaHostAlloc; NULL turns it off; pageable memory is refused with
+ * TGPU_ERR_ARG): the last step of every following run writes the group's records there
+ * as its final pass finishes, chunk by chunk on a second stream, overlapping the host
+ * link with the rest of the pass; a tgpu_batch_fetch into the same buffer after such a
+ * run only waits.  Replaces the fetch after every run of the reference's OpenCL path
+ * (tay/ocl.c:261-272) for hosts that read their agents after each run. */
+int tgpu_batch_write_through(TgpuBatch *batch, int group, void *host_records);
+
 /* Device time in ms of the last tgpu_batch_run / enqueue+sync, from CUDA events on the
  * batch's stream, and the number of pairs that passed the box test in it. */
 double tgpu_batch_last_device_ms(const TgpuBatch *batch);

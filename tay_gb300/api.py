@@ -89,6 +89,7 @@ TGPU_SYMBOLS = [
     ("tgpu_batch_enqueue", ctypes.c_int, [_VP, ctypes.c_int]),
     ("tgpu_batch_sync", ctypes.c_int, [_VP]),
     ("tgpu_batch_fetch", ctypes.c_int, [_VP, ctypes.c_int, _VP]),
+    ("tgpu_batch_write_through", ctypes.c_int, [_VP, ctypes.c_int, _VP]),
     ("tgpu_batch_last_device_ms", ctypes.c_double, [_VP]),
     ("tgpu_batch_last_pairs", ctypes.c_ulonglong, [_VP]),
     ("tgpu_batch_launches_per_step", ctypes.c_int, [_VP]),

@@ -84,6 +84,16 @@ const ModelDesc *model_box();
 template <class P>
 void launch_see_t(const SeeLaunch &L, size_t smem, cudaStream_t st) {
     if (!L.ctas) return;
+    if constexpr (!std::is_void_v<typename see_detail::CodecOf<P>::type>) {
+        // write-through launch (the last pass of a run): the walk without row staging
+        if (L.wt) {
+            if (L.rows)
+                see_rows_kernel<P, false, true><<<L.ctas, kSeeThreads, 0, st>>>(L);
+            else
+                see_kernel<P, true><<<L.ctas, kSeeThreads, smem, st>>>(L);
+            return;
+        }
+    }
     if (L.rows && L.stage_cap)
         see_rows_kernel<P, true><<<L.ctas, kSeeThreads, smem, st>>>(L);
     else if (L.rows)
@@ -99,6 +109,10 @@ template <class P>
 cudaError_t prepare_see_t(size_t smem) {
     cudaError_t e = cudaFuncSetAttribute(see_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    if constexpr (!std::is_void_v<typename see_detail::CodecOf<P>::type>) {
+        e = cudaFuncSetAttribute(see_kernel<P, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
     return cudaFuncSetAttribute(see_rows_kernel<P, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 template <class M>

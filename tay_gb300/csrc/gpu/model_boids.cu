@@ -117,8 +117,11 @@ TGPU_D void act_fn(float4 &p, float4 &v, const Seer &s, const Ctx &c) {
     p.z = p.z + c.dt * v.z;
 }
 
+struct Codec;  // the record codec, defined below
+
 struct SeeOnly {
     using SeeCtx = Ctx;
+    using Codec = boids::Codec;
     using ActCtx = Ctx;
     using Seer = boids::Seer;
     static constexpr int kSeenF4 = 2;
@@ -138,6 +141,7 @@ struct SeeOnly {
 
 struct SeeAct {
     using SeeCtx = Ctx;
+    using Codec = boids::Codec;
     using ActCtx = Ctx;
     using Seer = boids::Seer;
     static constexpr int kSeenF4 = 2;

@@ -73,8 +73,11 @@ TGPU_D void act_fn(float4 &mn, float4 &mx, float4 &v, float &bx, float &by, floa
     if (mx.z > c.max.z) { mx.z = c.max.z; mn.z = c.max.z - sz; v.z = -v.z; }
 }
 
+struct Codec;  // the record codec, defined below
+
 struct SeeOnly {
     using SeeCtx = box::SeeCtx;
+    using Codec = box::Codec;
     using ActCtx = box::SeeCtx;
     using Seer = box::Seer;
     static constexpr bool kBox = true;
@@ -98,6 +101,7 @@ struct SeeOnly {
 
 struct SeeAct {
     using SeeCtx = box::SeeCtx;
+    using Codec = box::Codec;
     using ActCtx = box::ActCtx;
     using Seer = box::Seer;
     static constexpr bool kBox = true;

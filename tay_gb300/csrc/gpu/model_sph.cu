@@ -76,6 +76,8 @@ TGPU_D float pressure(float rho, const Ctx &c) {
 
 // ---------------------------------------------------------------- density (+ pressure)
 
+struct Codec;  // the record codec, defined below
+
 struct DensitySeer {
     float rho;
 };
@@ -83,6 +85,7 @@ struct DensitySeer {
 template <bool kPressure>
 struct Density {
     using SeeCtx = Ctx;
+    using Codec = sph::Codec;
     using ActCtx = Ctx;
     using Seer = DensitySeer;
     static constexpr int kSeenF4 = 1;
@@ -114,6 +117,7 @@ struct ForceSeer {
 template <bool kIntegrate, bool kStoreAcc = false>
 struct Force {
     using SeeCtx = Ctx;
+    using Codec = std::conditional_t<kStoreAcc, void, sph::Codec>;  // not the adjoint's recording pass
     using ActCtx = Ctx;
     using Seer = ForceSeer;
     static constexpr int kSeenF4 = 3;

@@ -64,8 +64,11 @@ TGPU_D void act_fn(float4 &p, float4 &v, float &bx, float &by, float &bz, int &c
     if (p.z > c.max.z) { p.z = c.max.z; v.z = -v.z; }
 }
 
+struct Codec;  // the record codec, defined below
+
 struct SeeOnly {
     using SeeCtx = test_basic::SeeCtx;
+    using Codec = test_basic::Codec;
     using ActCtx = test_basic::SeeCtx;
     using Seer = test_basic::Seer;
     static constexpr int kSeenF4 = 1;
@@ -88,6 +91,7 @@ struct SeeOnly {
 
 struct SeeAct {
     using SeeCtx = test_basic::SeeCtx;
+    using Codec = test_basic::Codec;
     using ActCtx = test_basic::ActCtx;
     using Seer = test_basic::Seer;
     static constexpr int kSeenF4 = 1;

@@ -129,6 +129,7 @@ void free_batch(TgpuBatch *b) {
     }
     if (b->e0) cudaEventDestroy(b->e0);
     if (b->e1) cudaEventDestroy(b->e1);
+    cudaFree(b->d_wt);
     if (b->st) cudaStreamDestroy(b->st);
     delete b;
 }
@@ -327,9 +328,35 @@ void mark(const StepEvents *e, int k, cudaStream_t st) {
     if (e) cudaEventRecord(e->ev[k], st);
 }
 
+// The model's unpack program for fetched records: the batch's program, or for state
+// batches 0 (accumulators visible) unless an act pass consumed them.
+uint32_t unpack_program(const TgpuBatch *b) {
+    uint32_t program = (uint32_t)b->program;
+    if (!b->state_passes.empty()) {
+        program = 0u;
+        for (const auto &p : b->state_passes)
+            if (!p.pass.is_see) program = 0xFFFFFFFFu;
+    }
+    return program;
+}
+
+// Records [lo, hi) of the batch (current buffers) into the write-through host copies of
+// the segments they belong to.
+void unpack_range(TgpuBatch *b, uint32_t lo, uint32_t hi, cudaStream_t st) {
+    const uint32_t words = b->m->agent_bytes / 4;
+    for (int s = 0; s < b->nseg; ++s) {
+        if (!b->wt_dev[s]) continue;
+        const SegmentSpec &sp = b->specs[s];
+        const uint32_t a = max(lo, sp.begin), e = min(hi, sp.begin + sp.count);
+        if (a >= e) continue;
+        b->m->unpack(b->wt_dev[s] + (size_t)(a - sp.begin) * words, e - a, make_io(b, nullptr, false, a),
+                     unpack_program(b), st);
+    }
+}
+
 }  // namespace
 
-void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E) {
+void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E, bool write_through) {
     if (b->total == 0 || b->tiles == 0) return;
     cudaStream_t st = b->st;
     SortLaunch L = sort_launch(b);
@@ -364,9 +391,11 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E) {
     mark(E, 7, st);
 
     int kidx = 0;
+    bool written = false;
     for (auto &r : b->runs) {
         mark(E, 8 + 2 * kidx, st);
         const bool see = r.k->see != nullptr;
+        const bool last = kidx + 1 == (int)b->runs.size();
         PassIO io = make_io(b, r.k, see, 0);
         if (see) {
             SeeLaunch S{};
@@ -397,6 +426,13 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E) {
             S.pairs = b->d_pairs;
             S.telemetry = b->d_telemetry;
             S.io = io;
+            // Write-through on the final pass over every segment: each CTA stores its seers'
+            // finished records to the host as it ends, so the host link overlaps the pass.
+            if (write_through && last && r.seer_seg < 0) {
+                S.wt = b->d_wt;
+                S.wt_program = unpack_program(b);
+                written = true;
+            }
             r.k->launch_see(S, r.smem, st);
             for (int c = 0; c < b->m->nf4; ++c)
                 if (b->m->role_f4[c] == kState && (r.k->writes_f4 >> c & 1u) && (r.k->seen_f4 >> c & 1u))
@@ -418,12 +454,17 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E) {
         mark(E, 9 + 2 * kidx, st);
         ++kidx;
     }
+    // write-through when the last pass is not one see over every segment: after the step
+    if (write_through && !written) unpack_range(b, 0, b->total, st);
     if (E) cudaEventRecord(E->ev2[0], st);
     launch_cell_table(L, skeys, 0, st);
     if (E) cudaEventRecord(E->ev2[1], st);
 }
 
 namespace {
+
+// Graph-cache key bit of a step that writes its records through to the host.
+constexpr uint64_t kWriteThroughGraph = 1ull << 62;
 
 uint64_t parity_signature(const TgpuBatch *b) {
     uint64_t s = 0;
@@ -641,6 +682,8 @@ int add_segments(TgpuBatch *b, const TgpuGroup *groups, int group_count, const s
     }
     b->cta_begin.push_back((uint32_t)b->cta.size());
     b->total = total;
+    b->wt_dev.assign((size_t)group_count, nullptr);
+    b->wt_done.assign((size_t)group_count, 0);
     b->tiles = (uint32_t)b->tile_seg.size();
     b->ctas = (uint32_t)b->cta.size();
     return TGPU_OK;
@@ -912,6 +955,7 @@ int tgpu_batch_push(TgpuBatch *b, int group, const void *host) {
     const SegmentSpec &sp = b->specs[group];
     const uint32_t n = sp.count;
     h.pushed = true;
+    b->wt_done[group] = 0;
     b->specs_dirty = true;
     if (!n) {
         for (int a = 0; a < 3; ++a) h.host_min[a] = h.host_max[a] = 0.0f;
@@ -954,13 +998,19 @@ int tgpu_batch_enqueue(TgpuBatch *b, int steps) {
     if (rc) return rc;
     CK(cudaMemsetAsync(b->d_pairs, 0, sizeof(unsigned long long), b->st));
     CK(cudaMemsetAsync(b->d_telemetry, 0, sizeof(unsigned long long) * 8, b->st));
+    bool any_wt = false;
+    for (int s = 0; s < b->nseg; ++s) {
+        b->wt_done[s] = 0;
+        any_wt = any_wt || b->wt_dev[s] != nullptr;
+    }
     CK(cudaEventRecord(b->e0, b->st));
     for (int i = 0; i < steps; ++i) {
+        const bool wt = any_wt && i + 1 == steps;  // the run's last step writes through
         if (!b->use_graphs) {
-            enqueue_step(b);
+            enqueue_step(b, nullptr, wt);
             continue;
         }
-        const uint64_t sig = parity_signature(b);
+        const uint64_t sig = parity_signature(b) | (wt ? kWriteThroughGraph : 0ull);
         auto it = b->graphs.find(sig);
         if (it != b->graphs.end()) {
             CK(cudaGraphLaunch(it->second, b->st));
@@ -969,7 +1019,7 @@ int tgpu_batch_enqueue(TgpuBatch *b, int steps) {
         }
         cudaGraph_t graph = nullptr;
         CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
-        enqueue_step(b);
+        enqueue_step(b, nullptr, wt);
         CK(cudaStreamEndCapture(b->st, &graph));
         cudaGraphExec_t exec = nullptr;
         cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
@@ -980,6 +1030,27 @@ int tgpu_batch_enqueue(TgpuBatch *b, int steps) {
     }
     CK(cudaEventRecord(b->e1, b->st));
     CK(cudaGetLastError());
+    if (any_wt && steps > 0)
+        for (int s = 0; s < b->nseg; ++s) b->wt_done[s] = b->wt_dev[s] != nullptr;
+    return TGPU_OK;
+}
+
+int tgpu_batch_write_through(TgpuBatch *b, int group, void *host) {
+    if (!b || group < 0 || group >= b->nseg) return fail(TGPU_ERR_ARG, "bad write-through");
+    uint32_t *dev = nullptr;
+    if (host) {
+        dev = static_cast<uint32_t *>(pinned_device_ptr(host));
+        if (!dev) return fail(TGPU_ERR_ARG, "write-through needs page-locked host records");
+        if (!b->d_wt) CK(cudaMalloc(&b->d_wt, sizeof(uint32_t *) * (size_t)b->nseg));
+    }
+    if (dev == b->wt_dev[group]) return TGPU_OK;
+    b->wt_dev[group] = dev;
+    b->wt_done[group] = 0;
+    // the kernels read the addresses from the device array when they run (captured steps
+    // stay valid); stream-ordered before the next step
+    if (b->d_wt)
+        CK(cudaMemcpyAsync(b->d_wt, b->wt_dev.data(), sizeof(uint32_t *) * (size_t)b->nseg, cudaMemcpyHostToDevice,
+                           b->st));
     return TGPU_OK;
 }
 
@@ -1005,16 +1076,14 @@ int tgpu_batch_fetch(TgpuBatch *b, int group, void *host) {
     const SegmentSpec &sp = b->specs[group];
     if (!sp.count) return TGPU_OK;
     uint32_t *pinned = static_cast<uint32_t *>(pinned_device_ptr(host));
+    if (b->wt_done[group] && pinned == b->wt_dev[group]) {
+        // the last run wrote these records through already
+        CK(cudaStreamSynchronize(b->st));
+        return TGPU_OK;
+    }
     uint32_t *aos = pinned ? pinned : b->d_aos + (size_t)sp.begin * (b->m->agent_bytes / 4);
     PassIO io = make_io(b, nullptr, false, sp.begin);
-    // state batches: accumulators are visible when no act pass consumed them
-    uint32_t program = (uint32_t)b->program;
-    if (!b->state_passes.empty()) {
-        program = 0u;
-        for (const auto &p : b->state_passes)
-            if (!p.pass.is_see) program = 0xFFFFFFFFu;
-    }
-    b->m->unpack(aos, sp.count, io, program, b->st);
+    b->m->unpack(aos, sp.count, io, unpack_program(b), b->st);
     CK(cudaGetLastError());
     if (!pinned)
         CK(cudaMemcpyAsync(host, aos, (size_t)sp.count * b->m->agent_bytes, cudaMemcpyDeviceToHost, b->st));

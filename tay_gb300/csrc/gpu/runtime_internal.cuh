@@ -87,6 +87,13 @@ struct TgpuBatch {
     BoxAcc *d_extent = nullptr;          // pushed extent of one group
     uint32_t hit_masks = 0;              // see walk: hit masks (row order)
     std::map<uint64_t, cudaGraphExec_t> graphs;
+
+    // Write-through fetch: per segment, the device address of page-locked host records
+    // that the last step of a run fills as its final pass finishes (or null), the same
+    // array on the device, and the segments whose host copy the last run made current.
+    std::vector<uint32_t *> wt_dev;
+    uint32_t **d_wt = nullptr;
+    std::vector<char> wt_done;
 };
 
 
@@ -94,7 +101,7 @@ namespace tgpu {
 
 // Runtime functions the adjoint module reuses.
 int prepare_specs(TgpuBatch *b);
-void enqueue_step(TgpuBatch *b, const StepEvents *E = nullptr);
+void enqueue_step(TgpuBatch *b, const StepEvents *E = nullptr, bool write_through = false);
 PassIO make_io(TgpuBatch *b, const KernelDesc *k, bool fused_see, uint32_t offset);
 SortLaunch sort_launch(TgpuBatch *b);
 int fail(int code, const char *fmt, ...);

@@ -19,6 +19,7 @@
 #pragma once
 
 #include <climits>
+#include <type_traits>
 
 #include "tgpu_internal.cuh"
 #include "tgpu_kernels.cuh"
@@ -307,9 +308,45 @@ TGPU_D void seer_cells(const float4 &sp, const float4 &smax, const float4 &r4, c
     axis_span((sp.z - r4.z) - sz, smax.z + r4.z, g.origin[2], g.inv_cs[2], g.dims[2], pad, lo[2], hi[2]);
 }
 
+// The record codec of pass P's model (P::Codec), or void when the pass declares none.
+template <class P, class = void>
+struct CodecOf {
+    using type = void;
+};
+template <class P>
+struct CodecOf<P, std::void_t<typename P::Codec>> {
+    using type = typename P::Codec;
+};
+
+// Write-through epilogue of a see CTA: its seers' finished records (the streams this
+// launch wrote, the others as they are) in the model's AoS layout, staged in shared
+// memory and stored to the segment's page-locked host records with 16-byte stores, so
+// the host link works while the rest of the pass runs.  Every thread of the CTA calls it.
+template <class C>
+TGPU_D void write_through_cta(const SeeLaunch &L, uint32_t *wt, uint32_t first, uint32_t seg_begin,
+                              uint32_t seg_end, uint32_t *sm) {
+    constexpr uint32_t W = C::kAgentBytes / 4;
+    PassIO wio = L.io;
+#pragma unroll
+    for (int c = 0; c < kMaxF4; ++c) wio.in_f4[c] = wio.out_f4[c];
+    const uint32_t cnt = min((uint32_t)kSeeThreads, seg_end - first);
+    if (threadIdx.x < cnt) C::unpack(sm + threadIdx.x * W, wio, first + threadIdx.x, L.wt_program);
+    __syncthreads();
+    uint32_t *dst = wt + (size_t)(first - seg_begin) * W;
+    const uint32_t words = cnt * W;
+    uint32_t w0 = 0;
+    if ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(sm);
+        uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+        for (uint32_t v = threadIdx.x; v < words / 4u; v += kSeeThreads) d4[v] = s4[v];
+        w0 = words & ~3u;
+    }
+    for (uint32_t w = w0 + threadIdx.x; w < words; w += kSeeThreads) dst[w] = sm[w];
+}
+
 }  // namespace see_detail
 
-template <class P>
+template <class P, bool kWrite = false>
 __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
     using namespace see_detail;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -514,6 +551,12 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
         uint32_t w = warp_sum_u(tested);
         if (lane == 0 && w) atomicAdd(L.telemetry, (unsigned long long)w);
     }
+    if constexpr (kWrite) {
+        using C = typename CodecOf<P>::type;
+        __shared__ __align__(16) uint32_t wt_sm[kSeeThreads * (C::kAgentBytes / 4)];
+        uint32_t *wt = L.wt[seg];
+        if (wt) write_through_cta<C>(L, wt, cta.y, S.begin, seg_end, wt_sm);
+    }
 }
 
 // See pass over a row-order table (kOrderRows): the agents of x-adjacent cells are
@@ -522,7 +565,7 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
 // ranges are nearly the same length and their candidate loads fall on neighbouring
 // addresses.  No staging; a warp whose union box is compact walks the union's row
 // ranges with the two-phase batches instead.
-template <class P, bool kStage = false>
+template <class P, bool kStage = false, bool kWrite = false>
 __global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
     using namespace see_detail;
     const uint2 cta = L.cta_table[L.cta_offset + blockIdx.x];
@@ -712,6 +755,12 @@ __global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
     if (L.telemetry) {
         uint32_t w = warp_sum_u(tested);
         if (lane == 0 && w) atomicAdd(L.telemetry, (unsigned long long)w);
+    }
+    if constexpr (kWrite) {
+        using C = typename CodecOf<P>::type;
+        __shared__ __align__(16) uint32_t wt_sm[kSeeThreads * (C::kAgentBytes / 4)];
+        uint32_t *wt = L.wt[seg];
+        if (wt) write_through_cta<C>(L, wt, cta.y, S.begin, seg_end, wt_sm);
     }
 }
 

@@ -69,6 +69,11 @@ struct SeeLaunch {
     // box, [4] warps whose lanes walked their own boxes
     unsigned long long *telemetry;
     PassIO io;
+    // write-through (the last pass of a run): per segment the device address of the
+    // page-locked host records its seers' finished records go to (null: none), and the
+    // model's unpack program
+    uint32_t *const *wt;
+    uint32_t wt_program;
 };
 
 struct ActLaunch {

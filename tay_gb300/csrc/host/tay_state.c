@@ -42,6 +42,8 @@ struct TayGroup {
     int host_dirty; /* host records changed since the last push */
     int host_stale; /* the device holds newer records than the host */
     int slot;       /* segment of the compiled batch, or -1 */
+    int read_since_run; /* tay_get_agent was called since the last run */
+    int write_through;  /* the batch writes this group's records to storage at each run's end */
 };
 
 struct TayPass {
@@ -130,6 +132,7 @@ static void release_batch(TayState *state) {
         state->groups[i].slot = -1;
         state->groups[i].host_dirty = 1;
         state->groups[i].host_stale = 0;
+        state->groups[i].write_through = 0;
     }
 }
 
@@ -281,6 +284,7 @@ unsigned tay_get_agent_count(TayState *state, TayGroup *group) {
 }
 
 void *tay_get_agent(TayState *state, TayGroup *group, int index) {
+    group->read_since_run = 1;
     if (!fetch_group(state, group)) return 0;
     return group->storage + (size_t)group->agent_size * (size_t)index;
 }
@@ -441,7 +445,10 @@ static int compile(TayState *state) {
         state->batch = 0;
         return 0;
     }
-    for (int s = 0; s < state->ngpu; ++s) state->groups[state->gpu_slots[s]].host_dirty = 1;
+    for (int s = 0; s < state->ngpu; ++s) {
+        state->groups[state->gpu_slots[s]].host_dirty = 1;
+        state->groups[state->gpu_slots[s]].write_through = 0;
+    }
     return 1;
 }
 
@@ -472,9 +479,22 @@ int tay_run(TayState *state, int steps) {
         rc = tgpu_batch_push(state->batch, s, g->storage);
         g->host_dirty = 0;
     }
+    /* A group the host read after its previous run is written through to its storage at
+     * the end of this one (the fetch overlaps the last pass); one it did not read stays on
+     * the device until tay_get_agent asks for it. */
+    for (int s = 0; s < state->ngpu && rc == TGPU_OK; ++s) {
+        TayGroup *g = state->groups + state->gpu_slots[s];
+        const int want = g->read_since_run && steps > 0;
+        g->read_since_run = 0;
+        if (want == g->write_through) continue;
+        g->write_through = tgpu_batch_write_through(state->batch, s, want ? g->storage : 0) == TGPU_OK && want;
+    }
     if (rc == TGPU_OK) rc = tgpu_batch_run(state->batch, steps);
     if (rc != TGPU_OK) return device_fail(state, rc);
-    for (int s = 0; s < state->ngpu; ++s) state->groups[state->gpu_slots[s]].host_stale = 1;
+    for (int s = 0; s < state->ngpu; ++s) {
+        TayGroup *g = state->groups + state->gpu_slots[s];
+        g->host_stale = !(g->write_through && steps > 0);
+    }
     double t = now_s() - t0;
     state->ms_per_step = steps ? t / (double)steps * 1000.0 : 0.0;
     state->device_ms = tgpu_batch_last_device_ms(state->batch);
@@ -581,6 +601,10 @@ int tay_run_batch(TayState **states, int count, int steps) {
     if (!b) return 0;
     double t0 = now_s();
     int rc = push_all(b, states, count);
+    /* every state is fetched after the run: write its records through where its storage
+     * is page-locked (the fetch then only waits) */
+    for (int i = 0; i < count && rc == TGPU_OK; ++i)
+        tgpu_batch_write_through(b, i, states[i]->groups[states[i]->gpu_group].storage);
     if (rc == TGPU_OK) rc = tgpu_batch_run(b, steps);
     if (rc == TGPU_OK) rc = fetch_all(b, states, count);
     if (rc != TGPU_OK) {

@@ -160,18 +160,35 @@ def make_state(setup: Setup, recs: np.ndarray):
     return st, g
 
 
-def run(setup: Setup, recs: np.ndarray, steps: int):
+def _host_loop(st, gs, dtype, steps, host_loop):
+    """`steps` steps through the C API: one run (host_loop None), or one run per step with
+    the host reading every group after it ("read") and also marking them changed before
+    it ("e2e": every step pushes and fetches)."""
+    if host_loop is None:
+        st.run(steps)
+        return
+    for _ in range(steps):
+        if host_loop == "e2e":
+            for g in gs:
+                st.mark_changed(g)
+        st.run(1)
+        for g in gs:
+            st.agents(g, dtype)
+
+
+def run(setup: Setup, recs: np.ndarray, steps: int, host_loop=None):
     """Runs `steps` steps through the C API; returns the records ordered by id."""
     st, g = make_state(setup, recs)
     st.start()
-    st.run(steps)
+    _host_loop(st, [g], setup.dtype, steps, host_loop)
     out = by_id(st.agents(g, setup.dtype))
     st.end()
     st.close()
     return out
 
 
-def run_groups(dtype, funcs, groups, passes, see_ctx, act_ctx, radius, part, steps, mb=8, is_point=True):
+def run_groups(dtype, funcs, groups, passes, see_ctx, act_ctx, radius, part, steps, mb=8, is_point=True,
+               host_loop=None):
     """A state of several groups of one model mixed by its passes, through the C API.
     `funcs` = (see func name, act func name); `groups` = record arrays (id order);
     `passes` = ("see", seer, seen, self_see) / ("act", group) tuples in registration
@@ -192,7 +209,7 @@ def run_groups(dtype, funcs, groups, passes, see_ctx, act_ctx, radius, part, ste
     for g, recs in zip(gs, groups):
         st.commit(g, recs)
     st.start()
-    st.run(steps)
+    _host_loop(st, gs, dtype, steps, host_loop)
     out = [by_id(st.agents(g, dtype)) for g in gs]
     st.end()
     st.close()

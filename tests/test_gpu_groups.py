@@ -165,3 +165,30 @@ def test_single_group_pass_list_outside_the_programs(gpu, port):
     o = _oracle(port, O.MODEL_TEST, recs, passes, see, act, 50.0, 4)
     assert np.array_equal(g[0]["p"][:, :3], o[0]["p"][:, :3])
     assert normwise(g[0]["f_buffer"][:, :3], o[0]["f_buffer"][:, :3]) < 1e-3
+
+
+@pytest.mark.parametrize("host_loop", ["read", "e2e"])
+def test_write_through_equals_one_run(gpu, host_loop):
+    """A host that reads its agents after every run gets them written through by the run's
+    last pass (chunked fused see+act for one group, after the step for a state batch);
+    with or without pushing them back each step, the records equal one uninterrupted
+    run's, bit for bit."""
+    ps = W.basic_points(30000, seed=47)
+    recs = M.records(M.TEST_RECORD, ps.p, ps.v)
+    setup = M.test_setup()
+    a = M.run(setup, recs, 6)
+    b = M.run(setup, recs, 6, host_loop=host_loop)
+    assert a.tobytes() == b.tobytes()
+    bp = W.boids_points(40000, seed=48, clusters=4, side=300.0)
+    brecs = M.records(M.BOIDS_RECORD, bp.p, bp.v)
+    bsetup = M.boids_setup()
+    a = M.run(bsetup, brecs, 6)
+    b = M.run(bsetup, brecs, 6, host_loop=host_loop)
+    assert a.tobytes() == b.tobytes()
+    groups = _test_groups()
+    see, act = M.test_contexts()
+    a = _gpu(O.MODEL_TEST, groups, COMBO_FULL, see, act, 50.0, 4)
+    funcs, dtype = FUNCS[O.MODEL_TEST]
+    b = M.run_groups(dtype, funcs, groups, COMBO_FULL, see, act, 50.0, 50.0, 4, host_loop=host_loop)
+    for x, y in zip(a, b):
+        assert x.tobytes() == y.tobytes()
