@@ -26,6 +26,9 @@ DEFAULT_CANDIDATES = (
        for cm in (1.0, 0.5, 0.34, 0.25) for xf in (1.0, 0.5, 0.25)]
     + [{"cell_multiple": 1.0, "union_factor": 2, "stage": 0, "cell_order": 0, "x_cell_factor": 1.0},
        {"cell_multiple": 1.0, "union_factor": 2, "stage": 1, "cell_order": 0, "x_cell_factor": 1.0}]
+    # row walk with the CTA's union rows bulk-copied (TMA) into shared memory
+    + [{"cell_multiple": cm, "union_factor": 1, "stage": 1, "cell_order": 1, "x_cell_factor": 0.5}
+       for cm in (1.0, 0.5)]
 )
 
 
