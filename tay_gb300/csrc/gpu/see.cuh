@@ -99,21 +99,6 @@ struct GlobalSeen {
     TGPU_D float4 f4(int k, uint32_t j) const { return __ldg(s[k] + j); }
 };
 
-// Largest rounding error, in cells, of a cell coordinate computed as
-// floor((p - origin) * inv_cs): a few ulps of the largest coordinate magnitude plus the
-// relative error of the multiply on coordinates up to 1024 cells.
-TGPU_D float grid_pad(const Grid &g, const SegmentSpec &s, const BoxAcc &b) {
-    float m = 0.0f, csmin = g.cs[0];
-    for (int a = 0; a < 3; ++a) {
-        float lo = s.fixed_box ? s.box_min[a] : ordered_to_float(b.lo[a]);
-        float hi = s.fixed_box ? s.box_max[a] : ordered_to_float(b.hi[a]);
-        m = fmaxf(m, fmaxf(fabsf(lo), fabsf(hi)));
-        csmin = fminf(csmin, g.cs[a]);
-    }
-    float ulp = m * 1.1920929e-7f;  // 2^-23
-    return fmaxf(1.0f / 512.0f, 16.0f * ulp / csmin + 1024.0f * 4.0f * 1.1920929e-7f);
-}
-
 // Loads a candidate position from shared memory (staged) or through the read-only cache.
 TGPU_D float4 load_pos(const float4 *src, uint32_t j, bool global) {
     return global ? __ldg(src + j) : src[j];

@@ -66,7 +66,10 @@ __global__ void __launch_bounds__(kSortThreads) bbox_kernel(const SegmentSpec *_
     uint32_t lo[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
     uint32_t hi[3] = {0u, 0u, 0u};
     uint32_t sz[3] = {0u, 0u, 0u};
-    for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads) {
+#pragma unroll
+    for (uint32_t k = 0; k < kSortTile / kSortThreads; ++k) {  // every load of the thread in flight
+        const uint32_t i = beg + k * kSortThreads + threadIdx.x;
+        if (i >= end) continue;
         float4 p = pos[i];
         float c[3] = {p.x, p.y, p.z};
         for (int a = 0; a < 3; ++a) {
@@ -172,14 +175,26 @@ __global__ void __launch_bounds__(kSortThreads) keys_hist_kernel(const SegmentSp
     const uint32_t end = min(beg + (uint32_t)kSortTile, s.begin + s.count);
     for (int p = 0; p < passes; ++p) h[p][threadIdx.x] = 0;
     __syncthreads();
-    for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads) {
+    const uint32_t lane = lane_id();
+#pragma unroll
+    for (uint32_t r = 0; r < kSortTile / kSortThreads; ++r) {  // every load of the thread in flight
+        const uint32_t i = beg + r * kSortThreads + threadIdx.x;
+        const bool live = i < end;
+        const uint32_t m = __ballot_sync(0xffffffffu, live);  // warp-uniform: i grows with the lane
+        if (!live) continue;
         float4 q = pos[i];
         uint32_t cx = (uint32_t)cell_coord(q.x, g.origin[0], g.inv_cs[0], g.dims[0]);
         uint32_t cy = (uint32_t)cell_coord(q.y, g.origin[1], g.inv_cs[1], g.dims[1]);
         uint32_t cz = (uint32_t)cell_coord(q.z, g.origin[2], g.inv_cs[2], g.dims[2]);
         uint32_t k = cell_key(s, cx, cy, cz);
         keys[i] = k;
-        for (int p = 0; p < passes; ++p) atomicAdd(&h[p][(k >> (8 * p)) & digit_mask(key_bits, p)], 1u);
+        // A tile's agents are neighbours in space (last step's order), so most share their
+        // upper digits: one shared atomic per distinct digit of the warp, not per agent.
+        for (int p = 0; p < passes; ++p) {
+            const uint32_t d = (k >> (8 * p)) & digit_mask(key_bits, p);
+            const uint32_t peers = __match_any_sync(m, d);
+            if (lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&h[p][d], (uint32_t)__popc(peers));
+        }
     }
     __syncthreads();
     for (int p = 0; p < passes; ++p) {
@@ -267,7 +282,13 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(const SegmentSpe
         const uint32_t i = beg + warp * (kSortTile / kWarps) + r * 32 + lane;
         key[r] = i < end ? keys_in[i] : 0u;
         dig[r] = i < end ? ((key[r] >> shift) & mask) : 256u;
-        if (dig[r] < 256u) atomicAdd(&tile_hist[dig[r]], 1u);
+    }
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+        // one shared atomic per distinct digit of the warp (a tile's keys share their upper
+        // digits, which per-key atomics would serialize on one address)
+        const uint32_t peers = __match_any_sync(0xffffffffu, dig[r]);
+        if (dig[r] < 256u && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&tile_hist[dig[r]], (uint32_t)__popc(peers));
     }
     __syncthreads();
     volatile uint32_t *mine = look + ((size_t)pass * gridDim.x + tile) * 256u + threadIdx.x;
@@ -379,10 +400,7 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(const SegmentSpe
 
 // ------------------------------------------------------------------ cell table
 
-TGPU_D uint32_t table_index(const Grid &g, uint32_t key) {
-    uint32_t x = compact10(key), y = compact10(key >> 1), z = compact10(key >> 2);
-    return (z * (uint32_t)g.dims[1] + y) * (uint32_t)g.dims[0] + x;
-}
+constexpr uint32_t kTableBlocks = kSortTile / kSortThreads;
 
 // Records {first, end} of every run of equal keys at the run's cell (write_runs = 1), or
 // clears those entries again (write_runs = 0) before the next sort.  Row order: the first
@@ -394,70 +412,83 @@ __global__ void __launch_bounds__(kSortThreads) cell_table_kernel(const SegmentS
                                                                   const BoxAcc *__restrict__ box,
                                                                   const uint32_t *__restrict__ keys,
                                                                   uint2 *__restrict__ table, int write_runs) {
-    const uint32_t seg = tile_seg[blockIdx.x];
+    // kTableBlocks blocks per radix tile, one key per thread; the segment's grid is
+    // derived once per block
+    __shared__ uint32_t s_dx, s_dy;
+    const uint32_t tile = blockIdx.x / kTableBlocks, part = blockIdx.x % kTableBlocks;
+    const uint32_t seg = tile_seg[tile];
     const SegmentSpec s = specs[seg];
-    const Grid g = segment_grid(s, box[seg]);
-    const uint32_t t = blockIdx.x - s.tile_begin;
-    const uint32_t beg = s.begin + t * kSortTile;
+    if (threadIdx.x == 0) {
+        const Grid g = segment_grid(s, box[seg]);
+        s_dx = (uint32_t)g.dims[0];
+        s_dy = (uint32_t)g.dims[1];
+    }
+    __syncthreads();
+    const uint32_t dx = s_dx, dy = s_dy;
+    const uint32_t beg = s.begin + (tile - s.tile_begin) * kSortTile + part * kSortThreads;
     const uint32_t seg_end = s.begin + s.count;
-    const uint32_t end = min(beg + (uint32_t)kSortTile, seg_end);
+    const uint32_t end = min(beg + (uint32_t)kSortThreads, seg_end);
+    const uint32_t i = beg + threadIdx.x;
     if (s.order == kOrderRows) {
         // The first agent of a row writes its header's x_first / first, the last agent
         // x_last / end, and the first agent of every other cell the start entries of the
-        // cells after the previous occupied one up to its own; the clear zeroes headers.
-        // Gap fills are written by the warp together, 32 consecutive entries per store.
+        // cells after the previous occupied one up to its own; the clear zeroes headers
+        // (entries are read only inside a row's occupied span, where every step writes them).
+        // A gap of up to kLaneGap entries is written by its own lane; longer ones by the
+        // warp together, 32 consecutive entries per store.
+        constexpr uint32_t kLaneGap = 32;
         uint4 *hdr = reinterpret_cast<uint4 *>(table + s.table_base);
         uint32_t *words = reinterpret_cast<uint32_t *>(table + s.table_base) + row_entry_word(s);
         const uint32_t b = axis_bits(s);
         const uint32_t xmask = (1u << b) - 1u;
-        const uint32_t dx = (uint32_t)g.dims[0];
         const uint32_t lane = threadIdx.x & 31u;
-        for (uint32_t base = beg; base < end; base += kSortThreads) {
-            const uint32_t i = base + threadIdx.x;
-            uint32_t off = 0u, len = 0u;
-            if (i < end) {
-                const uint32_t k = keys[i];
-                const uint32_t row = k >> b, x = k & xmask;
-                const bool row_first = (i == s.begin) || (keys[i - 1] >> b) != row;
-                const bool row_last = (i + 1 == seg_end) || (keys[i + 1] >> b) != row;
-                const uint32_t y = compact2_10(row), z = compact2_10(row >> 1);
-                const uint32_t r = z * (uint32_t)g.dims[1] + y;
-                if (!write_runs) {
-                    if (row_first) hdr[r] = make_uint4(0u, 0u, 0u, 0u);
-                } else {
-                    uint32_t *h = reinterpret_cast<uint32_t *>(hdr + r);
-                    if (row_first) {
-                        h[0] = x;
-                        h[2] = i;
-                    } else if (keys[i - 1] != k) {
-                        const uint32_t x0 = (keys[i - 1] & xmask) + 1u;
-                        off = r * dx + x0;
-                        len = x + 1u - x0;
-                    }
-                    if (row_last) {
-                        h[1] = x;
-                        h[3] = i + 1u;
+        uint32_t off = 0u, len = 0u;
+        if (i < end) {
+            const uint32_t k = keys[i];
+            const uint32_t row = k >> b, x = k & xmask;
+            const uint32_t kp = i == s.begin ? ~k : keys[i - 1];
+            const bool row_first = (kp >> b) != row;
+            const bool row_last = (i + 1 == seg_end) || (keys[i + 1] >> b) != row;
+            const uint32_t r = compact2_10(row >> 1) * dy + compact2_10(row);
+            if (!write_runs) {
+                if (row_first) hdr[r] = make_uint4(0u, 0u, 0u, 0u);
+            } else {
+                uint32_t *h = reinterpret_cast<uint32_t *>(hdr + r);
+                if (row_first) {
+                    h[0] = x;
+                    h[2] = i;
+                } else if (kp != k) {
+                    const uint32_t x0 = (kp & xmask) + 1u;
+                    off = r * dx + x0;
+                    len = x + 1u - x0;
+                    if (len <= kLaneGap) {
+                        for (uint32_t c = 0; c < len; ++c) words[off + c] = i;
+                        len = 0u;
                     }
                 }
+                if (row_last) {
+                    h[1] = x;
+                    h[3] = i + 1u;
+                }
             }
-            uint32_t m = __ballot_sync(0xffffffffu, len > 0u);
-            while (m) {
-                const int l = __ffs(m) - 1;
-                m &= m - 1u;
-                const uint32_t o = __shfl_sync(0xffffffffu, off, l);
-                const uint32_t n = __shfl_sync(0xffffffffu, len, l);
-                const uint32_t v = __shfl_sync(0xffffffffu, i, l);
-                for (uint32_t c = lane; c < n; c += 32u) words[o + c] = v;
-            }
+        }
+        uint32_t m = __ballot_sync(0xffffffffu, len > 0u);
+        while (m) {
+            const int l = __ffs(m) - 1;
+            m &= m - 1u;
+            const uint32_t o = __shfl_sync(0xffffffffu, off, l);
+            const uint32_t n = __shfl_sync(0xffffffffu, len, l);
+            const uint32_t v = __shfl_sync(0xffffffffu, i, l);
+            for (uint32_t c = lane; c < n; c += 32u) words[o + c] = v;
         }
         return;
     }
-    for (uint32_t i = beg + threadIdx.x; i < end; i += kSortThreads) {
+    if (i < end) {
         const uint32_t k = keys[i];
         const bool first = (i == s.begin) || keys[i - 1] != k;
         const bool last = (i + 1 == seg_end) || keys[i + 1] != k;
-        if (!first && !last) continue;
-        uint2 *e = table + s.table_base + table_index(g, k);
+        if (!first && !last) return;
+        uint2 *e = table + s.table_base + ((compact10(k >> 2) * dy + compact10(k >> 1)) * dx + compact10(k));
         if (write_runs) {
             if (first) e->x = i;
             if (last) e->y = i + 1;
@@ -583,7 +614,8 @@ cudaError_t selftest_sort_wait(uint32_t *err_host) {
 }
 
 void launch_cell_table(const SortLaunch &L, const uint32_t *sorted_keys, int write_runs, cudaStream_t st) {
-    cell_table_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.box, sorted_keys, L.table, write_runs);
+    cell_table_kernel<<<L.tiles * kTableBlocks, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.box, sorted_keys, L.table,
+                                                                     write_runs);
 }
 
 void launch_gather(uint32_t n, const uint32_t *perm, const GatherSet &set, cudaStream_t st) {

@@ -187,3 +187,30 @@ def test_staged_rows_bit_identical_full_size(gpu, tuning):
     assert p0 == p1
     assert r0.tobytes() == r1.tobytes()
     assert t1["staged_ctas"] > 0
+
+
+@pytest.mark.parametrize("tuning", [
+    {"cell_order": 1}, {"cell_order": 1, "x_cell_factor": 0.25}, {"cell_order": 1, "cell_multiple": 0.5},
+    {"cell_order": 1, "union_factor": 4}, {"cell_order": 1, "stage": 1, "x_cell_factor": 0.25},
+    {"cell_order": 1, "hit_masks": 1, "x_cell_factor": 0.5},
+])
+def test_rows_with_long_gaps_match_oracle(gpu, port, tuning):
+    """Agents in two slabs at the ends of x, so every occupied row has a gap of dozens of
+    cells (written by the warp together, short gaps by their own lane): the lookups of a
+    seer's own range, a warp's union and a CTA's staged union must find exactly the
+    oracle's neighbours."""
+    ps = W.basic_points(20000, seed=17)
+    p = ps.p.copy()
+    x = p[:, 0] / 1000.0 * 60.0
+    p[:, 0] = np.where(np.arange(p.shape[0]) % 2 == 0, x, 940.0 + x)
+    recs = M.records(M.TEST_RECORD, p, ps.v)
+    setup = M.test_setup(passes=("agent_see",))
+    o = oracle_run(port, O.MODEL_TEST, setup, recs, 1)
+    try:
+        api.set_tuning(**tuning)
+        g = M.run(setup, recs, 1)
+    finally:
+        api.set_tuning()
+    assert g["b_buffer_count"].sum() > 0
+    assert np.array_equal(g["b_buffer_count"], o["b_buffer_count"])
+    assert normwise(g["b_buffer"][:, :3], o["b_buffer"][:, :3]) < TOL_1STEP
