@@ -186,7 +186,7 @@ CONFIG = {"workload": "boids_1M_zgrid", "agents": N_BOIDS, "radius": RADIUS, "ce
 
 
 def batched_workload(states):
-    """BASELINE batched boids: `states` states, N log-uniform in [1000, 65536], box side
+    """The batched boids workload: `states` states, N log-uniform in [1000, 65536], box side
     (125 N)^(1/3), radius U[5, 20] (cell = radius), same boids rules."""
     from tay_gb300 import models as M
     from tay_gb300 import workloads as W
@@ -245,7 +245,7 @@ def batched_vs_plain(states, steps, tune=True):
 
 
 def sph_leg(steps, tune=True):
-    """BASELINE SPH dam break: 64x128x64 = 524,288 particles on a 0.01 lattice in a
+    """The SPH dam break: 64x128x64 = 524,288 particles on a 0.01 lattice in a
     2.0 x 1.5 x 0.8 tank, h 0.02 (see radius 2h), four passes per step."""
     from tay_gb300 import api, autotune
     from tay_gb300 import models as M
@@ -274,7 +274,7 @@ def sph_leg(steps, tune=True):
 
 
 def adjoint_leg(steps=200, every=20, instances=32, keep=1, tune=True):
-    """BASELINE differentiable SPH calibration: `instances` SPH instances of 20,480
+    """The differentiable SPH calibration: `instances` SPH instances of 20,480
     particles (32x40x16 lattice, spacing 0.01, h 0.02), a `steps`-step rollout, loss = MSE
     of final positions against a target rollout (alpha 0.08, c0 22, same initial state);
     gradients w.r.t. (alpha, c0) and initial velocities from the adjoint with checkpoints
@@ -320,18 +320,21 @@ def adjoint_leg(steps=200, every=20, instances=32, keep=1, tune=True):
             "dloss_dalpha_mean": float(dp[:, 0].mean()), "dloss_dc0_mean": float(dp[:, 1].mean())}
 
 
-def features_leg(setup, recs, steps=20):
+def features_leg(setup, recs, tuning, steps=20):
     """The hot path's other shapes (the rows after the headline), each timed through the C
-    API: a two-group state with the combination test's passes, the device-resident loop
-    (tay_run(state, 1) with no host copies) beside the e2e loop, a 2-D space, a fixed space
-    box, and non-point (box) agents.  Device time per step from the engine's events."""
+    API with the headline's tuning: a two-group state with the combination test's passes,
+    the device-resident loop (tay_run(state, 1) with no host copies) beside the e2e loop, a
+    2-D space, a fixed space box, and non-point (box) agents.  Device time per step from
+    the engine's events."""
     import time
 
     from tay_gb300 import api
     from tay_gb300 import models as M
     from tay_gb300 import workloads as W
 
-    out = {}
+    api.set_tuning()
+    api.set_tuning(**tuning)
+    out = {"tuning": dict(tuning)}
     see, act = M.test_contexts(radius=10.0, hi=500.0)
 
     # two groups of 262,144, see a->a, a->b, b->b, b->a, act a, act b (test/test_combo.c)
@@ -421,6 +424,7 @@ def features_leg(setup, recs, steps=20):
                          "pair_interactions_per_s": st.pairs() / steps / (dev / 1000.0)}
     st.end()
     st.close()
+    api.set_tuning()
     return out
 
 
@@ -554,7 +558,7 @@ def run_gb300(args, rank, world, D):
             "metric": "pair-interactions/s", "value": all_pairs / secs, "unit": "pair-interactions/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded SplitMix64, BASELINE boids shape)",
+            "data": "synthetic (seeded SplitMix64, 64 Gaussian clusters of boids)",
             "config": dict(CONFIG, l2="flushed between timed steps", parallelism=f"replicas{world}"),
             "steps_per_s": args.steps / secs,
             "pairs_per_step": all_pairs / world / args.steps,
@@ -587,7 +591,7 @@ def run_gb300(args, rank, world, D):
             line["adjoint_keep1"] = adjoint_leg(keep=1, tune=tune)
             line["adjoint_record_all"] = adjoint_leg(every=0, tune=tune)
         if args.features:
-            line["features"] = features_leg(setup, recs)
+            line["features"] = features_leg(setup, recs, line["tuning"])
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(setup, recs, args.cpu_steps)
         print(json.dumps(line), flush=True)

@@ -172,7 +172,7 @@ unsigned tay_get_agent_count(TayState *state, TayGroup *group);
  * tay_run pushes them. */
 void tay_mark_agents_changed(TayState *state, TayGroup *group);
 
-/* NEW: differentiable SPH rollouts (the benchmark spec's hand-written adjoint; no
+/* NEW: differentiable SPH rollouts (a hand-written adjoint; no
  * counterpart in the reference).  tay_run_recorded advances `count` states (each one
  * TAY_GPU_Z_GRID group running sph_density, sph_pressure, sph_force, sph_integrate) by
  * `steps` steps like tay_run_batch, recording what the adjoint needs: with

@@ -119,9 +119,10 @@ int tgpu_batch_fetch(TgpuBatch *batch, int group, void *host_records);
 /* Write-through fetch of group `group` into page-locked `host_records` (from
  * tgpu_host_alloc or cudaHostAlloc; NULL turns it off; pageable memory is refused with
  * TGPU_ERR_ARG): the last step of every following run writes the group's records there
- * as its final pass finishes, chunk by chunk on a second stream, overlapping the host
- * link with the rest of the pass; a tgpu_batch_fetch into the same buffer after such a
- * run only waits.  Replaces the fetch after every run of the reference's OpenCL path
+ * from its final see pass, each CTA storing its seers' records as it ends, so the host
+ * link overlaps the rest of the pass (after the step when the last pass is an act or
+ * covers one group of a state); a tgpu_batch_fetch into the same buffer after such a run
+ * only waits.  Replaces the fetch after every run of the reference's OpenCL path
  * (tay/ocl.c:261-272) for hosts that read their agents after each run. */
 int tgpu_batch_write_through(TgpuBatch *batch, int group, void *host_records);
 
@@ -196,7 +197,7 @@ typedef struct TgpuTuning {
 void tgpu_set_tuning(const TgpuTuning *tuning);  /* NULL restores the defaults */
 void tgpu_get_tuning(TgpuTuning *tuning);
 
-/* Adjoint of SPH rollouts (spec: hand-written adjoint; no counterpart in the
+/* Adjoint of SPH rollouts (a hand-written reverse mode; no counterpart in the
  * reference).  For a batch running the full SPH sequence (sph_density, sph_pressure,
  * sph_force, sph_integrate):
  *   tgpu_adjoint_create   prepares a rollout of `steps` steps; checkpoint_every = k > 0

@@ -53,9 +53,11 @@ TgpuTuning default_tuning() {
     t.cell_multiple = 1.0f;
     t.union_factor = 1;
     t.use_graphs = 1;
-    t.cell_order = 0;
+    // row order with x cells of half the y / z cell: the autotuner's choice for every
+    // workload measured on GB300 (boids, SPH, batched states)
+    t.cell_order = 1;
     t.hit_masks = 0;
-    t.x_cell_factor = 1.0f;
+    t.x_cell_factor = 0.5f;
     return t;
 }
 TgpuTuning g_tuning = default_tuning();

@@ -36,7 +36,7 @@ def _see_counts(recs, radius=50.0, part=50.0, tuning=None):
         api.set_tuning()
 
 
-@pytest.mark.parametrize("tuning", [None, {"cell_order": 1}])
+@pytest.mark.parametrize("tuning", [{"cell_order": 0}, None])
 def test_single_agent(gpu, port, tuning):
     recs = _test_records(np.array([[10.0, 20.0, 30.0]], np.float32), np.array([[1.0, 0.0, 0.0]], np.float32))
     g, _ = _see_counts(recs, tuning=tuning)
@@ -46,7 +46,7 @@ def test_single_agent(gpu, port, tuning):
     assert np.allclose(out["p"][0, :3], [13.0, 20.0, 30.0])
 
 
-@pytest.mark.parametrize("tuning", [None, {"cell_order": 1}])
+@pytest.mark.parametrize("tuning", [{"cell_order": 0}, None])
 def test_coincident_agents(gpu, port, tuning):
     p = np.zeros((700, 3), np.float32) + np.float32(123.25)
     recs = _test_records(p)
@@ -55,7 +55,7 @@ def test_coincident_agents(gpu, port, tuning):
     assert np.all(g["b_buffer"][:, :3] == 0.0)
 
 
-@pytest.mark.parametrize("tuning", [None, {"cell_order": 1}, {"cell_order": 1, "x_cell_factor": 0.25}])
+@pytest.mark.parametrize("tuning", [{"cell_order": 0}, None, {"cell_order": 1, "x_cell_factor": 0.25}])
 def test_neighbours_exactly_at_the_radius(gpu, port, tuning):
     """A lattice with spacing equal to the radius: the 26 lattice neighbours are at |d| = r
     on every axis they differ in, and the inclusive test counts them."""
@@ -79,7 +79,7 @@ def test_flat_axis(gpu, port):
     assert np.array_equal(g["b_buffer_count"], o["b_buffer_count"])
 
 
-@pytest.mark.parametrize("tuning", [None, {"cell_order": 1}])
+@pytest.mark.parametrize("tuning", [{"cell_order": 0}, None])
 def test_far_from_origin(gpu, port, tuning):
     """Coordinates near 1e6 with radius 5: float spacing there is 1/16, so cell
     coordinates round; the neighbour sets must still equal the oracle's."""

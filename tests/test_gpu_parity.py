@@ -112,7 +112,9 @@ def test_batch_matches_individual_runs(gpu):
     {"cell_order": 1, "hit_masks": 1}, {"cell_order": 1, "hit_masks": 1, "cell_multiple": 0.5},
     {"cell_order": 1, "x_cell_factor": 0.25}, {"cell_order": 1, "cell_multiple": 0.5, "x_cell_factor": 0.5},
     {"cell_order": 1, "stage": 1}, {"cell_order": 1, "stage": 1, "x_cell_factor": 0.5, "stage_cap": 256},
-    {"union_factor": 2}, {"stage": 1}, {"cell_multiple": 0.5}, {"cell_multiple": 1.5},
+    {"cell_order": 1, "x_cell_factor": 1.0},
+    {"cell_order": 0}, {"cell_order": 0, "union_factor": 2}, {"cell_order": 0, "stage": 1},
+    {"cell_order": 0, "cell_multiple": 0.5}, {"cell_order": 0, "cell_multiple": 1.5},
 ])
 def test_walk_tunings_match_oracle(gpu, port, tuning):
     """Every cell order, cell size and see walk gives the oracle's neighbour counts bit for
