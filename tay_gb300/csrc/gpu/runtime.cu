@@ -276,7 +276,7 @@ int tgpu::prepare_specs(TgpuBatch *b) {
     CK(cudaMemcpyAsync(b->d_specs, b->specs.data(), sizeof(SegmentSpec) * b->nseg, cudaMemcpyHostToDevice, b->st));
     for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
     b->graphs.clear();
-    const int passes = (int)((b->key_bits + 7) / 8);
+    const int passes = sort_passes(b->key_bits);
     b->launches_per_step = 2 + passes * 5 + 1 + 1 + (int)b->runs.size() + 1;
     return TGPU_OK;
 }

@@ -33,9 +33,11 @@ TGPU_D T warp_max(T v) {
     return v;
 }
 
+// Mask of pass `pass`'s digit of D-bit digits (the last pass may have fewer bits).
+template <int D>
 TGPU_D uint32_t digit_mask(uint32_t key_bits, int pass) {
-    const int bits = min(8, (int)key_bits - 8 * pass);
-    return bits >= 8 ? 0xFFu : ((1u << bits) - 1u);
+    const int bits = min(D, (int)key_bits - D * pass);
+    return bits >= D ? (1u << D) - 1u : ((1u << bits) - 1u);
 }
 
 TGPU_D uint32_t warp_incl_scan(uint32_t v) {
@@ -156,9 +158,10 @@ TGPU_D uint32_t count_index(const SegmentSpec &s, uint32_t digit, uint32_t local
 }
 
 // One pass over the positions: the grid from the box, the cell key of every agent, and
-// per-segment histograms of every 8-bit digit of the keys (order-independent, so all
+// per-segment histograms of every D-bit digit of the keys (order-independent, so all
 // passes' digit offsets are known before the first scatter).  hist layout:
-// [segment][pass][256].
+// [segment][pass][kMaxRadix].
+template <int D>
 __global__ void __launch_bounds__(kSortThreads) keys_hist_kernel(const SegmentSpec *__restrict__ specs,
                                                                  const uint32_t *__restrict__ tile_seg,
                                                                  const BoxAcc *__restrict__ box,
@@ -166,14 +169,16 @@ __global__ void __launch_bounds__(kSortThreads) keys_hist_kernel(const SegmentSp
                                                                  uint32_t *__restrict__ keys,
                                                                  uint32_t *__restrict__ hist, int passes,
                                                                  uint32_t key_bits) {
-    __shared__ uint32_t h[kMaxSortPasses][256];
+    constexpr uint32_t R = 1u << D;
+    __shared__ uint32_t h[kMaxSortPasses][R];
     const uint32_t seg = tile_seg[blockIdx.x];
     const SegmentSpec s = specs[seg];
     const Grid g = segment_grid(s, box[seg]);
     const uint32_t t = blockIdx.x - s.tile_begin;
     const uint32_t beg = s.begin + t * kSortTile;
     const uint32_t end = min(beg + (uint32_t)kSortTile, s.begin + s.count);
-    for (int p = 0; p < passes; ++p) h[p][threadIdx.x] = 0;
+    for (int p = 0; p < passes; ++p)
+        for (uint32_t d = threadIdx.x; d < R; d += kSortThreads) h[p][d] = 0;
     __syncthreads();
     const uint32_t lane = lane_id();
 #pragma unroll
@@ -191,40 +196,52 @@ __global__ void __launch_bounds__(kSortThreads) keys_hist_kernel(const SegmentSp
         // A tile's agents are neighbours in space (last step's order), so most share their
         // upper digits: one shared atomic per distinct digit of the warp, not per agent.
         for (int p = 0; p < passes; ++p) {
-            const uint32_t d = (k >> (8 * p)) & digit_mask(key_bits, p);
+            const uint32_t d = (k >> (D * p)) & digit_mask<D>(key_bits, p);
             const uint32_t peers = __match_any_sync(m, d);
             if (lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&h[p][d], (uint32_t)__popc(peers));
         }
     }
     __syncthreads();
-    for (int p = 0; p < passes; ++p) {
-        const uint32_t c = h[p][threadIdx.x];
-        if (c) atomicAdd(&hist[((size_t)seg * kMaxSortPasses + p) * 256u + threadIdx.x], c);
-    }
+    for (int p = 0; p < passes; ++p)
+        for (uint32_t d = threadIdx.x; d < R; d += kSortThreads) {
+            const uint32_t c = h[p][d];
+            if (c) atomicAdd(&hist[((size_t)seg * kMaxSortPasses + p) * kMaxRadix + d], c);
+        }
 }
 
 // Per segment and pass: the histogram becomes each digit's first output slot (the
-// segment's begin plus the exclusive prefix over digits).  One 256-thread block per segment.
+// segment's begin plus the exclusive prefix over digits).  One 256-thread block per
+// segment; each thread owns R / 256 consecutive digits.
+template <uint32_t R>
 __global__ void __launch_bounds__(256) digit_offsets_kernel(const SegmentSpec *__restrict__ specs,
                                                             uint32_t *__restrict__ hist, int passes) {
+    constexpr uint32_t kPer = R / 256u;
     __shared__ uint32_t warp_sums[8];
-    __shared__ uint32_t total;
     const SegmentSpec s = specs[blockIdx.x];
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
     for (int p = 0; p < passes; ++p) {
-        uint32_t *h = hist + ((size_t)blockIdx.x * kMaxSortPasses + p) * 256u;
-        const uint32_t v = h[threadIdx.x];
-        const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
-        uint32_t incl = warp_incl_scan(v);
+        uint32_t *h = hist + ((size_t)blockIdx.x * kMaxSortPasses + p) * kMaxRadix + threadIdx.x * kPer;
+        uint32_t v[kPer], sum = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) {
+            v[k] = h[k];
+            sum += v[k];
+        }
+        const uint32_t incl = warp_incl_scan(sum);
         if (lane == 31) warp_sums[warp] = incl;
         __syncthreads();
         if (warp == 0) {
-            uint32_t w = lane < 8 ? warp_sums[lane] : 0u;
-            uint32_t wi = warp_incl_scan(w);
+            const uint32_t w = lane < 8 ? warp_sums[lane] : 0u;
+            const uint32_t wi = warp_incl_scan(w);
             if (lane < 8) warp_sums[lane] = wi - w;
-            if (lane == 7) total = wi;
         }
         __syncthreads();
-        h[threadIdx.x] = s.begin + warp_sums[warp] + incl - v;
+        uint32_t run = s.begin + warp_sums[warp] + incl - sum;
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) {
+            h[k] = run;
+            run += v[k];
+        }
         __syncthreads();
     }
 }
@@ -243,6 +260,9 @@ constexpr uint32_t kLookSpinLimit = 1u << 20;  // polls of one predecessor word 
 // back over the earlier tiles of its segment (a tile's first tile starts from the segment's
 // digit offsets).  Tiles take ids in order, so every tile a block waits for is already
 // running; each wait is bounded and reports kErrSortLookback through *err when it runs out.
+// D-bit digits (R = 2^D bins); each thread owns R / 256 consecutive digits for the per-digit
+// work, and looks back for all of them together.
+template <int D>
 __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(const SegmentSpec *__restrict__ specs,
                                                                 const uint32_t *__restrict__ tile_seg,
                                                                 const uint32_t *__restrict__ keys_in,
@@ -252,18 +272,20 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(const SegmentSpe
                                                                 const uint32_t *__restrict__ hist,
                                                                 uint32_t *__restrict__ look, uint32_t *tile_ctr,
                                                                 uint32_t *err, int pass, uint32_t mask) {
+    constexpr uint32_t R = 1u << D;
+    constexpr uint32_t kPer = R / kSortThreads;  // digits per thread
     constexpr int kWarps = kSortThreads / 32;
     constexpr int kRounds = kSortTile / kSortThreads;
-    __shared__ uint32_t warp_hist[kWarps][256];
-    __shared__ uint32_t digit_base[256];
-    __shared__ uint32_t local_start[256];
+    __shared__ uint32_t warp_hist[kWarps][R];
+    __shared__ uint32_t digit_base[R];
+    __shared__ uint32_t local_start[R];
     __shared__ uint32_t warp_sums[kWarps];
     __shared__ uint32_t keys_s[kSortTile], vals_s[kSortTile];
-    __shared__ uint32_t tile_hist[256];
+    __shared__ uint32_t tile_hist[R];
     __shared__ uint32_t s_tile;
     if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr + pass, 1u);
-    for (int i = threadIdx.x; i < kWarps * 256; i += kSortThreads) (&warp_hist[0][0])[i] = 0;
-    tile_hist[threadIdx.x] = 0;
+    for (uint32_t i = threadIdx.x; i < kWarps * R; i += kSortThreads) (&warp_hist[0][0])[i] = 0;
+    for (uint32_t d = threadIdx.x; d < R; d += kSortThreads) tile_hist[d] = 0;
     __syncthreads();
     const uint32_t tile = s_tile;
     const uint32_t seg = tile_seg[tile];
@@ -272,7 +294,10 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(const SegmentSpe
     const uint32_t beg = s.begin + t * kSortTile;
     const uint32_t end = min(beg + (uint32_t)kSortTile, s.begin + s.count);
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
-    const int shift = 8 * pass;
+    const int shift = D * pass;
+    const uint32_t *seg_hist = hist + ((size_t)seg * kMaxSortPasses + pass) * kMaxRadix;
+    uint32_t *tile_look = look + ((size_t)pass * gridDim.x) * R;  // [tile][R] of this pass
+    const uint32_t d0 = threadIdx.x * kPer;                         // this thread's first digit
 
     uint32_t key[kRounds], val[kRounds], rank[kRounds], dig[kRounds];
     // the tile's digit counts first, published before the ranking so that later tiles
@@ -281,22 +306,24 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(const SegmentSpe
     for (int r = 0; r < kRounds; ++r) {
         const uint32_t i = beg + warp * (kSortTile / kWarps) + r * 32 + lane;
         key[r] = i < end ? keys_in[i] : 0u;
-        dig[r] = i < end ? ((key[r] >> shift) & mask) : 256u;
+        dig[r] = i < end ? ((key[r] >> shift) & mask) : R;
     }
 #pragma unroll
     for (int r = 0; r < kRounds; ++r) {
         // one shared atomic per distinct digit of the warp (a tile's keys share their upper
         // digits, which per-key atomics would serialize on one address)
         const uint32_t peers = __match_any_sync(0xffffffffu, dig[r]);
-        if (dig[r] < 256u && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&tile_hist[dig[r]], (uint32_t)__popc(peers));
+        if (dig[r] < R && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&tile_hist[dig[r]], (uint32_t)__popc(peers));
     }
     __syncthreads();
-    volatile uint32_t *mine = look + ((size_t)pass * gridDim.x + tile) * 256u + threadIdx.x;
-    if (t == 0)
-        *mine = kLookPrefix | ((hist[((size_t)seg * kMaxSortPasses + pass) * 256u + threadIdx.x] + tile_hist[threadIdx.x]) &
-                               kLookValue);
-    else
-        *mine = kLookAgg | tile_hist[threadIdx.x];
+#pragma unroll
+    for (uint32_t k = 0; k < kPer; ++k) {
+        volatile uint32_t *mine = tile_look + (size_t)tile * R + d0 + k;
+        if (t == 0)
+            *mine = kLookPrefix | ((seg_hist[d0 + k] + tile_hist[d0 + k]) & kLookValue);
+        else
+            *mine = kLookAgg | tile_hist[d0 + k];
+    }
 #pragma unroll
     for (int r = 0; r < kRounds; ++r) {
         const uint32_t i = beg + warp * (kSortTile / kWarps) + r * 32 + lane;
@@ -316,68 +343,97 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(const SegmentSpe
     }
     __syncthreads();
     {
-        // per digit (one thread each): prefix over warps, the tile's count, the look-back
-        const uint32_t d = threadIdx.x;
-        uint32_t run = 0;
-        for (int w = 0; w < kWarps; ++w) {
-            const uint32_t c = warp_hist[w][d];
-            warp_hist[w][d] = run;
-            run += c;
-        }
-        uint32_t excl;
-        if (t == 0) {
-            excl = hist[((size_t)seg * kMaxSortPasses + pass) * 256u + d];
-        } else {
-            // windows of up to 8 predecessors, loaded together: add counts back to the
-            // nearest inclusive prefix; spin (bounded) only on a word not yet published
-            excl = 0;
-            uint32_t next = tile;  // predecessors still to add: [tile_begin, next)
-            bool done = false;
-            while (!done) {
-                const uint32_t n = min(8u, next - s.tile_begin);
-                uint32_t v[8];
+        // per digit (kPer consecutive ones per thread): prefix over warps, the tile's count,
+        // the look-back
+        uint32_t run[kPer], excl[kPer];
 #pragma unroll
-                for (int k = 0; k < 8; ++k)
-                    v[k] = (uint32_t)k < n ? *(const volatile uint32_t *)(look + ((size_t)pass * gridDim.x + next - 1 - k) * 256u + d)
-                                           : 0u;
-                for (uint32_t k = 0; k < n && !done; ++k) {
-                    const volatile uint32_t *w = look + ((size_t)pass * gridDim.x + next - 1 - k) * 256u + d;
-                    uint32_t x = v[k];
-                    for (uint32_t spin = 0; (x >> 30) == 0u; ++spin) {
-                        if (spin == kLookSpinLimit) {
-                            atomicOr(err, kErrSortLookback);
-                            break;
+        for (uint32_t k = 0; k < kPer; ++k) {
+            uint32_t acc = 0;
+            for (int w = 0; w < kWarps; ++w) {
+                const uint32_t c = warp_hist[w][d0 + k];
+                warp_hist[w][d0 + k] = acc;
+                acc += c;
+            }
+            run[k] = acc;
+            excl[k] = t == 0 ? seg_hist[d0 + k] : 0u;
+        }
+        if (t != 0) {
+            // windows of up to 8 predecessors, loaded together for every digit still open:
+            // add counts back to the nearest inclusive prefix; spin (bounded) only on a
+            // word not yet published
+            bool done[kPer];
+#pragma unroll
+            for (uint32_t k = 0; k < kPer; ++k) done[k] = false;
+            uint32_t next = tile;  // predecessors still to add: [tile_begin, next)
+            bool open = true;
+            while (open) {
+                const uint32_t n = min(8u, next - s.tile_begin);
+                uint32_t v[kPer][8];
+#pragma unroll
+                for (uint32_t k = 0; k < kPer; ++k)
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        v[k][q] = (!done[k] && (uint32_t)q < n)
+                                      ? *(const volatile uint32_t *)(tile_look + (size_t)(next - 1 - q) * R + d0 + k)
+                                      : 0u;
+#pragma unroll
+                for (uint32_t k = 0; k < kPer; ++k) {
+                    for (uint32_t q = 0; q < n && !done[k]; ++q) {
+                        const volatile uint32_t *w = tile_look + (size_t)(next - 1 - q) * R + d0 + k;
+                        uint32_t x = v[k][q];
+                        for (uint32_t spin = 0; (x >> 30) == 0u; ++spin) {
+                            if (spin == kLookSpinLimit) {
+                                atomicOr(err, kErrSortLookback);
+                                break;
+                            }
+                            __nanosleep(32);
+                            x = *w;
                         }
-                        __nanosleep(32);
-                        x = *w;
+                        excl[k] += x & kLookValue;
+                        if ((x >> 30) != 1u) done[k] = true;  // an inclusive prefix (or a wait that ran out)
                     }
-                    excl += x & kLookValue;
-                    if ((x >> 30) != 1u) done = true;  // an inclusive prefix (or a wait that ran out)
                 }
                 next -= n;
-                if (!done && next == s.tile_begin) {
-                    // only counts down to the segment's first tile: start from its digit offsets
-                    excl += hist[((size_t)seg * kMaxSortPasses + pass) * 256u + d];
-                    done = true;
+                open = false;
+#pragma unroll
+                for (uint32_t k = 0; k < kPer; ++k) {
+                    if (!done[k] && next == s.tile_begin) {
+                        // only counts down to the segment's first tile: start from its digit offsets
+                        excl[k] += seg_hist[d0 + k];
+                        done[k] = true;
+                    }
+                    open = open || !done[k];
                 }
             }
-            *mine = kLookPrefix | ((excl + run) & kLookValue);
+#pragma unroll
+            for (uint32_t k = 0; k < kPer; ++k)
+                *(volatile uint32_t *)(tile_look + (size_t)tile * R + d0 + k) = kLookPrefix | ((excl[k] + run[k]) & kLookValue);
         }
-        digit_base[d] = excl;
         // the tile's own digit-sorted layout: exclusive scan of its digit counts
-        const uint32_t incl = warp_incl_scan(run);
+        uint32_t sum = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) {
+            digit_base[d0 + k] = excl[k];
+            sum += run[k];
+        }
+        const uint32_t incl = warp_incl_scan(sum);
         if (lane == 31) warp_sums[warp] = incl;
         __syncthreads();
         uint32_t before = 0;
         for (uint32_t w = 0; w < warp; ++w) before += warp_sums[w];
-        local_start[d] = before + incl - run;
+        uint32_t start = before + incl - sum;
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) {
+            local_start[d0 + k] = start;
+            start += run[k];
+        }
     }
     __syncthreads();
     // stage the tile in digit order, then write runs of equal digits to consecutive
     // global slots (coalesced), not one sector per key
 #pragma unroll
     for (int r = 0; r < kRounds; ++r) {
-        if (dig[r] < 256u) {
+        if (dig[r] < R) {
             const uint32_t j = local_start[dig[r]] + warp_hist[warp][dig[r]] + rank[r];
             keys_s[j] = key[r];
             vals_s[j] = val[r];
@@ -526,24 +582,26 @@ void launch_box(const SortLaunch &L, cudaStream_t st) {
 
 // Sorts the keys of every segment; on return *sorted_keys / *perm point at the buffers
 // holding the sorted keys and the permutation (sorted slot -> previous slot).
-void launch_sort(const SortLaunch &L, cudaStream_t st, uint32_t **sorted_keys, uint32_t **perm) {
+template <int D>
+void launch_sort_digits(const SortLaunch &L, cudaStream_t st, uint32_t **sorted_keys, uint32_t **perm) {
+    constexpr uint32_t R = 1u << D;
     uint32_t *kin = L.keys[0], *kout = L.keys[1];
     uint32_t *vin = nullptr, *vout = L.vals[1];
     const int passes = sort_passes(L.key_bits);
     // zero the histograms, the tile counters and the look-back words of the passes used
     cudaMemsetAsync(L.sort_scratch, 0,
-                    sizeof(uint32_t) * ((size_t)L.segments * kMaxSortPasses * 256u + kMaxSortPasses +
-                                        (size_t)passes * L.tiles * 256u),
+                    sizeof(uint32_t) * ((size_t)L.segments * kMaxSortPasses * kMaxRadix + kMaxSortPasses +
+                                        (size_t)passes * L.tiles * R),
                     st);
     uint32_t *hist = L.sort_scratch;
-    uint32_t *tile_ctr = hist + (size_t)L.segments * kMaxSortPasses * 256u;
+    uint32_t *tile_ctr = hist + (size_t)L.segments * kMaxSortPasses * kMaxRadix;
     uint32_t *look = tile_ctr + kMaxSortPasses;
-    keys_hist_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.box, L.pos, kin, hist, passes, L.key_bits);
-    digit_offsets_kernel<<<L.segments, 256, 0, st>>>(L.specs, hist, passes);
+    keys_hist_kernel<D><<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.box, L.pos, kin, hist, passes, L.key_bits);
+    digit_offsets_kernel<R><<<L.segments, 256, 0, st>>>(L.specs, hist, passes);
     for (int p = 0; p < passes; ++p) {
-        const int bits = std::min(8, (int)L.key_bits - 8 * p);
-        onesweep_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, kin, vin, kout, vout, hist, look,
-                                                          tile_ctr, L.err, p, (1u << bits) - 1u);
+        const int bits = std::min(D, (int)L.key_bits - D * p);
+        onesweep_kernel<D><<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, kin, vin, kout, vout, hist, look,
+                                                             tile_ctr, L.err, p, (1u << bits) - 1u);
         // ping-pong: the next pass reads what this one wrote
         uint32_t *tk = kin;
         kin = kout;
@@ -561,6 +619,13 @@ void launch_sort(const SortLaunch &L, cudaStream_t st, uint32_t **sorted_keys, u
     *perm = vin;
 }
 
+void launch_sort(const SortLaunch &L, cudaStream_t st, uint32_t **sorted_keys, uint32_t **perm) {
+    if (sort_digit_bits(L.key_bits) == 9)
+        launch_sort_digits<9>(L, st, sorted_keys, perm);
+    else
+        launch_sort_digits<8>(L, st, sorted_keys, perm);
+}
+
 // Self-test of the look-back's bounded wait: one block takes tile 1 of a two-tile segment
 // whose tile 0 never publishes, so every digit's wait runs out (each after kLookSpinLimit
 // polls, well under a second) and the kernel reports kErrSortLookback in *err and returns.
@@ -572,7 +637,7 @@ cudaError_t selftest_sort_wait(uint32_t *err_host) {
     spec.tile_begin = 0;
     spec.tile_count = 2;
     const uint32_t tile_seg[2] = {0u, 0u};
-    const size_t hist_words = (size_t)kMaxSortPasses * 256u;
+    const size_t hist_words = (size_t)kMaxSortPasses * kMaxRadix;
     SegmentSpec *d_spec = nullptr;
     uint32_t *d_tile_seg = nullptr, *d_keys = nullptr, *d_out = nullptr, *d_hist = nullptr, *d_look = nullptr,
              *d_ctr = nullptr, *d_err = nullptr;
@@ -596,8 +661,8 @@ cudaError_t selftest_sort_wait(uint32_t *err_host) {
     if (e == cudaSuccess) {
         // gridDim.x = 1 but tile = 1: the look-back words of tile t sit at t * 256 (two
         // tiles' worth allocated), keys and values out of tile 1 land in [0, 2 * kSortTile)
-        onesweep_kernel<<<1, kSortThreads>>>(d_spec, d_tile_seg, d_keys, nullptr, d_out, d_out + 2 * kSortTile, d_hist,
-                                             d_look, d_ctr, d_err, 0, 0xFFu);
+        onesweep_kernel<8><<<1, kSortThreads>>>(d_spec, d_tile_seg, d_keys, nullptr, d_out, d_out + 2 * kSortTile,
+                                                d_hist, d_look, d_ctr, d_err, 0, 0xFFu);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaDeviceSynchronize();

@@ -88,14 +88,20 @@ struct ActLaunch {
 
 void launch_box(const SortLaunch &L, cudaStream_t st);
 constexpr int kMaxSortPasses = 4;  // 32-bit keys in 8-bit digits
+constexpr uint32_t kMaxRadix = 512;  // bins of the widest digit (9 bits)
 
-constexpr int sort_passes(uint32_t key_bits) { return (int)((key_bits + 7u) / 8u); }
+// Digit width of a radix sort of `key_bits`-bit keys: 9 bits where that takes one pass
+// fewer than 8-bit digits (17-18 and 25-27-bit keys), else 8.
+constexpr int sort_digit_bits(uint32_t key_bits) { return (key_bits + 8u) / 9u < (key_bits + 7u) / 8u ? 9 : 8; }
+constexpr int sort_passes(uint32_t key_bits) {
+    return (int)((key_bits + (uint32_t)sort_digit_bits(key_bits) - 1u) / (uint32_t)sort_digit_bits(key_bits));
+}
 
 // Bytes of the sort's scratch: per-segment histograms of every digit, one tile counter per
 // pass, and the look-back words of every (pass, tile, digit).
 constexpr size_t sort_scratch_bytes(uint32_t segments, uint32_t tiles) {
-    return sizeof(uint32_t) * ((size_t)segments * kMaxSortPasses * 256u + kMaxSortPasses +
-                               (size_t)kMaxSortPasses * tiles * 256u);
+    return sizeof(uint32_t) * ((size_t)segments * kMaxSortPasses * kMaxRadix + kMaxSortPasses +
+                               (size_t)kMaxSortPasses * tiles * kMaxRadix);
 }
 
 // Bounding box of n positions into *out (reset first), for the pushed extent.
