@@ -149,6 +149,7 @@ SeeLaunch see_launch(TgpuBatch *b, const KernelRun &r, const PassIO &io) {
     SeeLaunch S{};
     S.specs = b->d_specs;
     S.box = b->d_box;
+    S.grids = b->d_grids;
     S.table = b->table;
     S.cta_table = b->d_cta;
     S.radii = r.d_radii;
@@ -224,6 +225,7 @@ void backward_step(TgpuAdjoint *a, const Record &r) {
     cudaStream_t st = b->st;
     cudaMemcpyAsync(b->d_box, r.box, (size_t)b->nseg * sizeof(BoxAcc), cudaMemcpyDeviceToDevice, st);
     SortLaunch L = sort_launch(b);
+    launch_grids(L, st);  // the recorded step's grids from its restored boxes
     launch_cell_table(L, r.keys, 1, st);
 
     PassIO io{};

@@ -39,7 +39,8 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 // byte offsets inside the scratch array
 constexpr size_t kOffSpec = 0;
 constexpr size_t kOffBox = align256(kOffSpec + sizeof(SegmentSpec));
-constexpr size_t kOffPairs = align256(kOffBox + sizeof(BoxAcc));
+constexpr size_t kOffGrid = align256(kOffBox + sizeof(BoxAcc));
+constexpr size_t kOffPairs = align256(kOffGrid + sizeof(SegGrid));
 constexpr size_t kOffTileSeg = align256(kOffPairs + sizeof(unsigned long long));
 constexpr size_t kOffRadii = align256(kOffTileSeg + sizeof(uint32_t) * kNoallocTiles);
 constexpr size_t kOffCtx = align256(kOffRadii + sizeof(float4));
@@ -162,6 +163,7 @@ extern "C" int tgpu_see_noalloc(const float *positions, unsigned n, const float 
     L.specs = reinterpret_cast<const SegmentSpec *>(scratch + kOffSpec);
     L.tile_seg = reinterpret_cast<const uint32_t *>(scratch + kOffTileSeg);
     L.box = reinterpret_cast<BoxAcc *>(scratch + kOffBox);
+    L.grids = reinterpret_cast<SegGrid *>(scratch + kOffGrid);
     L.pos = reinterpret_cast<const float4 *>(positions);
     L.keys[0] = reinterpret_cast<uint32_t *>(scratch + kOffKeys0);
     L.keys[1] = reinterpret_cast<uint32_t *>(scratch + kOffKeys1);
@@ -191,6 +193,7 @@ extern "C" int tgpu_see_noalloc(const float *positions, unsigned n, const float 
     SeeLaunch S{};
     S.specs = L.specs;
     S.box = L.box;
+    S.grids = L.grids;
     S.table = L.table;
     S.cta_table = reinterpret_cast<const uint2 *>(scratch + kOffCta);
     S.radii = reinterpret_cast<const float4 *>(scratch + kOffRadii);

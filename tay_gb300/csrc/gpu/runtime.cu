@@ -110,6 +110,7 @@ void free_batch(TgpuBatch *b) {
     cudaFree(b->d_tile_seg);
     cudaFree(b->d_cta);
     cudaFree(b->d_box);
+    cudaFree(b->d_grids);
     for (int c = 0; c < kMaxF4; ++c)
         for (int k = 0; k < 2; ++k) cudaFree(b->f4[c][k]);
     for (int c = 0; c < kMaxU32; ++c)
@@ -318,6 +319,7 @@ SortLaunch tgpu::sort_launch(TgpuBatch *b) {
     L.sort_scratch = b->sort_scratch;
     L.err = b->d_err;
     L.table = b->table;
+    L.grids = b->d_grids;
     L.segments = (uint32_t)b->nseg;
     L.tiles = b->tiles;
     L.key_bits = b->key_bits;
@@ -403,6 +405,7 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E, bool write_through) {
             SeeLaunch S{};
             S.specs = b->d_specs;
             S.box = b->d_box;
+            S.grids = b->d_grids;
             S.table = b->table;
             S.cta_table = b->d_cta;
             S.radii = r.d_radii;
@@ -709,6 +712,7 @@ int alloc_batch(TgpuBatch *b) {
     CKR(cudaMalloc(&b->d_tile_seg, sizeof(uint32_t) * std::max<uint32_t>(b->tiles, 1)));
     CKR(cudaMalloc(&b->d_cta, sizeof(uint2) * std::max<uint32_t>(b->ctas, 1)));
     CKR(cudaMalloc(&b->d_box, sizeof(BoxAcc) * b->nseg));
+    CKR(cudaMalloc(&b->d_grids, sizeof(SegGrid) * b->nseg));
     if (b->tiles) CKR(cudaMemcpy(b->d_tile_seg, b->tile_seg.data(), sizeof(uint32_t) * b->tiles, cudaMemcpyHostToDevice));
     if (b->ctas) CKR(cudaMemcpy(b->d_cta, b->cta.data(), sizeof(uint2) * b->ctas, cudaMemcpyHostToDevice));
     for (int c = 0; c < m->nf4; ++c) {

@@ -62,6 +62,7 @@ struct TgpuBatch {
     uint32_t *d_tile_seg = nullptr;
     uint2 *d_cta = nullptr;
     BoxAcc *d_box = nullptr;
+    SegGrid *d_grids = nullptr;  // per segment: this step's grid (from the box)
     float4 *f4[kMaxF4][2] = {};
     uint32_t *u32[kMaxU32][2] = {};
     int cur_f4[kMaxF4] = {};

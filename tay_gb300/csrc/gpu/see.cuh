@@ -347,8 +347,9 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
     const SegmentSpec S = L.specs[seg];                       // seers
     const SegmentSpec T = L.specs[L.cross ? L.seen_seg : seg];  // seen agents: grid and table
     const BoxAcc B = L.box[L.cross ? L.seen_seg : seg];
-    const Grid g = segment_grid(T, B);
-    const float pad = grid_pad(g, T, B);
+    const SegGrid &G = L.grids[L.cross ? L.seen_seg : seg];
+    const Grid g = G.g;
+    const float pad = G.pad;
     const float4 r4 = L.radii[seg];
     const typename P::SeeCtx &sctx = *reinterpret_cast<const typename P::SeeCtx *>(L.ctx + (size_t)seg * L.ctx_stride);
     const typename P::ActCtx &actx =
@@ -558,8 +559,9 @@ __global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
     const SegmentSpec S = L.specs[seg];                       // seers
     const SegmentSpec T = L.specs[L.cross ? L.seen_seg : seg];  // seen agents: grid and table
     const BoxAcc B = L.box[L.cross ? L.seen_seg : seg];
-    const Grid g = segment_grid(T, B);
-    const float pad = grid_pad(g, T, B);
+    const SegGrid &G = L.grids[L.cross ? L.seen_seg : seg];
+    const Grid g = G.g;
+    const float pad = G.pad;
     const float4 r4 = L.radii[seg];
     const typename P::SeeCtx &sctx = *reinterpret_cast<const typename P::SeeCtx *>(L.ctx + (size_t)seg * L.ctx_stride);
     const typename P::ActCtx &actx =

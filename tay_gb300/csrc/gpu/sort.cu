@@ -157,6 +157,20 @@ TGPU_D uint32_t count_index(const SegmentSpec &s, uint32_t digit, uint32_t local
     return 256u * s.tile_begin + digit * s.tile_count + local_tile;
 }
 
+// Each segment's grid for this step from its box (or fixed box), with its rounding pad:
+// one thread per segment.
+__global__ void grid_kernel(const SegmentSpec *__restrict__ specs, const BoxAcc *__restrict__ box,
+                            SegGrid *__restrict__ grids, uint32_t segments) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= segments) return;
+    const SegmentSpec sp = specs[s];
+    const BoxAcc b = box[s];
+    SegGrid out;
+    out.g = segment_grid(sp, b);
+    out.pad = grid_pad(out.g, sp, b);
+    grids[s] = out;
+}
+
 // One pass over the positions: the grid from the box, the cell key of every agent, and
 // per-segment histograms of every D-bit digit of the keys (order-independent, so all
 // passes' digit offsets are known before the first scatter).  hist layout:
@@ -164,7 +178,7 @@ TGPU_D uint32_t count_index(const SegmentSpec &s, uint32_t digit, uint32_t local
 template <int D>
 __global__ void __launch_bounds__(kSortThreads) keys_hist_kernel(const SegmentSpec *__restrict__ specs,
                                                                  const uint32_t *__restrict__ tile_seg,
-                                                                 const BoxAcc *__restrict__ box,
+                                                                 const SegGrid *__restrict__ grids,
                                                                  const float4 *__restrict__ pos,
                                                                  uint32_t *__restrict__ keys,
                                                                  uint32_t *__restrict__ hist, int passes,
@@ -173,7 +187,7 @@ __global__ void __launch_bounds__(kSortThreads) keys_hist_kernel(const SegmentSp
     __shared__ uint32_t h[kMaxSortPasses][R];
     const uint32_t seg = tile_seg[blockIdx.x];
     const SegmentSpec s = specs[seg];
-    const Grid g = segment_grid(s, box[seg]);
+    const Grid g = grids[seg].g;
     const uint32_t t = blockIdx.x - s.tile_begin;
     const uint32_t beg = s.begin + t * kSortTile;
     const uint32_t end = min(beg + (uint32_t)kSortTile, s.begin + s.count);
@@ -465,22 +479,14 @@ constexpr uint32_t kTableBlocks = kSortTile / kSortThreads;
 // entries after its cell; a row's first agent clears the whole row.
 __global__ void __launch_bounds__(kSortThreads) cell_table_kernel(const SegmentSpec *__restrict__ specs,
                                                                   const uint32_t *__restrict__ tile_seg,
-                                                                  const BoxAcc *__restrict__ box,
+                                                                  const SegGrid *__restrict__ grids,
                                                                   const uint32_t *__restrict__ keys,
                                                                   uint2 *__restrict__ table, int write_runs) {
-    // kTableBlocks blocks per radix tile, one key per thread; the segment's grid is
-    // derived once per block
-    __shared__ uint32_t s_dx, s_dy;
+    // kTableBlocks blocks per radix tile, one key per thread
     const uint32_t tile = blockIdx.x / kTableBlocks, part = blockIdx.x % kTableBlocks;
     const uint32_t seg = tile_seg[tile];
     const SegmentSpec s = specs[seg];
-    if (threadIdx.x == 0) {
-        const Grid g = segment_grid(s, box[seg]);
-        s_dx = (uint32_t)g.dims[0];
-        s_dy = (uint32_t)g.dims[1];
-    }
-    __syncthreads();
-    const uint32_t dx = s_dx, dy = s_dy;
+    const uint32_t dx = (uint32_t)grids[seg].g.dims[0], dy = (uint32_t)grids[seg].g.dims[1];
     const uint32_t beg = s.begin + (tile - s.tile_begin) * kSortTile + part * kSortThreads;
     const uint32_t seg_end = s.begin + s.count;
     const uint32_t end = min(beg + (uint32_t)kSortThreads, seg_end);
@@ -578,6 +584,11 @@ void launch_extent(const float4 *pos, uint32_t n, BoxAcc *out, cudaStream_t st) 
 void launch_box(const SortLaunch &L, cudaStream_t st) {
     box_reset_kernel<<<(L.segments + 127) / 128, 128, 0, st>>>(L.box, L.segments);
     bbox_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.pos, L.pos_max, L.box);
+    launch_grids(L, st);
+}
+
+void launch_grids(const SortLaunch &L, cudaStream_t st) {
+    grid_kernel<<<(L.segments + 127) / 128, 128, 0, st>>>(L.specs, L.box, L.grids, L.segments);
 }
 
 // Sorts the keys of every segment; on return *sorted_keys / *perm point at the buffers
@@ -596,7 +607,8 @@ void launch_sort_digits(const SortLaunch &L, cudaStream_t st, uint32_t **sorted_
     uint32_t *hist = L.sort_scratch;
     uint32_t *tile_ctr = hist + (size_t)L.segments * kMaxSortPasses * kMaxRadix;
     uint32_t *look = tile_ctr + kMaxSortPasses;
-    keys_hist_kernel<D><<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.box, L.pos, kin, hist, passes, L.key_bits);
+    keys_hist_kernel<D><<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.grids, L.pos, kin, hist, passes,
+                                                          L.key_bits);
     digit_offsets_kernel<R><<<L.segments, 256, 0, st>>>(L.specs, hist, passes);
     for (int p = 0; p < passes; ++p) {
         const int bits = std::min(D, (int)L.key_bits - D * p);
@@ -679,8 +691,8 @@ cudaError_t selftest_sort_wait(uint32_t *err_host) {
 }
 
 void launch_cell_table(const SortLaunch &L, const uint32_t *sorted_keys, int write_runs, cudaStream_t st) {
-    cell_table_kernel<<<L.tiles * kTableBlocks, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.box, sorted_keys, L.table,
-                                                                     write_runs);
+    cell_table_kernel<<<L.tiles * kTableBlocks, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.grids, sorted_keys,
+                                                                     L.table, write_runs);
 }
 
 void launch_gather(uint32_t n, const uint32_t *perm, const GatherSet &set, cudaStream_t st) {

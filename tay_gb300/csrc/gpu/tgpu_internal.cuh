@@ -263,6 +263,13 @@ TGPU_D float grid_pad(const Grid &g, const SegmentSpec &s, const BoxAcc &b) {
     return fmaxf(1.0f / 512.0f, 16.0f * ulp / csmin + 1024.0f * 4.0f * 1.1920929e-7f);
 }
 
+// A segment's grid for one step with its rounding pad (grid_pad), derived once per step
+// from the bounding box by the grid kernel and read by every later kernel of the step.
+struct SegGrid {
+    Grid g;
+    float pad;
+};
+
 // Device-side error word: kernels never trap; they record the first failure here and
 // the host turns it into TAY_ERROR_CUDA.
 enum DeviceError : uint32_t {

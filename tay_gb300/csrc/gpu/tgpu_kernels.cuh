@@ -18,6 +18,7 @@ struct SortLaunch {
                                // counters and look-back words, zeroed by every sort
     uint32_t *err;             // device error word (DeviceError bits)
     uint2 *table;              // dense cell tables of all segments
+    SegGrid *grids;            // [segments] this step's grids, written by launch_box / launch_grids
     uint32_t segments;
     uint32_t tiles;
     uint32_t key_bits;
@@ -44,6 +45,7 @@ struct PassIO {
 struct SeeLaunch {
     const SegmentSpec *specs;
     const BoxAcc *box;
+    const SegGrid *grids;     // per segment this step's grid and rounding pad
     const uint2 *table;
     const uint2 *cta_table;   // per CTA {segment, first seer}
     const float4 *radii;      // per segment see radii of this pass
@@ -86,7 +88,10 @@ struct ActLaunch {
     PassIO io;
 };
 
+// Bounding boxes of every segment, then their grids (launch_grids).
 void launch_box(const SortLaunch &L, cudaStream_t st);
+// Grids of every segment from the boxes in L.box (after they were set or restored).
+void launch_grids(const SortLaunch &L, cudaStream_t st);
 constexpr int kMaxSortPasses = 4;  // 32-bit keys in 8-bit digits
 constexpr uint32_t kMaxRadix = 512;  // bins of the widest digit (9 bits)
 
