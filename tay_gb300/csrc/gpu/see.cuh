@@ -551,8 +551,10 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
 // ranges are nearly the same length and their candidate loads fall on neighbouring
 // addresses.  No staging; a warp whose union box is compact walks the union's row
 // ranges with the two-phase batches instead.
+// At most 64 registers (8 CTAs of 128 threads per SM) except for the staged walk: a few
+// spills cost less than the occupancy step above 64 (measured on the boids and SPH passes).
 template <class P, bool kStage = false, bool kWrite = false>
-__global__ void __launch_bounds__(kSeeThreads) see_rows_kernel(SeeLaunch L) {
+__global__ void __launch_bounds__(kSeeThreads, kStage ? 1 : 8) see_rows_kernel(SeeLaunch L) {
     using namespace see_detail;
     const uint2 cta = L.cta_table[L.cta_offset + blockIdx.x];
     const uint32_t seg = cta.x;
