@@ -277,7 +277,7 @@ constexpr uint32_t kLookSpinLimit = 1u << 20;  // polls of one predecessor word 
 // D-bit digits (R = 2^D bins); each thread owns R / 256 consecutive digits for the per-digit
 // work, and looks back for all of them together.
 template <int D>
-__global__ void __launch_bounds__(kSortThreads) onesweep_kernel(const SegmentSpec *__restrict__ specs,
+__global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(const SegmentSpec *__restrict__ specs,
                                                                 const uint32_t *__restrict__ tile_seg,
                                                                 const uint32_t *__restrict__ keys_in,
                                                                 const uint32_t *__restrict__ vals_in,
