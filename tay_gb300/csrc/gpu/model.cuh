@@ -56,7 +56,8 @@ struct ModelDesc {
     int nkernels;
     const ProgramDesc *programs;
     int nprograms;
-    void (*pack)(const uint32_t *aos, uint32_t n, const PassIO &io, cudaStream_t st);
+    // AoS -> SoA; the packed positions' extent is reduced into *extent (reset by the caller)
+    void (*pack)(const uint32_t *aos, uint32_t n, const PassIO &io, BoxAcc *extent, cudaStream_t st);
     void (*unpack)(uint32_t *aos, uint32_t n, const PassIO &io, uint32_t program, cudaStream_t st);
     int nonpoint;  // 1: box agents, float4 stream 0 the min corner (the position), 1 the max
 };
@@ -116,8 +117,8 @@ cudaError_t prepare_see_t(size_t smem) {
     return cudaFuncSetAttribute(see_rows_kernel<P, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 template <class M>
-void pack_t(const uint32_t *aos, uint32_t n, const PassIO &io, cudaStream_t st) {
-    if (n) pack_kernel<M><<<(n + 255) / 256, 256, 0, st>>>(aos, n, io);
+void pack_t(const uint32_t *aos, uint32_t n, const PassIO &io, BoxAcc *extent, cudaStream_t st) {
+    if (n) pack_kernel<M><<<(n + 255) / 256, 256, 0, st>>>(aos, n, io, extent);
 }
 template <class M>
 void unpack_t(uint32_t *aos, uint32_t n, const PassIO &io, uint32_t program, cudaStream_t st) {

@@ -983,10 +983,10 @@ int tgpu_batch_push(TgpuBatch *b, int group, const void *host) {
         io.out_u32[c] = b->u32[c][b->cur_u32[c]] + sp.begin;
         io.in_u32[c] = io.out_u32[c];
     }
-    b->m->pack(aos, n, io, b->st);
-    // extent of the pushed positions (it sizes the segment's grid budget), reduced on
-    // the device from the packed position stream
-    launch_extent(io.out_f4[0], n, b->d_extent, b->st);
+    // the pack also reduces the extent of the pushed positions (it sizes the segment's
+    // grid budget) on the device
+    reset_extent(b->d_extent, b->st);
+    b->m->pack(aos, n, io, b->d_extent, b->st);
     BoxAcc ext;
     CK(cudaMemcpyAsync(&ext, b->d_extent, sizeof(BoxAcc), cudaMemcpyDeviceToHost, b->st));
     CK(cudaGetLastError());

@@ -772,7 +772,8 @@ template <class M>
 // records are read (pack) or written (unpack) as one contiguous run of words per block:
 // coalesced in device memory, and large requests when `aos` is page-locked host memory
 // the kernel reads or writes in place (no separate copy).
-__global__ void __launch_bounds__(256) pack_kernel(const uint32_t *__restrict__ aos, uint32_t n, PassIO io) {
+__global__ void __launch_bounds__(256) pack_kernel(const uint32_t *__restrict__ aos, uint32_t n, PassIO io,
+                                                   BoxAcc *extent) {
     constexpr uint32_t W = M::kAgentBytes / 4;
     __shared__ __align__(16) uint32_t sm[256 * W];
     const uint32_t first = blockIdx.x * 256u;
@@ -789,7 +790,26 @@ __global__ void __launch_bounds__(256) pack_kernel(const uint32_t *__restrict__ 
     }
     for (uint32_t w = w0 + threadIdx.x; w < words; w += 256u) sm[w] = src[w];
     __syncthreads();
-    if (threadIdx.x < cnt) M::pack(sm + threadIdx.x * W, io, first + threadIdx.x);
+    const bool live = threadIdx.x < cnt;
+    if (live) M::pack(sm + threadIdx.x * W, io, first + threadIdx.x);
+    if (!extent) return;
+    // the extent of the packed positions (the grid budget's input), one atomic per warp
+    // and axis; the thread reads back the position it just wrote
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (live) p = io.out_f4[0][first + threadIdx.x];
+    const float c[3] = {p.x, p.y, p.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        uint32_t l = live ? float_to_ordered(c[a]) : 0xFFFFFFFFu, h = live ? float_to_ordered(c[a]) : 0u;
+        for (int o = 16; o > 0; o >>= 1) {
+            l = min(l, __shfl_xor_sync(0xffffffffu, l, o));
+            h = max(h, __shfl_xor_sync(0xffffffffu, h, o));
+        }
+        if ((threadIdx.x & 31u) == 0 && l <= h) {
+            atomicMin(&extent->lo[a], l);
+            atomicMax(&extent->hi[a], h);
+        }
+    }
 }
 
 template <class M>

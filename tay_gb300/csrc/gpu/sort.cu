@@ -116,28 +116,6 @@ __global__ void __launch_bounds__(kSortThreads) bbox_kernel(const SegmentSpec *_
     }
 }
 
-__global__ void __launch_bounds__(kSortThreads) extent_kernel(const float4 *__restrict__ pos, uint32_t n, BoxAcc *out) {
-    uint32_t lo[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
-    uint32_t hi[3] = {0u, 0u, 0u};
-    for (uint32_t i = blockIdx.x * kSortThreads + threadIdx.x; i < n; i += gridDim.x * kSortThreads) {
-        const float4 p = pos[i];
-        const float c[3] = {p.x, p.y, p.z};
-        for (int a = 0; a < 3; ++a) {
-            const uint32_t o = float_to_ordered(c[a]);
-            lo[a] = min(lo[a], o);
-            hi[a] = max(hi[a], o);
-        }
-    }
-    for (int a = 0; a < 3; ++a) {
-        const uint32_t l = warp_min(lo[a]);
-        const uint32_t h = warp_max(hi[a]);
-        if (lane_id() == 0) {
-            atomicMin(&out->lo[a], l);
-            atomicMax(&out->hi[a], h);
-        }
-    }
-}
-
 __global__ void box_reset_kernel(BoxAcc *box, uint32_t segments) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= segments) return;
@@ -576,10 +554,7 @@ __global__ void __launch_bounds__(256) gather_kernel(uint32_t n, const uint32_t 
 
 // ------------------------------------------------------------------ host-side launchers
 
-void launch_extent(const float4 *pos, uint32_t n, BoxAcc *out, cudaStream_t st) {
-    box_reset_kernel<<<1, 32, 0, st>>>(out, 1);
-    if (n) extent_kernel<<<std::min<uint32_t>((n + kSortThreads - 1) / kSortThreads, 152u * 8u), kSortThreads, 0, st>>>(pos, n, out);
-}
+void reset_extent(BoxAcc *out, cudaStream_t st) { box_reset_kernel<<<1, 32, 0, st>>>(out, 1); }
 
 void launch_box(const SortLaunch &L, cudaStream_t st) {
     box_reset_kernel<<<(L.segments + 127) / 128, 128, 0, st>>>(L.box, L.segments);

@@ -110,7 +110,8 @@ constexpr size_t sort_scratch_bytes(uint32_t segments, uint32_t tiles) {
 }
 
 // Bounding box of n positions into *out (reset first), for the pushed extent.
-void launch_extent(const float4 *pos, uint32_t n, BoxAcc *out, cudaStream_t st);
+// Resets an extent accumulator (the pack kernel reduces the pushed positions into it).
+void reset_extent(BoxAcc *out, cudaStream_t st);
 void launch_sort(const SortLaunch &L, cudaStream_t st, uint32_t **sorted_keys, uint32_t **perm);
 void launch_cell_table(const SortLaunch &L, const uint32_t *sorted_keys, int write_runs, cudaStream_t st);
 // Runs one radix tile whose predecessor never publishes; returns the device error word.
