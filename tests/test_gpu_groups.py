@@ -170,7 +170,8 @@ def test_single_group_pass_list_outside_the_programs(gpu, port):
 @pytest.mark.parametrize("host_loop", ["read", "e2e"])
 def test_write_through_equals_one_run(gpu, host_loop):
     """A host that reads its agents after every run gets them written through by the run's
-    last pass (chunked fused see+act for one group, after the step for a state batch);
+    last pass (from the fused see+act kernel's epilogue for one group, after the step for a
+    state batch);
     with or without pushing them back each step, the records equal one uninterrupted
     run's, bit for bit."""
     ps = W.basic_points(30000, seed=47)
