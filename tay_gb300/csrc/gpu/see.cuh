@@ -2,19 +2,21 @@
 //
 // See pass (replaces tay/cpu_z_grid.c:232-321 + tay/space.c:106-148, and the generated
 // OpenCL see kernel, tay/ocl_grid.c:376-417 + tay/ocl_generics.c:13-114):
-//   * one CTA = 128 consecutive seers in cell order (never crossing a segment);
+//   * one CTA = 128 consecutive seers in cell order (never crossing a segment), one seer
+//     per thread;
 //   * each seer's neighbour cells are the cells overlapping its box p +- r (padded by a
 //     fraction of a cell against rounding), clamped to the grid;
-//   * the CTA stages every cell of the union of its seers' cell boxes into shared
-//     memory, cells in row-major order, so each (y, z) row of cells is one contiguous
-//     run of staged agents;
-//   * each warp walks the rows of the union of its 32 seers' boxes; all 32 lanes read
-//     the same staged agent (a shared-memory broadcast), apply the reference's inclusive
-//     per-axis box test (space.c:62-68: skip when d < -r || d > r, d = seer - seen) and,
-//     when it passes, call the model's see function on registers: no atomics on agent
-//     state, the seer writes only its own accumulators;
-//   * when the halo does not fit the staging buffer, the same walk reads the cells from
-//     global memory through the dense cell table.
+//   * row order (see_rows_kernel, the default): each lane walks its own rows of cells,
+//     one contiguous candidate range per (y, z) row found from the row table, reading the
+//     candidates through L1; Morton order (see_kernel): cell by cell;
+//   * every candidate gets the reference's inclusive per-axis box test (space.c:62-68:
+//     skip when d < -r || d > r, d = seer - seen) and, when it passes, the model's see
+//     function on registers: no atomics on agent state, the seer writes only its own
+//     accumulators; a fused act runs in the epilogue;
+//   * tunings: a warp walks the union of its lanes' boxes with hit masks (union_factor,
+//     hit_masks), or the CTA first copies its union rows (row order, TMA bulk copies) or
+//     cells (Morton) into shared memory (stage); and a write-through instance stores the
+//     finished records to page-locked host memory from the epilogue.
 // Act pass (replaces tay/space.c:250-263): one thread per agent.
 #pragma once
 
