@@ -2,8 +2,8 @@
 //
 // Owns the device buffers of a batch of segments, resolves the registered passes to a
 // device model and its fused kernels, and enqueues each step as:
-//   bounding box -> keys + radix passes -> cell table -> reorder of the state streams
-//   -> the model's pass kernels -> cell table clear
+//   bounding box + grid -> keys + radix passes -> cell table -> reorder of the state
+//   streams -> the model's pass kernels -> cell table clear
 // (the step of tay/state.c:221-311: sort every group, run the passes in order, unsort).
 // Steps are captured once per buffer-parity pattern into CUDA graphs and replayed.
 #include <algorithm>

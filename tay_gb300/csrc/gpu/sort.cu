@@ -1,6 +1,6 @@
-// Z-grid sort for a batch of segments: bounding box, Morton cell keys, a stable LSD radix
-// sort of the keys (8-bit digits), the dense cell table, and the reorder of the
-// structure-of-arrays streams into cell order.
+// Z-grid sort for a batch of segments: bounding box and grid, cell keys (3-D Morton or
+// x-rows), a stable LSD radix sort of the keys (8- or 9-bit digits), the cell table, and the
+// reorder of the structure-of-arrays streams into cell order.
 //
 // Replaces, for the GPU Z-grid, the reference's serial counting sort
 // (tay/cpu_z_grid.c:156-221: count per cell, exclusive scan over every cell, memcpy of

@@ -9,10 +9,13 @@
 //     cell order, a fused see+act pass writes the fields it changes into the other copy;
 //   * per-step streams (accumulators, density/pressure) are single-buffered and valid
 //     only inside one step;
-//   * a dense cell table (uint2 {first, end} per cell, row-major over the segment's grid)
-//     per segment, written only at non-empty cells after each sort and cleared the same
-//     way before the next one (the reference clears its table per step too,
-//     tay/cpu_z_grid.c:223-225).
+//   * a cell table per segment: Morton order, uint2 {first, end} per cell, written only
+//     at non-empty cells; row order, one header per (y, z) row {x_first, x_last, first,
+//     end} plus start entries over each row's occupied span.  Written after each sort and
+//     cleared the same way before the next one (the reference clears its table per step
+//     too, tay/cpu_z_grid.c:223-225);
+//   * per segment and step, the grid (origin, cell size, cells per axis) and its rounding
+//     pad, derived once from the bounding box.
 #pragma once
 
 #include <cuda_runtime.h>
