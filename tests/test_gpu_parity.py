@@ -216,3 +216,27 @@ def test_rows_with_long_gaps_match_oracle(gpu, port, tuning):
     assert g["b_buffer_count"].sum() > 0
     assert np.array_equal(g["b_buffer_count"], o["b_buffer_count"])
     assert normwise(g["b_buffer"][:, :3], o["b_buffer"][:, :3]) < TOL_1STEP
+
+
+def test_batched_workload_full_size_equals_single_states(gpu):
+    """The full batched workload (512 boids states, N log-uniform in [1000, 65536], about
+    8.2 M agents, radius U[5, 20]) advanced by tay_run_batch for 2 steps: every state's
+    records equal those of the same state run alone through tay_run, bit for bit (same
+    segment grid and order, written through by the batched see pass)."""
+    bb = W.batched_boids(states=512, seed=4)
+    setups, recs_list = [], []
+    for ps, r, _side in bb.states:
+        recs_list.append(M.records(M.BOIDS_RECORD, ps.p, ps.v))
+        setups.append(M.boids_setup(r=r, part=r, mb=4))
+    assert sum(r.shape[0] for r in recs_list) > 8_000_000
+    states = [M.make_state(s, r) for s, r in zip(setups, recs_list)]
+    for st, _ in states:
+        st.start()
+    api.run_batch([st for st, _ in states], 2)
+    for k, ((st, g), s, r) in enumerate(zip(states, setups, recs_list)):
+        out = M.by_id(st.agents(g, M.BOIDS_RECORD))
+        st.end()
+        st.close()
+        if k % 8 == 0:  # every 8th state alone (64 single runs keep the test short)
+            single = M.run(s, r, 2)
+            assert out.tobytes() == single.tobytes(), k
