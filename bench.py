@@ -67,6 +67,13 @@ def parse():
     return ap.parse_args()
 
 
+def rank_visible_device(local, visible):
+    """The device a rank keeps visible: the local rank's entry of CUDA_VISIBLE_DEVICES when
+    that lists devices, else the device whose index is the local rank."""
+    vis = [v.strip() for v in (visible or "").split(",") if v.strip()]
+    return vis[local % len(vis)] if vis else str(local)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -465,7 +472,8 @@ def run_gb300(args, rank, world, D):
     from tay_gb300 import api
     from tay_gb300 import models as M
 
-    gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(rank)).split(",")[0] or 0) if world == 1 else rank
+    first = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0].strip()
+    gpu_index = int(first) if first.isdigit() else 0  # physical index for the clock sampler
     setup, recs = workload()
     from tay_gb300 import autotune
 
@@ -604,7 +612,8 @@ def main():
         run_reference(args, rank, world)
         return
     if world > 1:
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+        # one GPU per rank, chosen before anything initialises CUDA
+        os.environ["CUDA_VISIBLE_DEVICES"] = rank_visible_device(local, os.environ.get("CUDA_VISIBLE_DEVICES"))
     D = Dist(world)
     try:
         run_gb300(args, rank, world, D)

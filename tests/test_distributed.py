@@ -43,3 +43,15 @@ def test_two_rank_reduction():
         assert p.exitcode == 0
     got = sorted(q.get(timeout=10) for _ in range(2))
     assert got == [(0, 2.0, 30.0), (1, 2.0, 30.0)]
+
+
+def test_rank_device_selection():
+    """Under torchrun every rank keeps one GPU visible: its entry of CUDA_VISIBLE_DEVICES."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert bench.rank_visible_device(1, "0,1,2,3") == "1"
+    assert bench.rank_visible_device(2, "4, 5,6") == "6"
+    assert bench.rank_visible_device(3, None) == "3"
+    assert bench.rank_visible_device(0, "") == "0"
+    assert bench.rank_visible_device(3, "7,6") == "6"
