@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=3, help="steps of the CPU baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=35,
+                    help="steps of the CPU baseline sample (about 10 s on 16 Grace cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batched-states", type=int, default=512, help="states of the batched leg (0 = skip)")
     ap.add_argument("--sph", type=int, default=1, help="1 = add the 524,288-particle SPH leg")
