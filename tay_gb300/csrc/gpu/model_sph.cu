@@ -136,18 +136,20 @@ struct Force {
         if (r2 < c.support2 && r2 > 0.0f) {
             const float4 bv = acc.f4(1, j);
             const float4 brp = acc.f4(2, j);
-            const float r = __fsqrt_rn(r2);
+            // 1/r from one correctly rounded reciprocal square root: r = r2 / r, dw / r as
+            // a product, and the viscosity term's two divisions as one
+            const float inv_r = __frsqrt_rn(r2);
+            const float r = r2 * inv_r;
             const float q = r * c.inv_h;
             const float dw = kernel_dw(q, c.sigma, c.inv_h);
             const float vx = s.v.x - bv.x, vy = s.v.y - bv.y, vz = s.v.z - bv.z;
             const float vr = (vx * dx + vy * dy) + vz * dz;
             float visc = 0.0f;
             if (vr < 0.0f) {
-                const float mu = (c.h * vr) / (r2 + c.eta2);
                 const float rho_bar = 0.5f * (s.rho + brp.x);
-                visc = -(c.alpha * c.c0 * mu) / rho_bar;
+                visc = -(c.alpha * c.c0 * (c.h * vr)) / ((r2 + c.eta2) * rho_bar);
             }
-            const float coef = -c.m * ((s.A + brp.z) + visc) * (dw / r);
+            const float coef = -c.m * ((s.A + brp.z) + visc) * (dw * inv_r);
             s.ax += coef * dx;
             s.ay += coef * dy;
             s.az += coef * dz;
