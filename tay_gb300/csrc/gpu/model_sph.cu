@@ -136,8 +136,8 @@ struct Force {
         if (r2 < c.support2 && r2 > 0.0f) {
             const float4 bv = acc.f4(1, j);
             const float4 brp = acc.f4(2, j);
-            // 1/r from one correctly rounded reciprocal square root: r = r2 / r, dw / r as
-            // a product, and the viscosity term's two divisions as one
+            // 1/r from one correctly rounded reciprocal square root, r = r2 * (1/r), dw / r
+            // as a product, and the viscosity term's two divisions as one
             const float inv_r = __frsqrt_rn(r2);
             const float r = r2 * inv_r;
             const float q = r * c.inv_h;
