@@ -1,8 +1,8 @@
 """Edge cases and full sizes on the GPU, against the oracle: a single agent, coincident
 agents, neighbours exactly at the radius (the reference's test is inclusive,
 tay/space.c:62-68), a flat axis (zero extent), coordinates far from the origin, tiny and
-large states in one batch, and the benchmark workloads at full size (1,048,576 boids and
-524,288 SPH particles, one step)."""
+large states in one batch, the benchmark workloads at full size (1,048,576 boids and
+524,288 SPH particles, one step), and an 8M-agent state (the largest indices of one segment)."""
 import numpy as np
 import pytest
 
@@ -141,3 +141,19 @@ def test_full_size_sph_density(gpu, port):
         api.set_tuning()
     o = oracle_run(port, O.MODEL_SPH, setup, recs, 1, threads=0)
     assert normwise(g["rho"], o["rho"]) < 1e-5
+
+
+@pytest.mark.parametrize("tuning", [{"cell_order": 0}, None])
+def test_eight_million_agents_counts_bit_exact(gpu, port, tuning):
+    """One state of 8,388,608 test agents (uniform, about 20 neighbours each): agent, cell,
+    CTA, tile and table indices at their largest for one segment; neighbour counts equal
+    the oracle's bit for bit in both cell orders."""
+    n = 8 << 20
+    ps = W.basic_points(n, seed=71, side=7400.0)
+    recs = M.records(M.TEST_RECORD, ps.p, ps.v)
+    g, setup = _see_counts(recs, tuning=tuning)
+    o = oracle_run(port, O.MODEL_TEST, setup, recs, 1)
+    assert g.shape[0] == n
+    assert g["b_buffer_count"].mean() > 10
+    assert np.array_equal(g["b_buffer_count"], o["b_buffer_count"])
+    assert normwise(g["b_buffer"][:, :3], o["b_buffer"][:, :3]) < 1e-5
