@@ -111,37 +111,37 @@ typedef struct TayState TayState;
 typedef struct TayGroup TayGroup;
 typedef struct TayPass TayPass;
 
-TayState *tay_create_state(void);
-void tay_destroy_state(TayState *state);
-int tay_switch_to_ocl(TayState *state);
-int tay_switch_to_host(TayState *state);
+TayState *tay_create_state(void); /* tay/tay.h:87, tay/state.c:11 */
+void tay_destroy_state(TayState *state); /* tay/tay.h:88, tay/state.c:35 */
+int tay_switch_to_ocl(TayState *state); /* tay/tay.h:89, tay/state.c:42 */
+int tay_switch_to_host(TayState *state); /* tay/tay.h:90, tay/state.c:50 */
 
-TayError tay_get_error(TayState *state);
+TayError tay_get_error(TayState *state); /* tay/tay.h:92, tay/state.c:59 */
 
-TayGroup *tay_add_group(TayState *state, unsigned agent_size, unsigned agent_capacity, int is_point);
-void tay_configure_space(TayState *state, TayGroup *group, TaySpaceType space_type, int space_dims, float4 min_part_sizes, int shared_size_in_megabytes);
-void tay_fix_space_box(TayState *state, TayGroup *group, float4 min, float4 max);
+TayGroup *tay_add_group(TayState *state, unsigned agent_size, unsigned agent_capacity, int is_point); /* tay/tay.h:94, tay/state.c:73 */
+void tay_configure_space(TayState *state, TayGroup *group, TaySpaceType space_type, int space_dims, float4 min_part_sizes, int shared_size_in_megabytes); /* tay/tay.h:95, tay/state.c:109 */
+void tay_fix_space_box(TayState *state, TayGroup *group, float4 min, float4 max); /* tay/tay.h:96, tay/state.c:120 */
 
-void tay_add_see(TayState *state, TayGroup *seer_group, TayGroup *seen_group, void (*func)(void *, void *, void *), char *func_name, float4 radii, int self_see, void *context, unsigned context_size);
-void tay_add_act(TayState *state, TayGroup *act_group, void (*func)(void *, void *), char *func_name, void *context, unsigned context_size);
+void tay_add_see(TayState *state, TayGroup *seer_group, TayGroup *seen_group, void (*func)(void *, void *, void *), char *func_name, float4 radii, int self_see, void *context, unsigned context_size); /* tay/tay.h:98, tay/state.c:135 */
+void tay_add_act(TayState *state, TayGroup *act_group, void (*func)(void *, void *), char *func_name, void *context, unsigned context_size); /* tay/tay.h:99, tay/state.c:149 */
 
-void tay_clear_all_agents(TayState *state, TayGroup *group);
-void *tay_get_available_agent(TayState *state, TayGroup *group);
-void tay_commit_available_agent(TayState *state, TayGroup *group);
-void *tay_get_agent(TayState *state, TayGroup *group, int index);
+void tay_clear_all_agents(TayState *state, TayGroup *group); /* tay/tay.h:101, tay/state.c:160 */
+void *tay_get_available_agent(TayState *state, TayGroup *group); /* tay/tay.h:102, tay/state.c:166 */
+void tay_commit_available_agent(TayState *state, TayGroup *group); /* tay/tay.h:103, tay/state.c:172 */
+void *tay_get_agent(TayState *state, TayGroup *group, int index); /* tay/tay.h:104, tay/state.c:178 */
 
-void tay_simulation_start(TayState *state);
-int tay_run(TayState *state, int steps);
-void tay_simulation_end(TayState *state);
+void tay_simulation_start(TayState *state); /* tay/tay.h:106, tay/state.c:183 */
+int tay_run(TayState *state, int steps); /* tay/tay.h:107, tay/state.c:194-323 */
+void tay_simulation_end(TayState *state); /* tay/tay.h:108, tay/state.c:325 */
 
-double tay_get_ms_per_step_for_last_run(TayState *state);
-void tay_log(void *file, char *fmt, ...);
+double tay_get_ms_per_step_for_last_run(TayState *state); /* tay/tay.h:110, tay/state.c:336 */
+void tay_log(void *file, char *fmt, ...); /* tay/tay.h:111, tay/thread.c:206 */
 
-void ocl_add_source(TayState *state, const char *source);
+void ocl_add_source(TayState *state, const char *source); /* tay/tay.h:113, tay/ocl.c:274 */
 
-void tay_threads_start(unsigned threads_count, unsigned thread_storage_size);
-void tay_threads_stop(void);
-unsigned tay_get_number_of_threads(void);
+void tay_threads_start(unsigned threads_count, unsigned thread_storage_size); /* tay/tay.h:115, tay/thread.c:70 */
+void tay_threads_stop(void); /* tay/tay.h:116, tay/thread.c:116 */
+unsigned tay_get_number_of_threads(void); /* tay/tay.h:117, tay/thread.c:120 */
 
 /* NEW: advances `count` states by `steps` steps together: every state must hold one
  * TAY_GPU_Z_GRID group running the same device model and pass sequence (agent counts,
