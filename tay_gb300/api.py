@@ -319,6 +319,12 @@ class Batch:
         self._check(self.L.tgpu_batch_fetch(self.ptr, i, out.ctypes.data), "tgpu_batch_fetch")
         return out
 
+    def write_through(self, i, host_ptr):
+        """tgpu_batch_write_through: the last step of every following run stores group i's
+        records into the page-locked buffer at host_ptr (an int address, e.g. from
+        host_alloc); None turns it off."""
+        self._check(self.L.tgpu_batch_write_through(self.ptr, i, host_ptr), "tgpu_batch_write_through")
+
     def profile(self, steps):
         n = self.L.tgpu_batch_kernel_classes(self.ptr)
         ms = (ctypes.c_double * n)()

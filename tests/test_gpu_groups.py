@@ -193,3 +193,29 @@ def test_write_through_equals_one_run(gpu, host_loop):
     b = M.run_groups(dtype, funcs, groups, COMBO_FULL, see, act, 50.0, 50.0, 4, host_loop=host_loop)
     for x, y in zip(a, b):
         assert x.tobytes() == y.tobytes()
+
+
+def test_engine_write_through_equals_fetch(gpu):
+    """Engine ABI: after a run with write-through into page-locked memory, the buffer holds
+    exactly what tgpu_batch_fetch returns; pageable memory is refused."""
+    ps = W.boids_points(50000, seed=49, clusters=4, side=300.0)
+    recs = M.records(M.BOIDS_RECORD, ps.p, ps.v)
+    setup = M.boids_setup()
+    b = api.Batch([(setup, recs)])
+    L = api.lib()
+    host = L.tgpu_host_alloc(recs.nbytes)
+    try:
+        b.push()
+        with pytest.raises(api.TayError):
+            b.write_through(0, recs.ctypes.data)  # pageable
+        b.write_through(0, host)
+        b.run(3)
+        got = np.frombuffer(ctypes.string_at(host, recs.nbytes), dtype=recs.dtype).copy()
+        assert got.tobytes() == b.fetch(0).tobytes()
+        b.write_through(0, None)
+        b.run(1)
+        stale = np.frombuffer(ctypes.string_at(host, recs.nbytes), dtype=recs.dtype)
+        assert stale.tobytes() == got.tobytes()  # turned off: the buffer keeps the last write
+    finally:
+        b.close()
+        L.tgpu_host_free(host)
