@@ -328,6 +328,9 @@ SortLaunch tgpu::sort_launch(TgpuBatch *b) {
 
 namespace {
 
+// Segments up to which a row-order step clears its table with one memset per segment.
+constexpr int kMemsetClearSegments = 4;
+
 void mark(const StepEvents *e, int k, cudaStream_t st) {
     if (e) cudaEventRecord(e->ev[k], st);
 }
@@ -462,7 +465,14 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E, bool write_through) {
     // write-through when the last pass is not one see over every segment: after the step
     if (write_through && !written) unpack_range(b, 0, b->total, st);
     if (E) cudaEventRecord(E->ev2[0], st);
-    launch_cell_table(L, skeys, 0, st);
+    if (b->cell_order == kOrderRows && b->nseg <= kMemsetClearSegments) {
+        // row order: zeroing each segment's header region clears every row (entries are
+        // read only inside a row's span), one short memset instead of a pass over the keys
+        for (int s = 0; s < b->nseg; ++s)
+            cudaMemsetAsync(b->table + b->specs[s].table_base, 0, (size_t)b->specs[s].row_cap * sizeof(uint4), st);
+    } else {
+        launch_cell_table(L, skeys, 0, st);
+    }
     if (E) cudaEventRecord(E->ev2[1], st);
 }
 
