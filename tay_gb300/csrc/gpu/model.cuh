@@ -28,7 +28,8 @@ struct KernelDesc {
     uint32_t seen_f4;                  // float4 streams read from other agents (staged)
     int staged_f4;                     // number of staged float4 streams per agent
     // launch with the descriptor filled by the runtime
-    void (*launch_see)(const SeeLaunch &L, size_t smem, cudaStream_t st);
+    // returns true when it stored the records through L.wt (the pass declares a Codec)
+    bool (*launch_see)(const SeeLaunch &L, size_t smem, cudaStream_t st);
     void (*launch_act)(const ActLaunch &L, cudaStream_t st);
     cudaError_t (*prepare)(size_t smem);  // raises the kernel's dynamic shared memory limit
     int accumulates;                   // see kernel adds onto the seer's stored fields (several see
@@ -64,12 +65,12 @@ struct ModelDesc {
 
 // The SPH model's adjoint kernels (used by adjoint.cu).
 struct SphAdjointKernels {
-    void (*force_record)(const SeeLaunch &L, size_t smem, cudaStream_t st);  // force + integrate, also stores a
+    bool (*force_record)(const SeeLaunch &L, size_t smem, cudaStream_t st);  // force + integrate, also stores a
     cudaError_t (*force_record_prepare)(size_t smem);
     void (*integrate_adj)(const ActLaunch &L, cudaStream_t st);
-    void (*force_adj)(const SeeLaunch &L, size_t smem, cudaStream_t st);
+    bool (*force_adj)(const SeeLaunch &L, size_t smem, cudaStream_t st);
     cudaError_t (*force_adj_prepare)(size_t smem);
-    void (*density_adj)(const SeeLaunch &L, size_t smem, cudaStream_t st);
+    bool (*density_adj)(const SeeLaunch &L, size_t smem, cudaStream_t st);
     cudaError_t (*density_adj_prepare)(size_t smem);
     void (*scatter_adj)(const ActLaunch &L, cudaStream_t st);
     uint32_t ctx_bytes;
@@ -83,8 +84,8 @@ const ModelDesc *model_box();
 
 // helpers used by the model translation units
 template <class P>
-void launch_see_t(const SeeLaunch &L, size_t smem, cudaStream_t st) {
-    if (!L.ctas) return;
+bool launch_see_t(const SeeLaunch &L, size_t smem, cudaStream_t st) {
+    if (!L.ctas) return L.wt != nullptr;  // nothing to write
     if constexpr (!std::is_void_v<typename see_detail::CodecOf<P>::type>) {
         // write-through launch (the last pass of a run): the walk without row staging
         if (L.wt) {
@@ -92,7 +93,7 @@ void launch_see_t(const SeeLaunch &L, size_t smem, cudaStream_t st) {
                 see_rows_kernel<P, false, true><<<L.ctas, kSeeThreads, 0, st>>>(L);
             else
                 see_kernel<P, true><<<L.ctas, kSeeThreads, smem, st>>>(L);
-            return;
+            return true;
         }
     }
     if (L.rows && L.stage_cap)
@@ -101,6 +102,7 @@ void launch_see_t(const SeeLaunch &L, size_t smem, cudaStream_t st) {
         see_rows_kernel<P><<<L.ctas, kSeeThreads, 0, st>>>(L);
     else
         see_kernel<P><<<L.ctas, kSeeThreads, smem, st>>>(L);
+    return false;
 }
 template <class A>
 void launch_act_t(const ActLaunch &L, cudaStream_t st) {

@@ -439,9 +439,10 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E, bool write_through) {
             if (write_through && last && r.seer_seg < 0) {
                 S.wt = b->d_wt;
                 S.wt_program = unpack_program(b);
-                written = true;
             }
-            r.k->launch_see(S, r.smem, st);
+            // a pass without a record codec does not write through; the records are then
+            // unpacked after the step
+            if (r.k->launch_see(S, r.smem, st) && S.wt) written = true;
             for (int c = 0; c < b->m->nf4; ++c)
                 if (b->m->role_f4[c] == kState && (r.k->writes_f4 >> c & 1u) && (r.k->seen_f4 >> c & 1u))
                     b->cur_f4[c] ^= 1;
