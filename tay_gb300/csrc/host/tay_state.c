@@ -537,6 +537,7 @@ static int cache_matches(TayState **states, int count) {
 
 /* Builds (or reuses) the cached batch of `states`; returns it or NULL with errors set. */
 static TgpuBatch *batch_for(TayState **states, int count) {
+    if (count <= 0) return 0;
     for (int i = 0; i < count; ++i) {
         if (!states[i]->is_running) {
             set_error(states[i], TAY_ERROR_STATE_STATUS, "cannot run simulation steps if simulation is not started");
