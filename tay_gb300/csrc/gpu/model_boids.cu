@@ -221,10 +221,10 @@ constexpr uint32_t bit(int k) { return 1u << k; }
 
 const KernelDesc kKernels[] = {
     {"boids_see", nullptr, bit(ACC0) | bit(ACC1) | bit(ACC2), 0, bit(POS) | bit(VEL), 2, launch_see_t<SeeOnly>, nullptr,
-     prepare_see_t<SeeOnly>},
+     prepare_see_t<SeeOnly>, 0},
     {"boids_see", "boids_act", bit(POS) | bit(VEL), 0, bit(POS) | bit(VEL), 2, launch_see_t<SeeAct>, nullptr,
-     prepare_see_t<SeeAct>},
-    {nullptr, "boids_act", bit(POS) | bit(VEL), 0, 0, 0, nullptr, launch_act_t<Act>, nullptr},
+     prepare_see_t<SeeAct>, 0},
+    {nullptr, "boids_act", bit(POS) | bit(VEL), 0, 0, 0, nullptr, launch_act_t<Act>, nullptr, 0},
 };
 
 const ProgramDesc kPrograms[] = {
@@ -235,7 +235,7 @@ const ProgramDesc kPrograms[] = {
 
 const ModelDesc kModel = {
     "boids", 104, 5, 1, {kState, kState, kStep, kStep, kStep}, {kState}, (uint32_t)sizeof(Ctx), (uint32_t)sizeof(Ctx),
-    kKernels, 3, kPrograms, 3, pack_t<Codec>, unpack_t<Codec>,
+    kKernels, 3, kPrograms, 3, pack_t<Codec>, unpack_t<Codec>, 0,
 };
 
 }  // namespace boids

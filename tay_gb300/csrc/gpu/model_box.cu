@@ -186,9 +186,9 @@ const KernelDesc kKernels[] = {
     {"box_agent_see", nullptr, bit(BBUF), 0, bit(MIN) | bit(MAX), 1, launch_see_t<SeeOnly>, nullptr,
      prepare_see_t<SeeOnly>, 1},
     {"box_agent_see", "box_agent_act", bit(MIN) | bit(MAX) | bit(VEL) | bit(BBUF) | bit(FBUF), 0, bit(MIN) | bit(MAX), 1,
-     launch_see_t<SeeAct>, nullptr, prepare_see_t<SeeAct>},
+     launch_see_t<SeeAct>, nullptr, prepare_see_t<SeeAct>, 0},
     {nullptr, "box_agent_act", bit(MIN) | bit(MAX) | bit(VEL) | bit(BBUF) | bit(FBUF), 0, 0, 0, nullptr,
-     launch_act_t<Act>, nullptr},
+     launch_act_t<Act>, nullptr, 0},
 };
 
 const ProgramDesc kPrograms[] = {

@@ -210,13 +210,13 @@ constexpr uint32_t bit(int k) { return 1u << k; }
 
 const KernelDesc kKernels[] = {
     {"sph_density", nullptr, bit(RP), 0, bit(POS), 1, launch_see_t<Density<false>>, nullptr,
-     prepare_see_t<Density<false>>},
+     prepare_see_t<Density<false>>, 0},
     {"sph_density", "sph_pressure", bit(RP), 0, bit(POS), 1, launch_see_t<Density<true>>, nullptr,
-     prepare_see_t<Density<true>>},
+     prepare_see_t<Density<true>>, 0},
     {"sph_force", nullptr, bit(ACC), 0, bit(POS) | bit(VEL) | bit(RP), 3, launch_see_t<Force<false>>, nullptr,
-     prepare_see_t<Force<false>>},
+     prepare_see_t<Force<false>>, 0},
     {"sph_force", "sph_integrate", bit(POS) | bit(VEL), 0, bit(POS) | bit(VEL) | bit(RP), 3,
-     launch_see_t<Force<true>>, nullptr, prepare_see_t<Force<true>>},
+     launch_see_t<Force<true>>, nullptr, prepare_see_t<Force<true>>, 0},
 };
 
 const ProgramDesc kPrograms[] = {
@@ -420,7 +420,7 @@ const SphAdjointKernels kAdjoint = {
 
 const ModelDesc kModel = {
     "sph", 72, 4, 1, {kState, kState, kStep, kStep}, {kState}, (uint32_t)sizeof(Ctx), (uint32_t)sizeof(Ctx),
-    kKernels, 4, kPrograms, 4, pack_t<Codec>, unpack_t<Codec>,
+    kKernels, 4, kPrograms, 4, pack_t<Codec>, unpack_t<Codec>, 0,
 };
 
 }  // namespace sph

@@ -168,8 +168,8 @@ constexpr uint32_t bit(int k) { return 1u << k; }
 const KernelDesc kKernels[] = {
     {"agent_see", nullptr, bit(BBUF), 0, bit(POS), 1, launch_see_t<SeeOnly>, nullptr, prepare_see_t<SeeOnly>, 1},
     {"agent_see", "agent_act", bit(POS) | bit(VEL) | bit(BBUF) | bit(FBUF), 0, bit(POS), 1, launch_see_t<SeeAct>,
-     nullptr, prepare_see_t<SeeAct>},
-    {nullptr, "agent_act", bit(POS) | bit(VEL) | bit(BBUF) | bit(FBUF), 0, 0, 0, nullptr, launch_act_t<Act>, nullptr},
+     nullptr, prepare_see_t<SeeAct>, 0},
+    {nullptr, "agent_act", bit(POS) | bit(VEL) | bit(BBUF) | bit(FBUF), 0, 0, 0, nullptr, launch_act_t<Act>, nullptr, 0},
 };
 
 const ProgramDesc kPrograms[] = {
@@ -180,7 +180,7 @@ const ProgramDesc kPrograms[] = {
 
 const ModelDesc kModel = {
     "test_basic", 80, 4, 0, {kState, kState, kState, kState}, {}, (uint32_t)sizeof(SeeCtx), (uint32_t)sizeof(ActCtx),
-    kKernels, 3, kPrograms, 3, pack_t<Codec>, unpack_t<Codec>,
+    kKernels, 3, kPrograms, 3, pack_t<Codec>, unpack_t<Codec>, 0,
 };
 
 }  // namespace test_basic
