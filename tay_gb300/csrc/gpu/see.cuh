@@ -674,7 +674,9 @@ __global__ void __launch_bounds__(kSeeThreads, kStage ? 1 : 8) see_rows_kernel(S
                     mbar_wait_bounded(bar);
                 }
                 staged = __syncthreads_and(staged);
-                if (threadIdx.x == 0) mbar_inval(bar);  // every thread has left the wait
+                // every thread has left the wait; a barrier whose copies may still be pending
+                // (the waits ran out) is not invalidated
+                if (staged && threadIdx.x == 0) mbar_inval(bar);
                 if (staged) {
                     const SmemSeen sacc{stage, L.stage_cap};
                     if (active) {
