@@ -142,7 +142,8 @@ int tgpu_batch_profile(TgpuBatch *batch, int steps, double *ms, int n);
  * out[0] candidates box-tested (broad phase; out[0] vs pairs gives the neighbour-finding
  * efficiency), out[1] see CTAs that staged their halo in shared memory, out[2] see CTAs
  * that read it from global memory, out[3] warps that walked their union box, out[4]
- * warps whose lanes walked their own boxes. */
+ * warps whose lanes walked their own boxes, out[5] warps that replayed a pair list
+ * (pair_list_cap) instead of walking. */
 int tgpu_batch_telemetry(const TgpuBatch *batch, unsigned long long *out, int n);
 
 /* Number of kernel classes tgpu_batch_profile reports (4 + pass kernels). */
@@ -181,7 +182,12 @@ int tgpu_batch_program(const TgpuBatch *batch);
  *   hit_masks      cell order 1: each lane box-tests up to 32 candidates into a mask
  *                  before the lanes run the see function over their hits together
  *   x_cell_factor  cell order 1: x cells are this fraction of the y / z cells (finer x
- *                  cells tighten each row's candidate range without adding rows) */
+ *                  cells tighten each row's candidate range without adding rows)
+ *   pair_list_cap  cell order 1, no staging or hit masks: entries per agent of the pair
+ *                  list a see pass records for the next see pass over the same positions
+ *                  when the model pairs them (SPH density -> force), rounded up to a
+ *                  multiple of 4; agents with more pairs are walked again.  0: no pair
+ *                  lists */
 typedef struct TgpuTuning {
     int stage;
     unsigned stage_cap;
@@ -192,6 +198,7 @@ typedef struct TgpuTuning {
     unsigned cell_order;
     unsigned hit_masks;
     float x_cell_factor;
+    unsigned pair_list_cap;
 } TgpuTuning;
 
 void tgpu_set_tuning(const TgpuTuning *tuning);  /* NULL restores the defaults */

@@ -333,11 +333,11 @@ class Batch:
 
     def telemetry(self):
         """Counters of the last run: candidates tested, pairs, staged / global CTAs,
-        union / per-lane warps."""
+        union / per-lane warps, warps that replayed a pair list."""
         out = (ctypes.c_ulonglong * 8)()
         self._check(self.L.tgpu_batch_telemetry(self.ptr, out, 8), "tgpu_batch_telemetry")
         return {"candidates": out[0], "pairs": self.L.tgpu_batch_last_pairs(self.ptr), "staged_ctas": out[1],
-                "global_ctas": out[2], "union_warps": out[3], "lane_warps": out[4]}
+                "global_ctas": out[2], "union_warps": out[3], "lane_warps": out[4], "replay_warps": out[5]}
 
     def flush_l2(self):
         self._check(self.L.tgpu_batch_flush_l2(self.ptr), "tgpu_batch_flush_l2")
@@ -370,7 +370,8 @@ def run_batch(states, steps):
 class TgpuTuning(ctypes.Structure):
     _fields_ = [("stage", ctypes.c_int), ("stage_cap", ctypes.c_uint), ("stage_cells", ctypes.c_uint),
                 ("cell_multiple", ctypes.c_float), ("union_factor", ctypes.c_uint), ("use_graphs", ctypes.c_int),
-                ("cell_order", ctypes.c_uint), ("hit_masks", ctypes.c_uint), ("x_cell_factor", ctypes.c_float)]
+                ("cell_order", ctypes.c_uint), ("hit_masks", ctypes.c_uint), ("x_cell_factor", ctypes.c_float),
+                ("pair_list_cap", ctypes.c_uint)]
 
 
 def get_tuning() -> dict:
@@ -381,7 +382,8 @@ def get_tuning() -> dict:
 
 def set_tuning(**kw):
     """Sets tuning fields (stage, stage_cap, stage_cells, cell_multiple, union_factor,
-    use_graphs, cell_order, hit_masks, x_cell_factor) for batches created afterwards; no arguments restores the defaults."""
+    use_graphs, cell_order, hit_masks, x_cell_factor, pair_list_cap) for batches created afterwards; no arguments
+    restores the defaults."""
     if not kw:
         lib().tgpu_set_tuning(None)
         return

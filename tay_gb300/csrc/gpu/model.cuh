@@ -34,6 +34,8 @@ struct KernelDesc {
     cudaError_t (*prepare)(size_t smem);  // raises the kernel's dynamic shared memory limit
     int accumulates;                   // see kernel adds onto the seer's stored fields (several see
                                        // passes of one group accumulate); 0: starts from zero
+    int pair_list;                     // 1: can record a pair list for the next see pass (P::keep);
+                                       // 2: can replay the previous pass's list (P::replay_ok)
 };
 
 // A supported pass sequence: the func names in registration order, and the kernels

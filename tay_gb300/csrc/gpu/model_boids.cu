@@ -5,7 +5,10 @@
 // separation from neighbours inside sep_r.
 //   see(a, b):  d = b.p - a.p, d2 = (dx*dx + dy*dy) + dz*dz, each product and sum rounded
 //               separately (no FMA), so the neighbour decisions are bit-identical to an
-//               IEEE evaluation of the same expression on the CPU;
+//               IEEE evaluation of the same expression on the CPU (the separation term's
+//               products too: a product the compiler may fuse into the sum in one inlined
+//               copy of the see body and not in another would make results depend on the
+//               walk);
 //               if 0 < d2 < r2:   count++, coh += d, ali += b.v
 //                  if d2 < sep_r2: sep_count++, sep -= d * (1 / d2)
 //   act(a):     for (vec, n, w) in (sep, sep_count, w_sep), (ali, count, w_ali),
@@ -64,9 +67,9 @@ TGPU_D void see_fn(Seer &s, const float4 &a, const float4 &b, const Acc &acc, ui
         if (d2 < c.sep_r2) {
             const float inv = __frcp_rn(d2);
             s.sep_count += 1;
-            s.sx -= dx * inv;
-            s.sy -= dy * inv;
-            s.sz -= dz * inv;
+            s.sx -= __fmul_rn(dx, inv);
+            s.sy -= __fmul_rn(dy, inv);
+            s.sz -= __fmul_rn(dz, inv);
         }
     }
 }
@@ -221,10 +224,10 @@ constexpr uint32_t bit(int k) { return 1u << k; }
 
 const KernelDesc kKernels[] = {
     {"boids_see", nullptr, bit(ACC0) | bit(ACC1) | bit(ACC2), 0, bit(POS) | bit(VEL), 2, launch_see_t<SeeOnly>, nullptr,
-     prepare_see_t<SeeOnly>, 0},
+     prepare_see_t<SeeOnly>, 0, 0},
     {"boids_see", "boids_act", bit(POS) | bit(VEL), 0, bit(POS) | bit(VEL), 2, launch_see_t<SeeAct>, nullptr,
-     prepare_see_t<SeeAct>, 0},
-    {nullptr, "boids_act", bit(POS) | bit(VEL), 0, 0, 0, nullptr, launch_act_t<Act>, nullptr, 0},
+     prepare_see_t<SeeAct>, 0, 0},
+    {nullptr, "boids_act", bit(POS) | bit(VEL), 0, 0, 0, nullptr, launch_act_t<Act>, nullptr, 0, 0},
 };
 
 const ProgramDesc kPrograms[] = {

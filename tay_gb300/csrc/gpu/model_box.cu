@@ -184,11 +184,11 @@ constexpr uint32_t bit(int k) { return 1u << k; }
 
 const KernelDesc kKernels[] = {
     {"box_agent_see", nullptr, bit(BBUF), 0, bit(MIN) | bit(MAX), 1, launch_see_t<SeeOnly>, nullptr,
-     prepare_see_t<SeeOnly>, 1},
+     prepare_see_t<SeeOnly>, 1, 0},
     {"box_agent_see", "box_agent_act", bit(MIN) | bit(MAX) | bit(VEL) | bit(BBUF) | bit(FBUF), 0, bit(MIN) | bit(MAX), 1,
-     launch_see_t<SeeAct>, nullptr, prepare_see_t<SeeAct>, 0},
+     launch_see_t<SeeAct>, nullptr, prepare_see_t<SeeAct>, 0, 0},
     {nullptr, "box_agent_act", bit(MIN) | bit(MAX) | bit(VEL) | bit(BBUF) | bit(FBUF), 0, 0, 0, nullptr,
-     launch_act_t<Act>, nullptr, 0},
+     launch_act_t<Act>, nullptr, 0, 0},
 };
 
 const ProgramDesc kPrograms[] = {

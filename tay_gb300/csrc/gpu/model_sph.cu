@@ -10,7 +10,11 @@
 //                            Pi_ij = -alpha c0 mu_ij / rho_bar when v_ij.x_ij < 0,
 //                            mu_ij = h v_ij.x_ij / (r^2 + 0.01 h^2)
 // integrate:                 v += dt (a + g); x += dt v; walls: clamp, v *= -0.5
-// The neighbour decision r2 < (2h)^2 uses separately rounded products and sums.
+// The neighbour decision r2 < (2h)^2 uses separately rounded products and sums.  Every
+// multiply-add of the see functions is an explicit fused one, and 2 - q after q = r / h is
+// an explicitly rounded subtraction (a plain one may be fused with the product in one
+// inlined copy and not in another): each copy of a see body (row walk, union walk,
+// recording walk, list replay) and of the integrate epilogue rounds the same way.
 //
 // AoS record (72 bytes): tag u32[2] @0, p float4 @8, v float4 @24, a float4 @40,
 // rho @56, P @60, id @64, pad @68.
@@ -35,19 +39,19 @@ struct Ctx {
 TGPU_D float kernel_w(float q, float sigma) {
     if (q < 1.0f) {
         const float q2 = q * q;
-        return sigma * ((1.0f - 1.5f * q2) + 0.75f * (q2 * q));
+        return sigma * __fmaf_rn(0.75f, q2 * q, __fmaf_rn(-1.5f, q2, 1.0f));
     }
     if (q < 2.0f) {
-        const float t = 2.0f - q;
+        const float t = __fsub_rn(2.0f, q);
         return sigma * (0.25f * ((t * t) * t));
     }
     return 0.0f;
 }
 
 TGPU_D float kernel_dw(float q, float sigma, float inv_h) {
-    if (q < 1.0f) return (sigma * inv_h) * (-3.0f * q + 2.25f * (q * q));
+    if (q < 1.0f) return (sigma * inv_h) * __fmaf_rn(2.25f, q * q, -3.0f * q);
     if (q < 2.0f) {
-        const float t = 2.0f - q;
+        const float t = __fsub_rn(2.0f, q);
         return -(sigma * inv_h) * (0.75f * (t * t));
     }
     return 0.0f;
@@ -89,14 +93,20 @@ struct Density {
     using ActCtx = Ctx;
     using Seer = DensitySeer;
     static constexpr int kSeenF4 = 1;
+    // records the pairs inside the support for the force pass that follows (positions do
+    // not change between the two)
+    static constexpr int kPairList = 1;
     TGPU_D static int seen_stream(int) { return POS; }
+    TGPU_D static bool keep(const float4 &a, const float4 &b, const Ctx &c) {
+        return dist2(a.x - b.x, a.y - b.y, a.z - b.z) < c.support2;
+    }
     TGPU_D static void load(Seer &s, const PassIO &, uint32_t, const Ctx &, const Ctx &) { s.rho = 0.0f; }
     template <class Acc>
     TGPU_D static void see(Seer &s, const float4 &a, const float4 &b, const Acc &, uint32_t, const Ctx &c) {
         const float r2 = dist2(a.x - b.x, a.y - b.y, a.z - b.z);
         if (r2 < c.support2) {
             const float q = __fsqrt_rn(r2) * c.inv_h;
-            s.rho += c.m * kernel_w(q, c.sigma);
+            s.rho = __fmaf_rn(c.m, kernel_w(q, c.sigma), s.rho);
         }
     }
     TGPU_D static void finish(Seer &s, const float4 &, const PassIO &io, uint32_t i, const Ctx &c, const Ctx &) {
@@ -121,6 +131,11 @@ struct Force {
     using ActCtx = Ctx;
     using Seer = ForceSeer;
     static constexpr int kSeenF4 = 3;
+    // replays the density pass's list: its keep test (r2 < that pass's support2) admits
+    // every pair this see function acts on (r2 < support2, r2 > 0) when the support is not
+    // wider here; for the other candidates the see function does nothing
+    static constexpr int kPairList = 2;
+    TGPU_D static bool replay_ok(const Ctx &mine, const Ctx &rec) { return mine.support2 <= rec.support2; }
     TGPU_D static int seen_stream(int k) { return k == 0 ? POS : (k == 1 ? VEL : RP); }
     TGPU_D static void load(Seer &s, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {
         s.ax = s.ay = s.az = 0.0f;
@@ -143,16 +158,16 @@ struct Force {
             const float q = r * c.inv_h;
             const float dw = kernel_dw(q, c.sigma, c.inv_h);
             const float vx = s.v.x - bv.x, vy = s.v.y - bv.y, vz = s.v.z - bv.z;
-            const float vr = (vx * dx + vy * dy) + vz * dz;
+            const float vr = __fmaf_rn(vz, dz, __fmaf_rn(vy, dy, vx * dx));
             float visc = 0.0f;
             if (vr < 0.0f) {
                 const float rho_bar = 0.5f * (s.rho + brp.x);
                 visc = -(c.alpha * c.c0 * (c.h * vr)) / ((r2 + c.eta2) * rho_bar);
             }
             const float coef = -c.m * ((s.A + brp.z) + visc) * (dw * inv_r);
-            s.ax += coef * dx;
-            s.ay += coef * dy;
-            s.az += coef * dz;
+            s.ax = __fmaf_rn(coef, dx, s.ax);
+            s.ay = __fmaf_rn(coef, dy, s.ay);
+            s.az = __fmaf_rn(coef, dz, s.az);
         }
     }
     TGPU_D static void finish(Seer &s, const float4 &a, const PassIO &io, uint32_t i, const Ctx &, const Ctx &c) {
@@ -163,8 +178,8 @@ struct Force {
         const float acc[3] = {s.ax, s.ay, s.az};
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            v[k] = v[k] + c.dt * (acc[k] + c.g[k]);
-            p[k] = p[k] + c.dt * v[k];
+            v[k] = __fmaf_rn(c.dt, acc[k] + c.g[k], v[k]);
+            p[k] = __fmaf_rn(c.dt, v[k], p[k]);
         }
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
@@ -210,13 +225,13 @@ constexpr uint32_t bit(int k) { return 1u << k; }
 
 const KernelDesc kKernels[] = {
     {"sph_density", nullptr, bit(RP), 0, bit(POS), 1, launch_see_t<Density<false>>, nullptr,
-     prepare_see_t<Density<false>>, 0},
+     prepare_see_t<Density<false>>, 0, 0},
     {"sph_density", "sph_pressure", bit(RP), 0, bit(POS), 1, launch_see_t<Density<true>>, nullptr,
-     prepare_see_t<Density<true>>, 0},
+     prepare_see_t<Density<true>>, 0, 1},
     {"sph_force", nullptr, bit(ACC), 0, bit(POS) | bit(VEL) | bit(RP), 3, launch_see_t<Force<false>>, nullptr,
-     prepare_see_t<Force<false>>, 0},
+     prepare_see_t<Force<false>>, 0, 2},
     {"sph_force", "sph_integrate", bit(POS) | bit(VEL), 0, bit(POS) | bit(VEL) | bit(RP), 3,
-     launch_see_t<Force<true>>, nullptr, prepare_see_t<Force<true>>, 0},
+     launch_see_t<Force<true>>, nullptr, prepare_see_t<Force<true>>, 0, 2},
 };
 
 const ProgramDesc kPrograms[] = {

@@ -166,10 +166,10 @@ struct Codec {
 constexpr uint32_t bit(int k) { return 1u << k; }
 
 const KernelDesc kKernels[] = {
-    {"agent_see", nullptr, bit(BBUF), 0, bit(POS), 1, launch_see_t<SeeOnly>, nullptr, prepare_see_t<SeeOnly>, 1},
+    {"agent_see", nullptr, bit(BBUF), 0, bit(POS), 1, launch_see_t<SeeOnly>, nullptr, prepare_see_t<SeeOnly>, 1, 0},
     {"agent_see", "agent_act", bit(POS) | bit(VEL) | bit(BBUF) | bit(FBUF), 0, bit(POS), 1, launch_see_t<SeeAct>,
-     nullptr, prepare_see_t<SeeAct>, 0},
-    {nullptr, "agent_act", bit(POS) | bit(VEL) | bit(BBUF) | bit(FBUF), 0, 0, 0, nullptr, launch_act_t<Act>, nullptr, 0},
+     nullptr, prepare_see_t<SeeAct>, 0, 0},
+    {nullptr, "agent_act", bit(POS) | bit(VEL) | bit(BBUF) | bit(FBUF), 0, 0, 0, nullptr, launch_act_t<Act>, nullptr, 0, 0},
 };
 
 const ProgramDesc kPrograms[] = {

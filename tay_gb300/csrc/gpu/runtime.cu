@@ -58,6 +58,9 @@ TgpuTuning default_tuning() {
     t.cell_order = 1;
     t.hit_masks = 0;
     t.x_cell_factor = 0.5f;
+    // 251 lattice neighbours lie inside the SPH benchmark's support (2h = 4 spacings),
+    // with room for compression
+    t.pair_list_cap = 320;
     return t;
 }
 TgpuTuning g_tuning = default_tuning();
@@ -125,6 +128,8 @@ void free_batch(TgpuBatch *b) {
     cudaFree(b->d_aos);
     cudaFree(b->d_pairs);
     cudaFree(b->d_telemetry);
+    cudaFree(b->plist_idx);
+    cudaFree(b->plist_count);
     for (auto &r : b->runs) {
         cudaFree(r.d_radii);
         cudaFree(r.d_see_ctx);
@@ -434,6 +439,17 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E, bool write_through) {
             S.pairs = b->d_pairs;
             S.telemetry = b->d_telemetry;
             S.io = io;
+            if (r.list_mode) {
+                S.plist.idx = b->plist_idx;
+                S.plist.count = b->plist_count;
+                S.plist.stride = b->total;
+                S.plist.cap = b->plist_cap;
+                S.plist.mode = r.list_mode;
+                if (r.list_mode == 2u) {
+                    S.plist.rec_radii = b->runs[r.list_src].d_radii;
+                    S.plist.rec_ctx = b->runs[r.list_src].d_see_ctx;
+                }
+            }
             // Write-through on the final pass over every segment: each CTA stores its seers'
             // finished records to the host as it ends, so the host link overlaps the pass.
             if (write_through && last && r.seer_seg < 0) {
@@ -527,6 +543,7 @@ unsigned long long tgpu_batch_device_bytes(const TgpuBatch *b) {
     bytes += 256ull * 4 * (b->tiles ? b->tiles : 1);
     bytes += b->table_entries * sizeof(uint2);
     bytes += n * b->m->agent_bytes;
+    if (b->plist_idx) bytes += n * (4ull * b->plist_cap + sizeof(uint2));
     return bytes;
 }
 
@@ -781,6 +798,35 @@ int setup_see_run(TgpuBatch *b, KernelRun &r, int self_see) {
     return TGPU_OK;
 }
 
+// Pair lists between consecutive see runs of a batch's program: the first declares it
+// can record (pair_list 1), the next that it can replay (2), and the positions do not
+// change in between.  Row order walks through L1 only (the walks that record), and a
+// list that holds the seer itself unless the replaying pass skips it.  Whether the
+// recorded set covers the replaying pass's pairs depends on the radii and contexts of
+// each run, which can change between runs: the kernel checks that on the device and
+// walks when it does not hold.
+int setup_pair_lists(TgpuBatch *b) {
+    const uint32_t cap = g_tuning.pair_list_cap > 0xFFFFFFF0u ? 0xFFFFFFF0u : (g_tuning.pair_list_cap + 3u) & ~3u;
+    if (!cap || b->cell_order != kOrderRows || b->hit_masks || b->total == 0) return TGPU_OK;
+    bool any = false;
+    for (size_t k = 0; k + 1 < b->runs.size(); ++k) {
+        KernelRun &a = b->runs[k], &c = b->runs[k + 1];
+        if (a.k->pair_list != 1 || c.k->pair_list != 2 || a.list_mode || a.stage_cap || c.stage_cap) continue;
+        if (a.seer_seg >= 0 || c.seer_seg >= 0 || b->m->nonpoint) continue;
+        if (a.k->writes_f4 & 1u) continue;            // positions (stream 0) change in between
+        if (a.skip_self && !c.skip_self) continue;    // the list lacks the seer itself
+        a.list_mode = 1u;
+        c.list_mode = 2u;
+        c.list_src = (int)k;
+        any = true;
+    }
+    if (!any) return TGPU_OK;
+    b->plist_cap = cap;
+    CKR(cudaMalloc(&b->plist_idx, (size_t)(cap / 4u) * b->total * sizeof(uint4)));
+    CKR(cudaMalloc(&b->plist_count, (size_t)b->total * sizeof(uint2)));
+    return TGPU_OK;
+}
+
 #undef CKR
 
 const KernelDesc *find_kernel(const ModelDesc *m, const char *see, const char *act) {
@@ -867,6 +913,7 @@ int tgpu_batch_create(const TgpuGroup *groups, int group_count, TgpuBatch **out)
         }
         b->runs.push_back(r);
     }
+    if (!rc) rc = setup_pair_lists(b);
     for (int s = 0; s < b->nseg && !rc; ++s) rc = upload_contexts(b, s);
     if (rc) {
         free_batch(b);

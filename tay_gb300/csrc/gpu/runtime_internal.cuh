@@ -21,6 +21,8 @@ struct KernelRun {
     int skip_self = 0;
     int seer_seg = -1;  // state batches: the pass's seer (acting) segment; -1: every segment
     int seen_seg = -1;  // state batches: the segment whose agents a see pass reads
+    uint32_t list_mode = 0;  // pair list (PairList): 0 none, 1 record, 2 replay
+    int list_src = -1;       // replay: the run that records the list
 };
 
 struct HostSeg {
@@ -78,6 +80,11 @@ struct TgpuBatch {
     size_t ctx_stride = 0;
     std::vector<KernelRun> runs;
     int launches_per_step = 0;
+    // pair list of a recording see pass for the next one (PairList): [cap / 4][total]
+    // groups of four entries and per agent {entries, box-test passes with other agents}
+    uint4 *plist_idx = nullptr;
+    uint2 *plist_count = nullptr;
+    uint32_t plist_cap = 0;
 
     cudaStream_t st = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;

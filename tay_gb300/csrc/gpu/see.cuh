@@ -106,9 +106,43 @@ TGPU_D float4 load_pos(const float4 *src, uint32_t j, bool global) {
     return global ? __ldg(src + j) : src[j];
 }
 
+// A pass's role in a pair list (PairList): P::kPairList when it declares one, else 0.
+template <class P, class = void>
+struct ListOf {
+    static constexpr int value = 0;
+};
+template <class P>
+struct ListOf<P, decltype((void)P::kPairList)> {
+    static constexpr int value = P::kPairList;
+};
+
+// The walk of a pass that records no pair list.
+struct NoRec {};
+
+// One seer's pair-list recorder: box-test passes with agents other than itself, and the
+// candidates the model keeps (P::keep), appended in walk order up to the capacity (the
+// count keeps growing past it, which marks the list incomplete).  Each entry goes straight
+// to its word of its group of four (measured faster than staging the group in shared
+// memory and storing it whole); a partial last group's other words are never read.
+struct ListRec {
+    uint4 *idx;
+    uint32_t stride, cap, seer, n, other;
+};
+
+template <class P>
+TGPU_D void record_pair(ListRec &r, const float4 &a, const float4 &b, uint32_t j, const typename P::SeeCtx &c) {
+    r.other += j != r.seer ? 1u : 0u;
+    if (P::keep(a, b, c)) {
+        if (r.n < r.cap)
+            reinterpret_cast<uint32_t *>(r.idx)[((size_t)(r.n >> 2) * r.stride + r.seer) * 4u + (r.n & 3u)] = j;
+        ++r.n;
+    }
+}
+
 // Union walk over candidates [j0, j1) of `src`: batches of up to 32, a box-test phase
 // into per-lane hit masks (all lanes read the same candidate), then a see phase in which
-// every lane with hits runs the see function on its next hit.
+// every lane with hits runs the see function on its next hit (each lane's hits in the
+// order of its own walk).
 template <class P, class Acc>
 TGPU_D void union_batches(typename P::Seer &s, const float4 &sp, const float4 &r4, bool active, uint32_t j0,
                           uint32_t j1, uint32_t self, const float4 *src, const Acc &acc,
@@ -147,13 +181,14 @@ struct UnrollOf<P, decltype((void)P::kLaneUnroll)> {
 };
 
 // Per-lane walk over candidates [j0, j1): UnrollOf<P> candidates per iteration for
-// independent loads in flight.
-template <class P, class Acc>
+// independent loads in flight; a recording pass passes its recorder as `rec`.
+template <class P, class Acc, class Rec = NoRec>
 TGPU_D void lane_run(typename P::Seer &s, const float4 &sp, const float4 &r4, uint32_t j0, uint32_t j1, uint32_t self,
                      const float4 *src, const Acc &acc, const typename P::SeeCtx &sctx, uint32_t &pairs,
-                     uint32_t &tested) {
+                     uint32_t &tested, Rec *rec = nullptr) {
     constexpr bool kGlobal = Acc::kGlobal;
     constexpr int U = UnrollOf<P>::value;
+    constexpr bool kRec = std::is_same_v<Rec, ListRec>;
     if (j1 <= j0) return;
     tested += j1 - j0;
     uint32_t j = j0;
@@ -167,6 +202,7 @@ TGPU_D void lane_run(typename P::Seer &s, const float4 &sp, const float4 &r4, ui
         for (int u = 0; u < U; ++u)
             if (j + u != self && box_hit(sp, b[u], r4)) {
                 ++pairs;
+                if constexpr (kRec) record_pair<P>(*rec, sp, b[u], j + u, sctx);
                 P::see(s, sp, b[u], acc, j + u, sctx);
             }
     }
@@ -174,7 +210,34 @@ TGPU_D void lane_run(typename P::Seer &s, const float4 &sp, const float4 &r4, ui
         const float4 b0 = load_pos(src, j, kGlobal);
         if (j != self && box_hit(sp, b0, r4)) {
             ++pairs;
+            if constexpr (kRec) record_pair<P>(*rec, sp, b0, j, sctx);
             P::see(s, sp, b0, acc, j, sctx);
+        }
+    }
+}
+
+// Replay of a recorded pair list: the see function over the seer's n entries in their
+// recorded order, one group of four per load, two positions loaded ahead; words past the
+// n-th are never used; the seer itself is skipped when the pass skips self.
+template <class P, class Acc>
+TGPU_D void list_run(typename P::Seer &s, const float4 &sp, const PairList &pl, uint32_t i, uint32_t n, uint32_t self,
+                     const float4 *pos, const Acc &acc, const typename P::SeeCtx &sctx) {
+    const uint4 *e = pl.idx + i;
+    const size_t stride = pl.stride;
+    for (uint32_t t = 0; t < n; t += 4) {
+        const uint4 g = __ldg(e + (size_t)(t >> 2) * stride);
+        const uint32_t m = n - t;  // entries of this group: min(m, 4)
+        {
+            const float4 b0 = __ldg(pos + g.x);
+            const float4 b1 = m > 1u ? __ldg(pos + g.y) : b0;
+            if (g.x != self) P::see(s, sp, b0, acc, g.x, sctx);
+            if (m > 1u && g.y != self) P::see(s, sp, b1, acc, g.y, sctx);
+        }
+        if (m > 2u) {
+            const float4 b2 = __ldg(pos + g.z);
+            const float4 b3 = m > 3u ? __ldg(pos + g.w) : b2;
+            if (g.z != self) P::see(s, sp, b2, acc, g.z, sctx);
+            if (m > 3u && g.w != self) P::see(s, sp, b3, acc, g.w, sctx);
         }
     }
 }
@@ -595,6 +658,31 @@ __global__ void __launch_bounds__(kSeeThreads, kStage ? 1 : 8) see_rows_kernel(S
     const uint32_t self = (active && L.skip_self) ? i : 0xFFFFFFFFu;
     uint32_t pairs = 0;
     uint32_t tested = 0;
+    constexpr int kList = ListOf<P>::value;
+
+    // Replay of the previous pass's pair list (same positions, same table): a warp whose
+    // lanes all hold complete lists runs the see function over them in the recorded order,
+    // which is the order the row walk would visit them in; otherwise the warp walks.
+    bool replayed = false;
+    if constexpr (kList == 2 && !kBox) {
+        if (L.plist.mode == 2u) {
+            const float4 rr = L.plist.rec_radii[seg];
+            const auto &rctx =
+                *reinterpret_cast<const typename P::SeeCtx *>(L.plist.rec_ctx + (size_t)seg * L.ctx_stride);
+            // the recorded set covers this pass's pairs: the same box, and a keep test at
+            // least as wide as what this pass's see function acts on
+            const bool covers = rr.x == r4.x && rr.y == r4.y && rr.z == r4.z && P::replay_ok(sctx, rctx);
+            const uint2 c = active ? L.plist.count[i] : make_uint2(0u, 0u);
+            replayed = __all_sync(0xffffffffu, covers && c.x <= L.plist.cap);
+            if (replayed && L.telemetry && lane == 0) atomicAdd(L.telemetry + 5, 1ull);
+            if (replayed && active) {
+                list_run<P>(s, sp, L.plist, i, c.x, self, pos, acc, sctx);
+                // the walk's count: box-test passes with every other agent, and the seer
+                // itself unless the pass skips it
+                pairs += c.y + ((!L.skip_self && box_hit(sp, sp, r4)) ? 1u : 0u);
+            }
+        }
+    }
 
     // Optional staging (stage_cap > 0, point agents): the rows of the union of the CTA's
     // seer boxes are contiguous runs of agents, each copied into shared memory by one bulk
@@ -628,7 +716,9 @@ __global__ void __launch_bounds__(kSeeThreads, kStage ? 1 : 8) see_rows_kernel(S
         __syncthreads();
         const int X0 = hb[0], Y0 = hb[1], Z0 = hb[2];
         const int ny = hb[4] - Y0 + 1, nz = hb[5] - Z0 + 1;
-        const long long nrows = (hb[3] >= X0 && ny > 0 && nz > 0) ? (long long)ny * nz : 0;
+        // (never for a pass that records or replays a pair list)
+        const long long nrows =
+            (L.plist.mode == 0u && hb[3] >= X0 && ny > 0 && nz > 0) ? (long long)ny * nz : 0;
         if (nrows > 0 && nrows <= (long long)L.stage_cells) {
             // each union row's candidate range over the union's x cells
             for (uint32_t t = threadIdx.x; t < (uint32_t)nrows; t += kSeeThreads) {
@@ -708,12 +798,35 @@ __global__ void __launch_bounds__(kSeeThreads, kStage ? 1 : 8) see_rows_kernel(S
 
     const int wl0 = warp_min_i(lo[0]), wl1 = warp_min_i(lo[1]), wl2 = warp_min_i(lo[2]);
     const int wh0 = warp_max_i(hi[0]), wh1 = warp_max_i(hi[1]), wh2 = warp_max_i(hi[2]);
-    if (!staged && wl0 <= wh0) {
+    // a recording pass (launch-uniform) takes the per-lane walk, which records (every walk
+    // visits a lane's hits in the same order; recording along the union walk measured slower)
+    const bool recording = kList == 1 && !kBox && L.plist.mode == 1u;
+    if (!staged && !replayed && wl0 <= wh0) {
         const int lane_vol = active ? (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) * (hi[0] - lo[0] + 1) : 0;
         const long long union_vol = (long long)(wh0 - wl0 + 1) * (wh1 - wl1 + 1) * (wh2 - wl2 + 1);
-        const bool union_mode = !kBox && union_vol <= (long long)L.union_factor * warp_max_i(lane_vol);
+        const bool union_mode =
+            !kBox && !recording && union_vol <= (long long)L.union_factor * warp_max_i(lane_vol);
         if (L.telemetry && lane == 0) atomicAdd(L.telemetry + (union_mode ? 3 : 4), 1ull);
-        if (union_mode) {
+        bool walked = false;
+        if constexpr (kList == 1 && !kBox) {
+            if (recording) {
+                // the per-lane walk with the recorder (a block of its own: folded into the
+                // plain walks it costs the non-recording kernels registers)
+                if (active) {
+                    ListRec rec{L.plist.idx, L.plist.stride, L.plist.cap, i, 0u, 0u};
+                    for (int z = lo[2]; z <= hi[2]; ++z)
+                        for (int y = lo[1]; y <= hi[1]; ++y) {
+                            const uint2 jr =
+                                row_range(words, hdr, (uint32_t)z * dy0 + (uint32_t)y, dx0, lo[0], hi[0]);
+                            lane_run<P>(s, sp, r4, jr.x, jr.y, self, pos, acc, sctx, pairs, tested, &rec);
+                        }
+                    L.plist.count[i] = make_uint2(rec.n, rec.other);
+                }
+                walked = true;
+            }
+        }
+        if (walked) {
+        } else if (union_mode) {
             for (int z = wl2; z <= wh2; ++z)
                 for (int y = wl1; y <= wh1; ++y) {
                     const uint2 jr = row_range(words, hdr, (uint32_t)z * dy0 + (uint32_t)y, dx0, wl0, wh0);
@@ -739,6 +852,8 @@ __global__ void __launch_bounds__(kSeeThreads, kStage ? 1 : 8) see_rows_kernel(S
                         lane_run<P>(s, sp, r4, jr.x, jr.y, self, pos, acc, sctx, pairs, tested);
                 }
         }
+    } else if (recording && active) {
+        L.plist.count[i] = make_uint2(0u, 0u);  // no cell to walk: an empty, complete list
     }
     if (active) P::finish(s, sp, L.io, i, sctx, actx);
     if (L.pairs) {

@@ -42,6 +42,23 @@ struct PassIO {
     uint32_t *out_u32[kMaxU32];
 };
 
+// Pair list shared by two consecutive see passes over unchanged positions (row order):
+// the recording pass stores, per seer, the candidates that passed the box test and the
+// model's keep test, in walk order; the replaying pass runs its see function over them
+// instead of walking the rows again.  Entries come in groups of four: entries 4g..4g+3 of
+// seer i are the 16 bytes idx[g * stride + i], so a lane stores one group per four
+// entries and the lanes of a warp read their g-th groups from 512 consecutive bytes.
+struct PairList {
+    uint4 *idx;
+    uint2 *count;             // per seer {entries (may exceed cap: overflow), box-test passes
+                              // with agents other than itself}
+    uint32_t stride;          // agents of the batch
+    uint32_t cap;             // entries per seer (a multiple of 4)
+    uint32_t mode;            // 0: none, 1: record, 2: replay
+    const float4 *rec_radii;  // replay: the recording pass's radii, per segment
+    const char *rec_ctx;      // replay: the recording pass's see contexts (stride ctx_stride)
+};
+
 struct SeeLaunch {
     const SegmentSpec *specs;
     const BoxAcc *box;
@@ -68,7 +85,8 @@ struct SeeLaunch {
     // telemetry (the reference's TAY_TELEMETRY counters, tay/space.c:50-60, plus the
     // kernel's own paths): [0] candidates box-tested (broad phase), [1] staged CTAs,
     // [2] CTAs that read the halo from global memory, [3] warps that walked the union
-    // box, [4] warps whose lanes walked their own boxes
+    // box, [4] warps whose lanes walked their own boxes, [5] warps that replayed a pair
+    // list
     unsigned long long *telemetry;
     PassIO io;
     // write-through (the last pass of a run): per segment the device address of the
@@ -76,6 +94,7 @@ struct SeeLaunch {
     // model's unpack program
     uint32_t *const *wt;
     uint32_t wt_program;
+    PairList plist;
 };
 
 struct ActLaunch {

@@ -1,0 +1,97 @@
+"""GPU: pair lists shared by SPH's density and force passes.  The density pass records each
+particle's neighbours inside the support in walk order; the force pass replays them
+instead of walking the rows again.  Every result must equal the walk's bit for bit, and so
+must the pair counts, whether every warp replays, some lists overflow their capacity (those
+warps walk), or the force pass's box differs from the density pass's (no warp replays)."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from tay_gb300 import api
+from tay_gb300 import models as M
+from tay_gb300 import workloads as W
+
+from parity import normwise, oracle_run
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(setup, recs, steps, **tuning):
+    api.set_tuning(**tuning)
+    try:
+        b = api.Batch([(setup, recs)])
+        try:
+            b.push()
+            pairs = [b.run(1)[1] for _ in range(steps)]
+            return b.fetch(0), pairs, b.telemetry()
+        finally:
+            b.close()
+    finally:
+        api.set_tuning()
+
+
+def _dam(nx, ny, nz):
+    sph = W.sph_dam(nx, ny, nz)
+    return M.records(M.SPH_RECORD, sph.points.p, sph.points.v)
+
+
+@pytest.mark.parametrize("cap", [320, 200, 16])
+def test_replay_equals_walk(gpu, cap):
+    """A 32 x 40 x 16 dam break, 5 steps.  Bulk particles have 251 neighbours inside the
+    support (2h = 4 lattice spacings), those at walls and corners fewer: at capacity 320
+    every warp replays, at 200 only the warps of the thinnest regions, at 16 none."""
+    recs = _dam(32, 40, 16)
+    setup = M.sph_setup(mb=256)
+    walk, p_walk, t_walk = _run(setup, recs, 5, pair_list_cap=0)
+    lists, p_lists, t_lists = _run(setup, recs, 5, pair_list_cap=cap)
+    assert p_walk == p_lists
+    assert walk.tobytes() == lists.tobytes()
+    assert t_walk["replay_warps"] == 0
+    warps = (recs.shape[0] + 31) // 32
+    if cap == 320:
+        assert t_lists["replay_warps"] == warps  # the last step's force pass, every warp
+        assert t_lists["candidates"] < t_walk["candidates"]
+    if cap == 16:
+        assert t_lists["replay_warps"] == 0
+
+
+def test_wider_force_box_walks(gpu):
+    """A force pass whose box is 1% wider than the density pass's gets no replay (the
+    recorded set was found with the smaller box); its see function acts only inside the
+    support, so the results still equal the walk's."""
+    recs = _dam(32, 40, 16)
+    setup = M.sph_setup(mb=256)
+    passes = [dataclasses.replace(p, radius=p.radius * 1.01) if p.name == "sph_force" else p for p in setup.passes]
+    wide = dataclasses.replace(setup, passes=passes)
+    walk, p_walk, _ = _run(wide, recs, 3, pair_list_cap=0)
+    lists, p_lists, t_lists = _run(wide, recs, 3)
+    assert t_lists["replay_warps"] == 0
+    assert p_walk == p_lists
+    assert walk.tobytes() == lists.tobytes()
+
+
+def test_full_size_replay_bit_identical(gpu):
+    """The 524,288-particle dam break (the SPH benchmark workload) at the default tuning,
+    3 steps: replayed force passes equal the walk bit for bit."""
+    recs = _dam(64, 128, 64)
+    setup = M.sph_setup(mb=512)
+    walk, p_walk, _ = _run(setup, recs, 3, pair_list_cap=0)
+    lists, p_lists, t_lists = _run(setup, recs, 3)
+    assert t_lists["replay_warps"] > 0
+    assert p_walk == p_lists
+    assert walk.tobytes() == lists.tobytes()
+
+
+def test_replay_matches_oracle(gpu, port):
+    """Against the oracle (CpuZGrid restatement), 5 steps of a 16 x 24 x 16 dam with pair
+    lists on: positions within the one-step tolerance, velocities within the many-step one."""
+    recs = _dam(16, 24, 16)
+    setup = M.sph_setup()
+    g, _, t = _run(setup, recs, 5)
+    g = M.by_id(g)  # fetched in cell order
+    assert t["replay_warps"] > 0
+    o = oracle_run(port, O.MODEL_SPH, setup, recs, 5)
+    assert normwise(g["p"][:, :3], o["p"][:, :3]) < 1e-5
+    assert normwise(g["v"][:, :3], o["v"][:, :3]) < 1e-3

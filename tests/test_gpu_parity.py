@@ -191,6 +191,39 @@ def test_staged_rows_bit_identical_full_size(gpu, tuning):
     assert t1["staged_ctas"] > 0
 
 
+@pytest.mark.parametrize("model", ["boids", "sph"])
+def test_row_walks_bit_identical(gpu, model):
+    """In row order the per-lane walk, the warp-union walk (union_factor), the hit-mask walk and
+    the staged walk visit each seer's neighbours in the same order, and every inlined copy of
+    the see body rounds the same way: records and pair counts are bit-identical (pair lists
+    off, so the SPH force pass walks too)."""
+    if model == "boids":
+        ps = W.boids_points(60000, seed=9, clusters=8, side=400.0)
+        recs = M.records(M.BOIDS_RECORD, ps.p, ps.v)
+        setup = M.boids_setup(r=10.0, part=10.0, mb=64)
+    else:
+        sph = W.sph_dam(32, 40, 16)
+        recs = M.records(M.SPH_RECORD, sph.points.p, sph.points.v)
+        setup = M.sph_setup(mb=256)
+    out = []
+    for tuning in ({"union_factor": 1}, {"union_factor": 64}, {"hit_masks": 1}, {"stage": 1}):
+        api.set_tuning(cell_order=1, pair_list_cap=0, **tuning)
+        try:
+            b = api.Batch([(setup, recs)])
+            try:
+                b.push()
+                pairs = [b.run(1)[1] for _ in range(4)]
+                out.append((b.fetch(0).tobytes(), pairs, b.telemetry()))
+            finally:
+                b.close()
+        finally:
+            api.set_tuning()
+    assert out[1][2]["union_warps"] > 0
+    for rec, pairs, _ in out[1:]:
+        assert pairs == out[0][1]
+        assert rec == out[0][0]
+
+
 @pytest.mark.parametrize("tuning", [
     {"cell_order": 1}, {"cell_order": 1, "x_cell_factor": 0.25}, {"cell_order": 1, "cell_multiple": 0.5},
     {"cell_order": 1, "union_factor": 4}, {"cell_order": 1, "stage": 1, "x_cell_factor": 0.25},
