@@ -596,7 +596,7 @@ def run_gb300(args, rank, world, D):
             line["sph"] = sph_leg(min(args.steps, 20), not args.no_autotune)
         if args.adjoint:
             tune = not args.no_autotune
-            line["adjoint"] = adjoint_leg(keep=4, tune=tune)
+            line["adjoint"] = adjoint_leg(keep=6, tune=tune)
             line["adjoint_keep1"] = adjoint_leg(keep=1, tune=tune)
             line["adjoint_record_all"] = adjoint_leg(every=0, tune=tune)
         if args.features:

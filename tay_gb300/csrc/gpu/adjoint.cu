@@ -196,14 +196,18 @@ void recorded_step(TgpuAdjoint *a, Record *r) {
         ++g.nu32;
     }
     launch_gather(b->total, perm, g, st);
-    // density + pressure
+    // density + pressure (recording the batch's pair list, when it keeps one)
     const KernelRun &rd = b->runs[0];
-    rd.k->launch_see(see_launch(b, rd, make_io(b, rd.k, true, 0)), 0, st);
-    // force + integrate, acceleration stored
+    SeeLaunch SD = see_launch(b, rd, make_io(b, rd.k, true, 0));
+    attach_pair_list(b, rd, SD);
+    rd.k->launch_see(SD, 0, st);
+    // force + integrate, acceleration stored (replaying the list)
     const KernelRun &rf = b->runs[1];
     PassIO io = make_io(b, rf.k, true, 0);
     const float4 *pos_in = io.in_f4[SPH_POS], *vel_in = io.in_f4[SPH_VEL];
-    a->K->force_record(see_launch(b, rf, io), 0, st);
+    SeeLaunch SF = see_launch(b, rf, io);
+    attach_pair_list(b, rf, SF);
+    a->K->force_record(SF, 0, st);
     for (int c = 0; c < b->m->nf4; ++c)
         if (b->m->role_f4[c] == kState && (rf.k->writes_f4 >> c & 1u) && (rf.k->seen_f4 >> c & 1u)) b->cur_f4[c] ^= 1;
     if (r) {
@@ -260,9 +264,16 @@ void backward_step(TgpuAdjoint *a, const Record &r) {
     fa.in_f4[A_VBAR] = fa.out_f4[A_VBAR] = a->vbar_s;
     fa.in_f4[A_RHOBAR] = fa.out_f4[A_RHOBAR] = a->rhobar;
     fa.in_f4[A_THETA] = fa.out_f4[A_THETA] = a->theta;
-    a->K->force_adj(see_launch(b, rf, fa), 0, st);
+    // the force adjoint records the step's pairs for the density adjoint when the batch
+    // keeps pair lists for its forward passes (the same cell order and walk conditions)
+    SeeLaunch F = see_launch(b, rf, fa);
     SeeLaunch D = see_launch(b, rd, fa);
     D.skip_self = 1;  // the self pair contributes nothing to the density adjoint
+    if (b->plist_idx && rf.skip_self) {
+        F.plist = PairList{b->plist_idx, b->plist_count, b->total, b->plist_cap, 1u, nullptr, nullptr};
+        D.plist = PairList{b->plist_idx, b->plist_count, b->total, b->plist_cap, 2u, rf.d_radii, rf.d_see_ctx};
+    }
+    a->K->force_adj(F, 0, st);
     a->K->density_adj(D, 0, st);
 
     PassIO sa = io;

@@ -304,6 +304,11 @@ struct ForceAdj {
     using ActCtx = Ctx;
     using Seer = ForceAdjSeer;
     static constexpr int kSeenF4 = 4;
+    // records the step's pairs inside the support for the density adjoint that follows
+    static constexpr int kPairList = 1;
+    TGPU_D static bool keep(const float4 &a, const float4 &b, const Ctx &c) {
+        return dist2(a.x - b.x, a.y - b.y, a.z - b.z) < c.support2;
+    }
     TGPU_D static int seen_stream(int k) { return k == 0 ? A_POS : (k == 1 ? A_VEL : (k == 2 ? A_RP : A_ABAR)); }
     TGPU_D static void load(Seer &s, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {
         s.v = io.in_f4[A_VEL][i];
@@ -392,6 +397,9 @@ struct DensityAdj {
     using ActCtx = Ctx;
     using Seer = DensityAdjSeer;
     static constexpr int kSeenF4 = 2;
+    // replays the force adjoint's list (same pairs: r2 < support2, r2 > 0)
+    static constexpr int kPairList = 2;
+    TGPU_D static bool replay_ok(const Ctx &mine, const Ctx &rec) { return mine.support2 <= rec.support2; }
     TGPU_D static int seen_stream(int k) { return k == 0 ? A_POS : A_RHOBAR; }
     TGPU_D static void load(Seer &s, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {
         s.rhob = io.in_f4[A_RHOBAR][i].x;
@@ -404,9 +412,9 @@ struct DensityAdj {
         if (!(r2 < c.support2 && r2 > 0.0f)) return;
         const float rinv = rsqrtf(r2);
         const float g = (s.rhob + acc.f4(1, j).x) * c.m * kernel_dw(r2 * rinv * c.inv_h, c.sigma, c.inv_h) * rinv;
-        s.xb[0] += g * dx;
-        s.xb[1] += g * dy;
-        s.xb[2] += g * dz;
+        s.xb[0] = __fmaf_rn(g, dx, s.xb[0]);
+        s.xb[1] = __fmaf_rn(g, dy, s.xb[1]);
+        s.xb[2] = __fmaf_rn(g, dz, s.xb[2]);
     }
     TGPU_D static void finish(Seer &s, const float4 &, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {
         const float4 xb = io.in_f4[A_XBAR][i];

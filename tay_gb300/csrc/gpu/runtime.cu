@@ -368,6 +368,19 @@ void unpack_range(TgpuBatch *b, uint32_t lo, uint32_t hi, cudaStream_t st) {
 
 }  // namespace
 
+void tgpu::attach_pair_list(const TgpuBatch *b, const KernelRun &r, SeeLaunch &S) {
+    if (!r.list_mode) return;
+    S.plist.idx = b->plist_idx;
+    S.plist.count = b->plist_count;
+    S.plist.stride = b->total;
+    S.plist.cap = b->plist_cap;
+    S.plist.mode = r.list_mode;
+    if (r.list_mode == 2u) {
+        S.plist.rec_radii = b->runs[r.list_src].d_radii;
+        S.plist.rec_ctx = b->runs[r.list_src].d_see_ctx;
+    }
+}
+
 void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E, bool write_through) {
     if (b->total == 0 || b->tiles == 0) return;
     cudaStream_t st = b->st;
@@ -439,17 +452,7 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E, bool write_through) {
             S.pairs = b->d_pairs;
             S.telemetry = b->d_telemetry;
             S.io = io;
-            if (r.list_mode) {
-                S.plist.idx = b->plist_idx;
-                S.plist.count = b->plist_count;
-                S.plist.stride = b->total;
-                S.plist.cap = b->plist_cap;
-                S.plist.mode = r.list_mode;
-                if (r.list_mode == 2u) {
-                    S.plist.rec_radii = b->runs[r.list_src].d_radii;
-                    S.plist.rec_ctx = b->runs[r.list_src].d_see_ctx;
-                }
-            }
+            attach_pair_list(b, r, S);
             // Write-through on the final pass over every segment: each CTA stores its seers'
             // finished records to the host as it ends, so the host link overlaps the pass.
             if (write_through && last && r.seer_seg < 0) {

@@ -110,6 +110,8 @@ namespace tgpu {
 // Runtime functions the adjoint module reuses.
 int prepare_specs(TgpuBatch *b);
 void enqueue_step(TgpuBatch *b, const StepEvents *E = nullptr, bool write_through = false);
+// The batch's pair list on a see launch of run r, when r records or replays one.
+void attach_pair_list(const TgpuBatch *b, const KernelRun &r, SeeLaunch &S);
 PassIO make_io(TgpuBatch *b, const KernelDesc *k, bool fused_see, uint32_t offset);
 SortLaunch sort_launch(TgpuBatch *b);
 int fail(int code, const char *fmt, ...);

@@ -146,6 +146,29 @@ def test_adjoint_row_order(gpu_grads):
     assert normwise(dv0, gpu_grads["dv0"]) < TOL
 
 
+def test_adjoint_pair_lists(gpu_grads):
+    """The recorded forward and the backward's recomputed segments replay the density pass's
+    pair lists in the force pass, and each backward step's density adjoint replays the force
+    adjoint's list.  With the lists off the rollout is the same bits; the gradients agree to
+    float rounding (the force adjoint records on the per-lane walk, which may round its
+    sums differently from the warp-union walk it takes without lists)."""
+    from tay_gb300 import api
+    out = []
+    for cap in (0, 320):
+        try:
+            api.set_tuning(pair_list_cap=cap)
+            roll = SphRollout(_instances(), STEPS, checkpoint_every=10, keep_segments=2)
+            x, _ = roll.forward()
+            grads = roll.backward(_dl_dx(x, gpu_grads["target"], roll))
+            roll.close()
+        finally:
+            api.set_tuning()
+        out.append((x, grads))
+    assert np.array_equal(out[0][0], out[1][0])
+    for a, b in zip(out[0][1], out[1][1]):
+        assert normwise(a, b) < 1e-6
+
+
 def test_fit_viscosity_and_sound_speed_to_a_target_rollout(gpu):
     """The adjoint used as intended: two instances starting at (alpha, c0) = (0.05, 20) and
     (0.12, 18) fitted with Adam to a target rollout made with (0.08, 22), 100 steps."""
