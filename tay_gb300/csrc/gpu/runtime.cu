@@ -824,6 +824,8 @@ int setup_pair_lists(TgpuBatch *b) {
         any = true;
     }
     if (!any) return TGPU_OK;
+    if ((uint64_t)cap * b->total > (1ull << 38))  // 1 TB of entries: a capacity no device holds
+        return fail(TGPU_ERR_ARG, "pair list of %u entries per agent for %u agents is too large", cap, b->total);
     b->plist_cap = cap;
     CKR(cudaMalloc(&b->plist_idx, (size_t)(cap / 4u) * b->total * sizeof(uint4)));
     CKR(cudaMalloc(&b->plist_count, (size_t)b->total * sizeof(uint2)));

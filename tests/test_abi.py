@@ -46,3 +46,19 @@ def test_device_models_are_registered(built):
                         ("sph_force", b"sph"), ("sph_integrate", b"sph")]:
         assert L.tgpu_model_of(name.encode()) == model
     assert L.tgpu_model_of(b"no_such_function") is None
+
+
+def test_tuning_struct_round_trips(built):
+    """TgpuTuning crosses the ABI field by field (the Python mirror has the C layout): every
+    field set from Python reads back unchanged, and no arguments restore the defaults."""
+    try:
+        api.set_tuning(stage=1, stage_cap=640, stage_cells=48, cell_multiple=0.5, union_factor=4, use_graphs=0,
+                       cell_order=0, hit_masks=1, x_cell_factor=0.25, pair_list_cap=96)
+        t = api.get_tuning()
+        assert t == {"stage": 1, "stage_cap": 640, "stage_cells": 48, "cell_multiple": 0.5, "union_factor": 4,
+                     "use_graphs": 0, "cell_order": 0, "hit_masks": 1, "x_cell_factor": 0.25, "pair_list_cap": 96}
+        api.set_tuning()
+        d = api.get_tuning()
+        assert d["cell_order"] == 1 and d["x_cell_factor"] == 0.5 and d["pair_list_cap"] == 320
+    finally:
+        api.set_tuning()
