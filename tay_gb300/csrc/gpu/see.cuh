@@ -16,7 +16,11 @@
 //   * tunings: a warp walks the union of its lanes' boxes with hit masks (union_factor,
 //     hit_masks), or the CTA first copies its union rows (row order, TMA bulk copies) or
 //     cells (Morton) into shared memory (stage); and a write-through instance stores the
-//     finished records to page-locked host memory from the epilogue.
+//     finished records to page-locked host memory from the epilogue;
+//   * pair lists: a pass can record each seer's kept candidates for the next pass over the
+//     same positions, which runs its see function over them instead of walking the rows
+//     (SPH density -> force); every walk and the replay visit a seer's neighbours in the
+//     same order, so they give the same bits.
 // Act pass (replaces tay/space.c:250-263): one thread per agent.
 #pragma once
 
