@@ -2,9 +2,8 @@
 
 Picks, by measurement on the GPU, the grid cell-size multiple (cell edge relative to the
 configured minimum part size), the cell order (3-D Morton cells or x-rows) with the x cell
-factor of row order, the warp walk (union walk threshold), whether see CTAs stage their
-halos in shared memory and, for the winner, whether consecutive see passes share pair lists
-(pair_list_cap on or 0).  Each candidate runs a few steps on a throwaway batch
+factor of row order, the warp walk (union walk threshold) and whether see CTAs stage their
+halos in shared memory.  Each candidate runs a few steps on a throwaway batch
 built from the same groups (the caller's state is not advanced); the fastest candidate is
 set as the library's tuning and cached per shape class (model, pass sequence, agent-count
 bucket, segment-count bucket, radius / part-size ratio) in a JSON file, so later runs of the
@@ -102,16 +101,8 @@ def autotune(groups, candidates=None, steps: int = 3, use_cache: bool = True, ev
     trials = []
     for cand in candidates or DEFAULT_CANDIDATES:
         trials.append((sum(measure(g, dict(base, **cand), steps) for g in states) / len(states), cand))
-    best_ms, best_cand = min(trials, key=lambda t: t[0])
-    best = dict(base, **best_cand)
-    if best.get("pair_list_cap", 0) and best.get("cell_order") == 1 and not best.get("stage") \
-            and not best.get("hit_masks"):
-        # pair lists exist only for such walks; keep them only where recording pays
-        off = dict(best, pair_list_cap=0)
-        off_ms = sum(measure(g, off, steps) for g in states) / len(states)
-        trials.append((off_ms, dict(best_cand, pair_list_cap=0)))
-        if off_ms < best_ms:
-            best_ms, best = off_ms, off
+    best_ms, best = min(trials, key=lambda t: t[0])
+    best = dict(base, **best)
     api.set_tuning(**best)
     entry = {"tuning": best, "ms_per_step": best_ms,
              "trials": [{"tuning": c, "ms_per_step": m} for m, c in trials]}
