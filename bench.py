@@ -273,12 +273,14 @@ def sph_leg(steps, tune=True):
         ms, p = B.run(1)
         dev_ms += ms
         pairs += p
+    tel = B.telemetry()  # the last step: warps that walked, and warps that replayed a pair list
     B.close()
     tuning = api.get_tuning()
     api.set_tuning()
     return {"particles": int(recs.shape[0]), "steps": steps, "ms_per_step": dev_ms / steps,
             "pair_interactions_per_s": pairs / (dev_ms / 1000.0), "pairs_per_step": pairs / steps,
-            "tuning": tuning}
+            "tuning": tuning,
+            "last_step_warps": {k: tel[k] for k in ("union_warps", "lane_warps", "replay_warps")}}
 
 
 def adjoint_leg(steps=200, every=20, instances=32, keep=1, tune=True):
