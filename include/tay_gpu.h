@@ -250,10 +250,13 @@ unsigned long long tgpu_batch_device_bytes(const TgpuBatch *batch);
  *     TGPU_ERR_ARG and a message from tgpu_noalloc_last_error();
  *   - the array is shared by every call and keeps the last call's contents (each call
  *     clears what must start at zero); calls whose work overlaps on the GPU race;
- *   - the first call on a device looks up the array's device address with that device
- *     current; make that first call before any stream capture;
+ *   - every call looks up the array's device address in the current device's context
+ *     (a host-side query), so it stays valid after that context is recreated;
  *   - work is enqueued on `stream` (a cudaStream_t, NULL for the default stream) and the
- *     call returns once it has finished. */
+ *     call returns once it has finished: it synchronises and reads back a status word,
+ *     so it may not be called while any stream is capturing;
+ *   - a CUDA error pending from earlier work is left in place for its owner and the call
+ *     returns TGPU_ERR_CUDA without starting. */
 int tgpu_see_noalloc(const float *positions, unsigned n, const float *radii, const float *min_part_sizes,
                      float *out, void *stream);
 unsigned tgpu_noalloc_max_agents(void);

@@ -17,10 +17,14 @@
 //     two calls whose work overlaps on the GPU (different streams, or different host
 //     threads) overwrite each other's data and race;
 //   * every GPU that loads the library holds the array until the process exits;
-//   * the first call on a device looks up the array's device address (once per device,
-//     with that device current); make that first call before any stream capture.
+//   * every call looks up the array's device address in the current device's context
+//     (cudaGetSymbolAddress, a host-side query), so a context that was destroyed and
+//     created again (cudaDeviceReset) never leaves a stale address behind;
+//   * the call waits for its own work (it synchronises the stream and reads back the
+//     device error word), so it may not be called while any stream is capturing;
+//   * a CUDA error left pending by earlier, unrelated work is not taken over: the call
+//     refuses to start and leaves that error in place for its owner.
 #include <cstdio>
-#include <mutex>
 
 #include "model.cuh"
 #include "tay_gpu.h"
@@ -92,9 +96,6 @@ __global__ void noalloc_unpermute_kernel(const uint32_t *perm, const float4 *acc
     if (i < n) out[perm[i]] = acc[i];
 }
 
-std::mutex g_noalloc_lock;
-unsigned char *g_noalloc_ptr[64] = {};
-
 thread_local char g_noalloc_err[256];
 
 int noalloc_fail(int code, const char *msg) {
@@ -123,25 +124,25 @@ extern "C" int tgpu_see_noalloc(const float *positions, unsigned n, const float 
         return noalloc_fail(TGPU_ERR_ARG, "tgpu_see_noalloc: null pointer argument");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
 
-    // once per device, with that device current: the array's device address
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= 64) return noalloc_fail(TGPU_ERR_CUDA, "tgpu_see_noalloc: no current device");
-    unsigned char *scratch = nullptr;
-    {
-        std::lock_guard<std::mutex> guard(g_noalloc_lock);
-        if (!g_noalloc_ptr[dev]) {
-            void *p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess) {
-                char msg[200];
-                snprintf(msg, sizeof(msg), "tgpu_see_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
-                return noalloc_fail(TGPU_ERR_CUDA, msg);
-            }
-            g_noalloc_ptr[dev] = static_cast<unsigned char *>(p);
-        }
-        scratch = g_noalloc_ptr[dev];
+    // an error pending from earlier work would be indistinguishable from this call's own
+    // launch errors below: leave it to its owner and do nothing
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess) {
+        char msg[200];
+        snprintf(msg, sizeof(msg), "tgpu_see_noalloc: an earlier CUDA error is pending (%s); not started",
+                 cudaGetErrorString(e));
+        return noalloc_fail(TGPU_ERR_CUDA, msg);
     }
+    // the array's device address in the current context, looked up on every call
+    void *scratch_addr = nullptr;
+    e = cudaGetSymbolAddress(&scratch_addr, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+        cudaGetLastError();  // the failed lookup's own error
+        char msg[200];
+        snprintf(msg, sizeof(msg), "tgpu_see_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+        return noalloc_fail(TGPU_ERR_CUDA, msg);
+    }
+    unsigned char *scratch = static_cast<unsigned char *>(scratch_addr);
 
     SegmentSpec spec{};
     spec.begin = 0;
@@ -215,8 +216,10 @@ extern "C" int tgpu_see_noalloc(const float *positions, unsigned n, const float 
     k.launch_see(S, 0, st);
     noalloc_unpermute_kernel<<<(n + 255) / 256, 256, 0, st>>>(perm, acc, reinterpret_cast<float4 *>(out), n);
     launch_cell_table(L, skeys, 0, st);
-    e = cudaStreamSynchronize(st);
-    if (e == cudaSuccess) e = cudaGetLastError();
+    // launch errors first (only this call's: nothing was pending at entry), then the
+    // errors of the work itself
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         char msg[200];
         snprintf(msg, sizeof(msg), "tgpu_see_noalloc: %s", cudaGetErrorString(e));
