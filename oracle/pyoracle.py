@@ -226,10 +226,12 @@ def reference():
     return _ref
 
 
-def sph_adjoint_f64(x0, v0, ctx64, steps, dl_dx=None, dl_dv=None):
-    """FP64 CPU adjoint of an SPH rollout (oracle/sph_adjoint.c), all pairs.
+def sph_adjoint_f64(x0, v0, ctx64, steps, dl_dx=None, dl_dv=None, backward=True):
+    """FP64 CPU adjoint of an SPH rollout (oracle/sph_adjoint.c): every pair within the
+    support, from per-step neighbour lists, summed in ascending index order.
     x0, v0, dl_dx, dl_dv: [n, 3]; ctx64: sph_context(np.float64, ...).  Returns
-    dict(dx0, dv0, dalpha, dc0, x_final, v_final)."""
+    dict(dx0, dv0, dalpha, dc0, x_final, v_final); with backward=False only the forward
+    rollout runs (x_final, v_final; the gradients are zero)."""
     lib = port().lib
     fn = lib.oracle_sph_adjoint_f64
     fn.restype = ctypes.c_int
@@ -243,8 +245,8 @@ def sph_adjoint_f64(x0, v0, ctx64, steps, dl_dx=None, dl_dv=None):
     dx0, dv0 = np.zeros((n, 3)), np.zeros((n, 3))
     xf, vf = np.zeros((n, 3)), np.zeros((n, 3))
     th = np.zeros(2)
-    r = fn(n, x0.ctypes.data, v0.ctypes.data, c.ctypes.data, steps, gx.ctypes.data, gv.ctypes.data, dx0.ctypes.data,
-           dv0.ctypes.data, th.ctypes.data, xf.ctypes.data, vf.ctypes.data)
+    r = fn(n, x0.ctypes.data, v0.ctypes.data, c.ctypes.data, steps, gx.ctypes.data, gv.ctypes.data,
+           dx0.ctypes.data if backward else None, dv0.ctypes.data, th.ctypes.data, xf.ctypes.data, vf.ctypes.data)
     if r != steps:
         raise RuntimeError("oracle_sph_adjoint_f64 failed")
     return {"dx0": dx0, "dv0": dv0, "dalpha": th[0], "dc0": th[1], "x_final": xf, "v_final": vf}

@@ -95,3 +95,36 @@ def test_replay_matches_oracle(gpu, port):
     o = oracle_run(port, O.MODEL_SPH, setup, recs, 5)
     assert normwise(g["p"][:, :3], o["p"][:, :3]) < 1e-5
     assert normwise(g["v"][:, :3], o["v"][:, :3]) < 1e-3
+
+
+def test_full_size_sph_against_oracle(gpu, port):
+    """The 524,288-particle dam break (64 x 128 x 64 lattice, the SPH benchmark workload),
+    pair lists on: one step of density, pressure and force with rho and a within 1e-5
+    normwise of the oracle; then 5 steps of all four passes, positions within 1e-5 and
+    velocities within 1e-3.  P = B ((rho / rho0)^7 - 1) turns a density error into a 7 times
+    larger one relative to max |P| (B, at the free surface), which puts P's normwise error
+    at the FP32 rounding floor itself: the FP32 oracle differs from the FP64 one by 9e-6
+    on this dam.  P is held to 1e-5 or twice that floor, whichever is larger (measured on
+    GB300: 1.0e-5)."""
+    recs = _dam(64, 128, 64)
+    tune = dict(cell_order=1, cell_multiple=0.25, x_cell_factor=0.5)
+    setup = M.sph_setup(passes=("sph_density", "sph_pressure", "sph_force"), mb=512)
+    g, _, t = _run(setup, recs, 1, **tune)
+    g = M.by_id(g)
+    assert t["replay_warps"] > 0
+    o = oracle_run(port, O.MODEL_SPH, setup, recs, 1, threads=0)
+    o64 = oracle_run(port, O.MODEL_SPH, setup, recs, 1, threads=0, real=np.float64)
+    for name, f in (("rho", "rho"), ("P", "P"), ("a", "a")):
+        gv, ov, wv = (x[f][:, :3] if f == "a" else x[f] for x in (g, o, o64))
+        e, floor = normwise(gv, ov), normwise(ov, wv)
+        print(f"full-size SPH one step {name}: GPU vs FP32 oracle {e:.2e}; FP32 oracle vs FP64 {floor:.2e}")
+        assert e < (max(1e-5, 2.0 * floor) if name == "P" else 1e-5), (name, e, floor)
+    setup = M.sph_setup(mb=512)
+    g, _, t = _run(setup, recs, 5, **tune)
+    g = M.by_id(g)
+    assert t["replay_warps"] > 0
+    o = oracle_run(port, O.MODEL_SPH, setup, recs, 5, threads=0)
+    ep, ev = normwise(g["p"][:, :3], o["p"][:, :3]), normwise(g["v"][:, :3], o["v"][:, :3])
+    print(f"full-size SPH 5 steps: p {ep:.2e} v {ev:.2e}")
+    assert ep < 1e-5
+    assert ev < 1e-3
