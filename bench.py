@@ -51,8 +51,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=35,
-                    help="steps of the CPU baseline sample (about 10 s on 16 Grace cores)")
+    ap.add_argument("--cpu-steps", type=int, default=100,
+                    help="largest CPU sample: the CPU baseline and the reference arm time min(steps, this) steps "
+                         "of the same workload from the same initial state (0.26 s per step on 16 Grace cores)")
+    ap.add_argument("--c1", type=int, default=1, help="1 = add the 100,000-agent test model leg and its CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batched-states", type=int, default=512, help="states of the batched leg (0 = skip)")
     ap.add_argument("--sph", type=int, default=1, help="1 = add the 524,288-particle SPH leg")
@@ -193,6 +195,11 @@ CONFIG = {"workload": "boids_1M_zgrid", "agents": N_BOIDS, "radius": RADIUS, "ce
           "passes": ["boids_see", "boids_act"], "seed": SEED}
 
 
+def bench_config(world):
+    """The workload description both arms print (the same keys and values)."""
+    return dict(CONFIG, l2="GPU arm: flushed between timed steps", parallelism=f"replicas{world}")
+
+
 def batched_workload(states):
     """The batched boids workload: `states` states, N log-uniform in [1000, 65536], box side
     (125 N)^(1/3), radius U[5, 20] (cell = radius), same boids rules."""
@@ -231,7 +238,7 @@ def batched_vs_plain(states, steps, tune=True):
     for s in singles:
         s.push()
         s.run(1)
-    plain_steps = max(1, min(steps, 3))
+    plain_steps = steps
     dev_p, pairs_p = 0.0, 0
     t0 = time.perf_counter()
     for _ in range(plain_steps):
@@ -244,7 +251,7 @@ def batched_vs_plain(states, steps, tune=True):
         s.close()
     tuning = api.get_tuning()
     api.set_tuning()
-    return {"tuning": tuning, "states": states, "agents": agents, "steps": steps,
+    return {"tuning": tuning, "states": states, "agents": agents, "steps": steps, "plain_steps": plain_steps,
             "batched_ms_per_step": wall_b * 1000.0, "batched_device_ms_per_step": dev_ms / steps,
             "batched_pairs_per_s": pairs / (wall_b * steps),
             "plain_ms_per_step": wall_p * 1000.0, "plain_device_ms_per_step": dev_p / plain_steps,
@@ -252,7 +259,7 @@ def batched_vs_plain(states, steps, tune=True):
             "speedup": wall_p / wall_b}
 
 
-def sph_leg(steps, tune=True):
+def sph_leg(steps, tune=True, cpu_steps=0):
     """The SPH dam break: 64x128x64 = 524,288 particles on a 0.01 lattice in a
     2.0 x 1.5 x 0.8 tank, h 0.02 (see radius 2h), four passes per step."""
     from tay_gb300 import api, autotune
@@ -277,10 +284,23 @@ def sph_leg(steps, tune=True):
     B.close()
     tuning = api.get_tuning()
     api.set_tuning()
-    return {"particles": int(recs.shape[0]), "steps": steps, "ms_per_step": dev_ms / steps,
-            "pair_interactions_per_s": pairs / (dev_ms / 1000.0), "pairs_per_step": pairs / steps,
-            "tuning": tuning,
-            "last_step_warps": {k: tel[k] for k in ("union_warps", "lane_warps", "replay_warps")}}
+    out = {"particles": int(recs.shape[0]), "steps": steps, "ms_per_step": dev_ms / steps,
+           "pair_interactions_per_s": pairs / (dev_ms / 1000.0), "pairs_per_step": pairs / steps,
+           "tuning": tuning,
+           "last_step_warps": {k: tel[k] for k in ("union_warps", "lane_warps", "replay_warps")}}
+    if cpu_steps:
+        from oracle import pyoracle as O
+
+        threads = os.cpu_count() or 1
+        ctx = setup.passes[0].ctx
+        r = O.port().run(O.MODEL_SPH, "z_grid", recs, ctx, ctx, setup.passes[0].radius, setup.part, cpu_steps, 15,
+                         threads=threads, mb=setup.mb)
+        secs = r.ms_per_step * cpu_steps / 1000.0
+        out["cpu_baseline"] = {"value": r.pairs / secs, "unit": "pair-interactions/s", "cores": threads,
+                               "kind": "port", "ms_per_step": r.ms_per_step,
+                               "sample": f"{cpu_steps} steps of the 524,288-particle dam (4 passes) on CpuZGrid "
+                                         f"(oracle restatement, {threads} threads)"}
+    return out
 
 
 def adjoint_leg(steps=200, every=20, instances=32, keep=1, tune=True):
@@ -328,6 +348,43 @@ def adjoint_leg(steps=200, every=20, instances=32, keep=1, tune=True):
             "forward_ms": fwd_ms, "recorded_forward_ms": rec_ms, "backward_ms": bwd_ms,
             "fwd_plus_bwd_over_fwd": (rec_ms + bwd_ms) / fwd_ms, "device_bytes": mem, "loss": loss,
             "dloss_dalpha_mean": float(dp[:, 0].mean()), "dloss_dc0_mean": float(dp[:, 1].mean())}
+
+
+def c1_leg(steps=100, cpu_steps=100):
+    """The first configuration: 100,000 test agents, positions U[0, 1000]^3, velocities
+    U[-1, 1]^3 (seed 1), see radius 50 with the test model's count and displacement sum,
+    act moving each agent and reflecting it at the walls, minimum part size 50, 100 steps.
+    GPU: device time through the C API; CPU: the oracle restatement of CpuGrid (the
+    configuration's structure) on all host threads, the same steps from the same state."""
+    from oracle import pyoracle as O
+    from tay_gb300 import api
+    from tay_gb300 import models as M
+    from tay_gb300 import workloads as W
+
+    ps = W.basic_points(100_000, seed=1)
+    recs = M.records(M.TEST_RECORD, ps.p, ps.v)
+    setup = M.test_setup(radius=50.0, part=50.0, mb=64)
+    st, g = M.make_state(setup, recs)
+    st.start()
+    st.run(3)
+    st.run(steps)
+    dev = st.L.tay_get_device_ms_for_last_run(st.ptr) / steps
+    pairs = st.pairs() / steps
+    st.end()
+    st.close()
+    out = {"agents": 100_000, "steps": steps, "ms_per_step": dev, "pairs_per_step": pairs,
+           "pair_interactions_per_s": pairs / (dev / 1000.0), "tuning": api.get_tuning()}
+    if cpu_steps:
+        threads = os.cpu_count() or 1
+        see, act = M.test_contexts(50.0)
+        r = O.port().run(O.MODEL_TEST, "grid", recs, see, act, 50.0, 50.0, cpu_steps, O.PASS_SEE0 | O.PASS_ACT0,
+                         threads=threads, mb=setup.mb)
+        secs = r.ms_per_step * cpu_steps / 1000.0
+        out["cpu_baseline"] = {"value": r.pairs / secs, "unit": "pair-interactions/s", "cores": threads,
+                               "kind": "port", "ms_per_step": r.ms_per_step,
+                               "sample": f"{cpu_steps} steps of the 100,000-agent workload on CpuGrid, part size 50 "
+                                         f"(oracle restatement, {threads} threads)"}
+    return out
 
 
 def features_leg(setup, recs, tuning, steps=20):
@@ -453,16 +510,27 @@ def cpu_baseline(setup, recs, steps):
             "ms_per_step": r.ms_per_step, "pairs_per_step": r.pairs / steps, "wall_s": round(wall, 2)}
 
 
+def cpu_sample_steps(args):
+    """Steps of the CPU sample, the same in the reference arm and in the GPU arm's CPU
+    baseline: the run's own step count, bounded by --cpu-steps."""
+    return max(1, min(args.steps, args.cpu_steps))
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
     setup, recs = workload()
-    for _ in range(min(args.warmup, 1)):
+    # warm-up: each oracle run starts from the initial records, so these only warm the
+    # host (threads, caches); the timed sample is the same as the GPU arm's CPU baseline
+    warm = min(args.warmup, 3)
+    for _ in range(warm):
         cpu_baseline(setup, recs, 1)
-    cb = cpu_baseline(setup, recs, max(1, args.steps if args.steps <= 10 else 10))
+    steps = cpu_sample_steps(args)
+    cb = cpu_baseline(setup, recs, steps)
     line = {"metric": "pair-interactions/s", "value": cb["value"], "unit": "pair-interactions/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": CONFIG,
+            "steps": steps, "warmup": warm, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded SplitMix64, 64 Gaussian clusters of boids)", "config": bench_config(world),
             "impl": "reference", "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": "pair-interactions/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
@@ -557,6 +625,13 @@ def run_gb300(args, rank, world, D):
     # act 2 x 36 B state + 40 B accumulators = 280 B
     step_bytes = N_BOIDS * (16 + 8 + 2 * 36 + (32 + 40) + (2 * 36 + 40))
     see_name = "see_rows_kernel<boids::SeeAct>" if api.get_tuning().get("cell_order") == 1 else "see_kernel<boids::SeeAct>"
+    # instruction-issue floor of the see kernel: every lane of every scheduler busy (152 SMs
+    # x 4 schedulers x 32 lanes per cycle at the sampled SM clock), 10 thread instructions
+    # per candidate box-tested (load, three subtractions, three compares, self test, loop)
+    # and 30 per pair that passed the box test (the see body with its distance test and
+    # accumulates); candidates and pairs from the device counters of the last step
+    sm_hz = 1e6 * (clk["sm_mhz"] or clk["sm_max_mhz"] or 2070.0)
+    floor_ms = 1000.0 * (10.0 * tel["candidates"] + 30.0 * tel["pairs"]) / (152 * 4 * 32 * sm_hz)
     traffic = None
     tp = os.path.join(ROOT, "profiles", "see_boids_traffic.json")
     if os.path.exists(tp):
@@ -570,7 +645,7 @@ def run_gb300(args, rank, world, D):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded SplitMix64, 64 Gaussian clusters of boids)",
-            "config": dict(CONFIG, l2="flushed between timed steps", parallelism=f"replicas{world}"),
+            "config": bench_config(world),
             "steps_per_s": args.steps / secs,
             "pairs_per_step": all_pairs / world / args.steps,
             "e2e": {"value": e2e_pairs / e2e_s, "unit": "pair-interactions/s",
@@ -581,6 +656,9 @@ def run_gb300(args, rank, world, D):
             "roofline": {"bound": "hbm", "kernel": see_name, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": see_bytes, "launch_ms": see_ms},
+            "issue_roofline": {"bound": "issue", "kernel": see_name, "floor_ms": floor_ms, "launch_ms": see_ms,
+                               "frac": floor_ms / see_ms, "instructions_per_candidate": 10,
+                               "instructions_per_pair": 30, "candidates": tel["candidates"], "pairs": tel["pairs"]},
             "step_roofline": {"achieved": step_bytes / (step_ms / 1000.0) / 1e9, "unit": "GB/s",
                               "frac": step_bytes / (step_ms / 1000.0) / 1e9 / peak,
                               "algorithmic_bytes_per_step": step_bytes, "profiled_step_ms": step_ms},
@@ -592,10 +670,13 @@ def run_gb300(args, rank, world, D):
             "autotune": None if tuned is None else {"trials": tuned["trials"], "ms_per_step": tuned["ms_per_step"]},
             "telemetry": tel,
         }
+        cpu = not args.no_cpu_baseline and world == 1
+        if args.c1:
+            line["c1"] = c1_leg(cpu_steps=100 if cpu else 0)
         if args.batched_states > 0:
             line["batched"] = batched_vs_plain(args.batched_states, min(args.steps, 20), not args.no_autotune)
         if args.sph:
-            line["sph"] = sph_leg(min(args.steps, 20), not args.no_autotune)
+            line["sph"] = sph_leg(min(args.steps, 20), not args.no_autotune, cpu_steps=2 if cpu else 0)
         if args.adjoint:
             tune = not args.no_autotune
             line["adjoint"] = adjoint_leg(keep=6, tune=tune)
@@ -603,8 +684,17 @@ def run_gb300(args, rank, world, D):
             line["adjoint_record_all"] = adjoint_leg(every=0, tune=tune)
         if args.features:
             line["features"] = features_leg(setup, recs, line["tuning"])
-        if not args.no_cpu_baseline and world == 1:
-            line["cpu_baseline"] = cpu_baseline(setup, recs, args.cpu_steps)
+        if cpu:
+            line["cpu_baseline"] = cpu_baseline(setup, recs, cpu_sample_steps(args))
+        # the benchmark spec's targets in one short object at the end of the line
+        tg = {"step_ms": round(line["ms_per_step"], 4), "see_launch_ms": round(see_ms, 4),
+              "see_issue_frac": round(floor_ms / see_ms, 3), "see_hbm_frac": round(achieved / peak, 4)}
+        if "batched" in line:
+            tg["batched_speedup"] = round(line["batched"]["speedup"], 2)
+        for k in ("adjoint", "adjoint_keep2", "adjoint_keep1"):
+            if k in line:
+                tg[k + "_fwd_bwd_over_fwd"] = round(line[k]["fwd_plus_bwd_over_fwd"], 3)
+        line["targets"] = tg
         print(json.dumps(line), flush=True)
 
 

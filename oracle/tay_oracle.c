@@ -313,8 +313,12 @@ static void o_z_grid_sort(OGroup *g) {
     g->sort_storage = t;
 }
 
-/* tay/cpu_grid.c:74-156 */
-static void o_grid_sort(OGroup *g) {
+/* tay/cpu_grid.c:74-156.  Returns 0, without touching the cells, when the grid has more
+ * cells than the structure's memory holds: the reference's shrink step rounds every axis
+ * up (tay/cpu_grid.c:100-108), which can leave cells_count above max_cells, and the
+ * reference then indexes past its cell array (it faults on the 1M-boid workload with 256 MB).
+ * Every other grid is the reference's, unchanged. */
+static int o_grid_sort(OGroup *g) {
     o_update_box(g);
     g->first_gcell = 0;
     unsigned long long cells_count = 1;
@@ -339,6 +343,11 @@ static void o_grid_sort(OGroup *g) {
             g->cell_counts[i] = (int)O_CEIL(g->cell_counts[i] / ratio);
             g->cell_size[i] = size / (REAL)g->cell_counts[i];
         }
+        unsigned long long shrunk = 1;
+        for (int i = 0; i < g->dims; ++i)
+            shrunk *= (unsigned long long)g->cell_counts[i];
+        if (shrunk > g->max_cells)
+            return 0;
     }
     for (unsigned a = 0; a < g->count; ++a) {
         int idx[3];
@@ -369,6 +378,7 @@ static void o_grid_sort(OGroup *g) {
     char *t = g->storage;
     g->storage = g->sort_storage;
     g->sort_storage = t;
+    return 1;
 }
 
 static void o_unsort(OGroup *g) {
@@ -616,11 +626,13 @@ static int o_group_finish(OGroup *g, int model, void *agents) {
     return ok;
 }
 
-static void o_sort(OGroup *g) {
+/* 0 when the group's structure cannot hold its grid (o_grid_sort). */
+static int o_sort(OGroup *g) {
     if (g->space == O_SPACE_Z_GRID)
         o_z_grid_sort(g);
     else if (g->space == O_SPACE_GRID)
-        o_grid_sort(g);
+        return o_grid_sort(g);
+    return 1;
 }
 
 static double o_seconds(const struct timespec *t0, const struct timespec *t1) {
@@ -690,8 +702,11 @@ int O_NAME(oracle_run)(int model, int space, int n, void *agents, const void *se
     memset(O_NAME(pairs_by_thread), 0, sizeof(O_NAME(pairs_by_thread)));
     struct timespec t0, t1;
     clock_gettime(CLOCK_MONOTONIC, &t0);
-    for (int step = 0; step < steps; ++step) {
-        o_sort(&g);
+    int sorted = 1;
+    for (int step = 0; step < steps && sorted; ++step) {
+        sorted = o_sort(&g);
+        if (!sorted)
+            break;
         for (int p = 0; p < passes_count; ++p) {
             OPassArg arg = {&g, &g, passes + p, passes[p].is_see && !passes[p].self_see};
             OTask task = {passes[p].is_see ? o_see_task : o_act_task, &arg};
@@ -702,7 +717,7 @@ int O_NAME(oracle_run)(int model, int space, int n, void *agents, const void *se
     clock_gettime(CLOCK_MONOTONIC, &t1);
     if (ms_per_step)
         *ms_per_step = steps ? o_seconds(&t0, &t1) / steps * 1000.0 : 0.0;
-    return o_group_finish(&g, model, agents) ? steps : 0;
+    return o_group_finish(&g, model, agents) && sorted ? steps : 0;
 }
 
 /* Runs `steps` steps of a state with several groups of one model (the test model's
@@ -767,9 +782,15 @@ int O_NAME(oracle_run_groups)(int model, int space, int ngroups, const int *coun
     memset(O_NAME(pairs_by_thread), 0, sizeof(O_NAME(pairs_by_thread)));
     struct timespec t0, t1;
     clock_gettime(CLOCK_MONOTONIC, &t0);
-    for (int step = 0; step < steps; ++step) {
+    int sorted = 1;
+    for (int step = 0; step < steps && sorted; ++step) {
         for (int k = 0; k < ngroups; ++k)
-            o_sort(g + k);
+            sorted &= o_sort(g + k);
+        if (!sorted) {
+            for (int k = 0; k < ngroups; ++k)
+                o_unsort(g + k);
+            break;
+        }
         for (int p = 0; p < npasses; ++p) {
             OGroup *seer = g + pass_seer[p];
             OGroup *seen = passes[p].is_see ? g + pass_seen[p] : seer;
@@ -783,7 +804,7 @@ int O_NAME(oracle_run_groups)(int model, int space, int ngroups, const int *coun
     clock_gettime(CLOCK_MONOTONIC, &t1);
     if (ms_per_step)
         *ms_per_step = steps ? o_seconds(&t0, &t1) / steps * 1000.0 : 0.0;
-    int ok = steps;
+    int ok = sorted ? steps : 0;
     for (int k = 0; k < ngroups; ++k)
         if (!o_group_finish(g + k, model, agents[k]))
             ok = 0;

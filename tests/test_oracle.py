@@ -165,3 +165,16 @@ def test_port_space_options_bit_exact_with_golden(port, name):
                  threads=3, dims=dims, box=box)
     port.set_space()
     assert same_records(model, r.records, GS[f"{name}__out"]), name
+
+
+def test_port_grid_overflow_is_an_error(port):
+    """The 1M-boid workload on CpuGrid with 256 MB: the reference's shrink step rounds each
+    axis up (tay/cpu_grid.c:100-108) and leaves more cells than its array holds, after which
+    the reference indexes past the array.  The restatement reports the run as failed
+    instead (the reference build itself is not run on this input); with 2048 MB the same
+    grid fits."""
+    ps = W.boids_points(1 << 20, seed=2)
+    recs = O.make_records(O.MODEL_BOIDS, ps.p, ps.v)
+    ctx = O.boids_context(np.float32)
+    with pytest.raises(RuntimeError, match="0 of 1 steps"):
+        port.run(O.MODEL_BOIDS, "grid", recs, ctx, ctx, 10.0, 10.0, 1, O.PASS_SEE0, mb=256)
