@@ -262,6 +262,26 @@ int tgpu_see_noalloc(const float *positions, unsigned n, const float *radii, con
 unsigned tgpu_noalloc_max_agents(void);
 const char *tgpu_noalloc_last_error(void);
 
+/* Device models a host brings itself (the counterpart of the reference's ocl_add_source,
+ * tay/ocl.c:274-282, and of its func_name-keyed kernels, tay/ocl.c:284-291 and
+ * tay/ocl_grid.c:376-417).  A model is CUDA code compiled by the host against
+ * include/tay_gpu_model.cuh: __device__ see / act policies, the record codec, the stream
+ * layout and the supported pass programs, gathered in one descriptor.  After
+ * registration its func names work in tay_add_see / tay_add_act on TAY_GPU_Z_GRID groups
+ * like the library's own models.
+ *   tgpu_register_model          registers a descriptor (a tgpu::ModelDesc) that stays
+ *                                valid for the life of the process; `abi` is
+ *                                TGPU_MODEL_ABI as the model was compiled.  Refused with
+ *                                TGPU_ERR_ARG (and a message) when the ABI differs, a field
+ *                                is missing or out of range, or a func name is already
+ *                                provided by another model.
+ *   tgpu_register_model_library  loads a shared library built from such a model (kept
+ *                                loaded) and registers the descriptor its exported
+ *                                `const void *tgpu_model_entry(unsigned *abi)` returns.
+ * Registration is process-wide and may happen before or between runs. */
+int tgpu_register_model(const void *desc, unsigned abi);
+int tgpu_register_model_library(const char *path);
+
 /* Resolves a func_name to its model; returns the model name or NULL. */
 const char *tgpu_model_of(const char *func_name);
 

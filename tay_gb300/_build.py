@@ -95,10 +95,25 @@ def build(verbose: bool = False, ptxas_verbose: bool = False, jobs: int = 0) -> 
         with cf.ThreadPoolExecutor(max_workers=jobs or min(len(tasks), os.cpu_count() or 4)) as ex:
             outputs = list(ex.map(lambda c: _run(c, verbose), tasks))
     if tasks or not os.path.exists(LIB):
-        _run([nvcc, "-shared", "-o", LIB] + objs + ["-lcudart"], verbose)
+        _run([nvcc, "-shared", "-o", LIB] + objs + ["-lcudart", "-ldl"], verbose)
     if ptxas_verbose:
         return "\n".join(outputs)
     return LIB
+
+
+def build_model(src: str, out: str, verbose: bool = False) -> str:
+    """Compiles a host's own device model (a .cu written against include/tay_gpu_model.cuh)
+    into the shared library `out`, for tgpu_register_model_library.  Rebuilt only when the
+    source or the engine's headers are newer."""
+    gpu = os.path.join(CSRC, "gpu")
+    deps = [src] + [os.path.join(gpu, f) for f in os.listdir(gpu) if f.endswith(".cuh")]
+    deps += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
+    if not _newer(deps, out):
+        return out
+    os.makedirs(os.path.dirname(os.path.abspath(out)), exist_ok=True)
+    _run([nvcc_path(), "-gencode", GENCODE, "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
+          "-Xcompiler", "-fPIC", "-shared", "--cudart", "shared", "-I", INCLUDE, "-I", gpu, src, "-o", out], verbose)
+    return out
 
 
 if __name__ == "__main__":

@@ -98,6 +98,8 @@ TGPU_SYMBOLS = [
     ("tgpu_set_tuning", None, [_VP]),
     ("tgpu_get_tuning", None, [_VP]),
     ("tgpu_model_of", ctypes.c_char_p, [ctypes.c_char_p]),
+    ("tgpu_register_model", ctypes.c_int, [_VP, ctypes.c_uint]),
+    ("tgpu_register_model_library", ctypes.c_int, [ctypes.c_char_p]),
     ("tgpu_batch_profile", ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
     ("tgpu_batch_kernel_classes", ctypes.c_int, [_VP]),
     ("tgpu_batch_telemetry", ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]),
@@ -355,6 +357,14 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def register_model_library(path):
+    """Registers the device model of a shared library built against
+    include/tay_gpu_model.cuh (tgpu_register_model_library); raises TayError when refused."""
+    L = lib()
+    if L.tgpu_register_model_library(os.fsencode(path)) != 0:
+        raise TayError(L.tgpu_last_error().decode())
 
 
 def run_batch(states, steps):

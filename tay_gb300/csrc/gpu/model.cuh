@@ -65,6 +65,12 @@ struct ModelDesc {
     int nonpoint;  // 1: box agents, float4 stream 0 the min corner (the position), 1 the max
 };
 
+// Layout stamp of the model interface: a model compiled against other definitions of the
+// launch descriptors or of ModelDesc carries another value and is refused at registration.
+constexpr unsigned kModelAbi = 0x01000000u ^ ((unsigned)sizeof(SeeLaunch) << 12) ^ ((unsigned)sizeof(ActLaunch) << 4) ^
+                               (unsigned)sizeof(ModelDesc) ^ ((unsigned)sizeof(KernelDesc) << 20) ^
+                               ((unsigned)sizeof(ProgramDesc) << 8);
+
 // The SPH model's adjoint kernels (used by adjoint.cu).
 struct SphAdjointKernels {
     bool (*force_record)(const SeeLaunch &L, size_t smem, cudaStream_t st);  // force + integrate, also stores a

@@ -6,6 +6,8 @@
 //   streams -> the model's pass kernels -> cell table clear
 // (the step of tay/state.c:221-311: sort every group, run the passes in order, unsort).
 // Steps are captured once per buffer-parity pattern into CUDA graphs and replayed.
+#include <dlfcn.h>
+
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -13,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -65,13 +68,22 @@ TgpuTuning default_tuning() {
 }
 TgpuTuning g_tuning = default_tuning();
 
+// Models a host registered (tgpu_register_model): kept for the life of the process, looked
+// up after the library's own.
+std::mutex g_models_lock;
+std::vector<const ModelDesc *> g_registered;
+
 const ModelDesc *model_list(int i) {
     switch (i) {
         case 0: return model_test_basic();
         case 1: return model_boids();
         case 2: return model_sph();
         case 3: return model_box();
-        default: return nullptr;
+        default: {
+            std::lock_guard<std::mutex> guard(g_models_lock);
+            const size_t k = (size_t)(i - 4);
+            return i >= 4 && k < g_registered.size() ? g_registered[k] : nullptr;
+        }
     }
 }
 
@@ -642,6 +654,80 @@ void tgpu_set_tuning(const TgpuTuning *t) {
 
 void tgpu_get_tuning(TgpuTuning *t) {
     if (t) *t = g_tuning;
+}
+
+// A host-built model: checked field by field before it joins the registry, so that a
+// descriptor built against another layout or with missing launchers is refused here rather
+// than failing inside a run.
+int tgpu_register_model(const void *desc, unsigned abi) {
+    if (!desc) return fail(TGPU_ERR_ARG, "tgpu_register_model: null descriptor");
+    if (abi != kModelAbi)
+        return fail(TGPU_ERR_ARG, "tgpu_register_model: descriptor built for model ABI 0x%08x, library has 0x%08x",
+                    abi, kModelAbi);
+    const ModelDesc *m = static_cast<const ModelDesc *>(desc);
+    if (!m->name || !m->name[0]) return fail(TGPU_ERR_ARG, "tgpu_register_model: model without a name");
+    if (m->agent_bytes < 24 || m->agent_bytes % 4)
+        return fail(TGPU_ERR_ARG, "model '%s': records of %u bytes (a multiple of 4, at least the tag and the position)",
+                    m->name, m->agent_bytes);
+    if (m->nf4 < 1 || m->nf4 > kMaxF4 || m->nu32 < 0 || m->nu32 > kMaxU32)
+        return fail(TGPU_ERR_ARG, "model '%s': %d float4 and %d u32 streams (1..%d and 0..%d)", m->name, m->nf4,
+                    m->nu32, kMaxF4, kMaxU32);
+    if (m->role_f4[0] != kState) return fail(TGPU_ERR_ARG, "model '%s': float4 stream 0 (the position) must be state", m->name);
+    for (int c = 0; c < m->nf4; ++c)
+        if (m->role_f4[c] != kState && m->role_f4[c] != kStep)
+            return fail(TGPU_ERR_ARG, "model '%s': float4 stream %d has no role", m->name, c);
+    for (int c = 0; c < m->nu32; ++c)
+        if (m->role_u32[c] != kState && m->role_u32[c] != kStep)
+            return fail(TGPU_ERR_ARG, "model '%s': u32 stream %d has no role", m->name, c);
+    if (!m->pack || !m->unpack) return fail(TGPU_ERR_ARG, "model '%s': no record codec", m->name);
+    if (m->see_ctx_bytes > 65536 || m->act_ctx_bytes > 65536)
+        return fail(TGPU_ERR_ARG, "model '%s': contexts above 64 KB", m->name);
+    if (!m->kernels || m->nkernels < 1 || !m->programs || m->nprograms < 1)
+        return fail(TGPU_ERR_ARG, "model '%s': no kernels or programs", m->name);
+    const uint32_t all_f4 = (1u << m->nf4) - 1u, all_u32 = (1u << m->nu32) - 1u;
+    for (int k = 0; k < m->nkernels; ++k) {
+        const KernelDesc &d = m->kernels[k];
+        const bool ok = d.see ? (d.launch_see && d.prepare) : (d.act && d.launch_act);
+        if (!ok || (d.writes_f4 & ~all_f4) || (d.seen_f4 & ~all_f4) || (d.writes_u32 & ~all_u32) ||
+            d.staged_f4 < 0 || d.staged_f4 > kMaxF4 || d.pair_list < 0 || d.pair_list > 2)
+            return fail(TGPU_ERR_ARG, "model '%s': kernel %d is incomplete or names streams it does not have", m->name, k);
+    }
+    for (int p = 0; p < m->nprograms; ++p) {
+        const ProgramDesc &pr = m->programs[p];
+        if (pr.passes < 1 || pr.passes > 4 || pr.kernels < 1 || pr.kernels > 4)
+            return fail(TGPU_ERR_ARG, "model '%s': program %d has %d passes in %d kernels", m->name, p, pr.passes,
+                        pr.kernels);
+        for (int q = 0; q < pr.passes; ++q)
+            if (!pr.names[q] || !model_has_func(m, pr.names[q]))
+                return fail(TGPU_ERR_ARG, "model '%s': program %d names a func no kernel provides", m->name, p);
+        for (int q = 0; q < pr.kernels; ++q)
+            if (pr.kernel_index[q] < 0 || pr.kernel_index[q] >= m->nkernels)
+                return fail(TGPU_ERR_ARG, "model '%s': program %d uses kernel %d of %d", m->name, p,
+                            pr.kernel_index[q], m->nkernels);
+    }
+    // a func name selects exactly one model
+    for (int k = 0; k < m->nkernels; ++k)
+        for (const char *fn : {m->kernels[k].see, m->kernels[k].act})
+            if (fn)
+                if (const ModelDesc *other = find_model(fn))
+                    return fail(TGPU_ERR_ARG, "model '%s': func '%s' is already provided by model '%s'", m->name, fn,
+                                other->name);
+    std::lock_guard<std::mutex> guard(g_models_lock);
+    g_registered.push_back(m);
+    return TGPU_OK;
+}
+
+int tgpu_register_model_library(const char *path) {
+    if (!path) return fail(TGPU_ERR_ARG, "tgpu_register_model_library: null path");
+    // kept loaded for the life of the process: the registry points into it
+    void *h = dlopen(path, RTLD_NOW | RTLD_LOCAL);
+    if (!h) return fail(TGPU_ERR_ARG, "tgpu_register_model_library: %s", dlerror());
+    using Entry = const void *(*)(unsigned *);
+    Entry entry = reinterpret_cast<Entry>(dlsym(h, "tgpu_model_entry"));
+    if (!entry) return fail(TGPU_ERR_ARG, "tgpu_register_model_library: %s exports no tgpu_model_entry", path);
+    unsigned abi = 0;
+    const void *desc = entry(&abi);
+    return tgpu_register_model(desc, abi);
 }
 
 const char *tgpu_model_of(const char *func_name) {
