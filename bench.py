@@ -61,6 +61,9 @@ def parse():
     ap.add_argument("--features", type=int, default=1, help="1 = add the two-group / resident / dims-2 / box legs")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--adjoint", type=int, default=1, help="1 = add the differentiable SPH leg")
+    ap.add_argument("--adjoint-steps", type=int, default=200, help="rollout steps of the differentiable SPH leg")
+    ap.add_argument("--adjoint-keeps", default="2,1,0",
+                    help="kept segments of each adjoint run (checkpoints every 20 steps; 0 records every step)")
     ap.add_argument("--stage", type=int, default=None, help="see kernel: 1 = stage halos in shared memory")
     ap.add_argument("--union-factor", type=int, default=None, help="see kernel: union walk threshold")
     ap.add_argument("--cell-order", type=int, default=None, help="0 = Morton cells, 1 = x-rows")
@@ -679,9 +682,10 @@ def run_gb300(args, rank, world, D):
             line["sph"] = sph_leg(min(args.steps, 20), not args.no_autotune, cpu_steps=2 if cpu else 0)
         if args.adjoint:
             tune = not args.no_autotune
-            line["adjoint"] = adjoint_leg(keep=6, tune=tune)
-            line["adjoint_keep1"] = adjoint_leg(keep=1, tune=tune)
-            line["adjoint_record_all"] = adjoint_leg(every=0, tune=tune)
+            for i, keep in enumerate(int(k) for k in args.adjoint_keeps.split(",") if k.strip()):
+                name = "adjoint_record_all" if keep == 0 else ("adjoint" if i == 0 else f"adjoint_keep{keep}")
+                line[name] = adjoint_leg(steps=args.adjoint_steps, every=0 if keep == 0 else 20, keep=max(keep, 1),
+                                         tune=tune)
         if args.features:
             line["features"] = features_leg(setup, recs, line["tuning"])
         if cpu:
@@ -691,8 +695,8 @@ def run_gb300(args, rank, world, D):
               "see_issue_frac": round(floor_ms / see_ms, 3), "see_hbm_frac": round(achieved / peak, 4)}
         if "batched" in line:
             tg["batched_speedup"] = round(line["batched"]["speedup"], 2)
-        for k in ("adjoint", "adjoint_keep2", "adjoint_keep1"):
-            if k in line:
+        for k in line:
+            if k.startswith("adjoint"):
                 tg[k + "_fwd_bwd_over_fwd"] = round(line[k]["fwd_plus_bwd_over_fwd"], 3)
         line["targets"] = tg
         print(json.dumps(line), flush=True)

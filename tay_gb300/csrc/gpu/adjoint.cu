@@ -37,6 +37,14 @@ struct Checkpoint {
     uint32_t *id;
 };
 
+// The pair list of one step of a segment (the batch's list layout, PairList): recorded by
+// the step's forward density pass, replayed by its forward force pass and, in the backward
+// sweep, by the force and density adjoints.
+struct StepList {
+    uint4 *idx;
+    uint2 *count;
+};
+
 // gid[i] = begin(segment of i) + id[i]
 __global__ void __launch_bounds__(kSortThreads) gid_kernel(const SegmentSpec *__restrict__ specs,
                                                            const uint32_t *__restrict__ tile_seg,
@@ -86,6 +94,9 @@ struct TgpuAdjoint {
     const tgpu::SphAdjointKernels *K = nullptr;
     std::vector<tgpu::Record> rec;
     std::vector<tgpu::Checkpoint> cp;  // cp[k] = state before step k*every; last = final state
+    // checkpoint mode with pair lists: one list per step of a segment, filled by the forward
+    // run for the last segment and by each recomputation for the others
+    std::vector<tgpu::StepList> lists;
     float4 *xbar_id = nullptr, *vbar_id = nullptr, *xbar_s = nullptr, *vbar_s = nullptr;
     float4 *abar = nullptr, *rhobar = nullptr, *theta = nullptr;
     double *d_theta = nullptr;
@@ -172,8 +183,9 @@ SeeLaunch see_launch(TgpuBatch *b, const KernelRun &r, const PassIO &io) {
 }
 
 // One forward step (the SPH program's kernels, with the acceleration stored), recording
-// the step into `r` when given.
-void recorded_step(TgpuAdjoint *a, Record *r) {
+// the step into `r` when given, and its pair list into `pl` when given (else into the
+// batch's own list).
+void recorded_step(TgpuAdjoint *a, Record *r, const StepList *pl = nullptr) {
     TgpuBatch *b = a->b;
     cudaStream_t st = b->st;
     SortLaunch L = sort_launch(b);
@@ -200,6 +212,10 @@ void recorded_step(TgpuAdjoint *a, Record *r) {
     const KernelRun &rd = b->runs[0];
     SeeLaunch SD = see_launch(b, rd, make_io(b, rd.k, true, 0));
     attach_pair_list(b, rd, SD);
+    if (pl && SD.plist.mode) {
+        SD.plist.idx = pl->idx;
+        SD.plist.count = pl->count;
+    }
     rd.k->launch_see(SD, 0, st);
     // force + integrate, acceleration stored (replaying the list)
     const KernelRun &rf = b->runs[1];
@@ -207,6 +223,10 @@ void recorded_step(TgpuAdjoint *a, Record *r) {
     const float4 *pos_in = io.in_f4[SPH_POS], *vel_in = io.in_f4[SPH_VEL];
     SeeLaunch SF = see_launch(b, rf, io);
     attach_pair_list(b, rf, SF);
+    if (pl && SF.plist.mode) {
+        SF.plist.idx = pl->idx;
+        SF.plist.count = pl->count;
+    }
     a->K->force_record(SF, 0, st);
     for (int c = 0; c < b->m->nf4; ++c)
         if (b->m->role_f4[c] == kState && (rf.k->writes_f4 >> c & 1u) && (rf.k->seen_f4 >> c & 1u)) b->cur_f4[c] ^= 1;
@@ -224,7 +244,10 @@ void recorded_step(TgpuAdjoint *a, Record *r) {
     launch_cell_table(L, skeys, 0, st);
 }
 
-void backward_step(TgpuAdjoint *a, const Record &r) {
+// One backward step.  With `pl` (the step's stored pair list) the force adjoint and the
+// density adjoint replay it; without, the force adjoint walks and records the batch's list
+// for the density adjoint.
+void backward_step(TgpuAdjoint *a, const Record &r, const StepList *pl = nullptr) {
     TgpuBatch *b = a->b;
     cudaStream_t st = b->st;
     cudaMemcpyAsync(b->d_box, r.box, (size_t)b->nseg * sizeof(BoxAcc), cudaMemcpyDeviceToDevice, st);
@@ -269,11 +292,19 @@ void backward_step(TgpuAdjoint *a, const Record &r) {
     SeeLaunch F = see_launch(b, rf, fa);
     SeeLaunch D = see_launch(b, rd, fa);
     D.skip_self = 1;  // the self pair contributes nothing to the density adjoint
-    if (b->plist_idx && rf.skip_self) {
-        F.plist = PairList{b->plist_idx, b->plist_count, b->total, b->plist_cap, 1u, nullptr, nullptr};
-        D.plist = PairList{b->plist_idx, b->plist_count, b->total, b->plist_cap, 2u, rf.d_radii, rf.d_see_ctx};
+    if (pl) {
+        // the forward density pass's list: it holds every pair inside the support (and the
+        // particle itself, which both adjoints skip)
+        F.plist = PairList{pl->idx, pl->count, b->total, b->plist_cap, 2u, rd.d_radii, rd.d_see_ctx};
+        D.plist = F.plist;
+        a->K->force_adj_replay(F, 0, st);
+    } else {
+        if (b->plist_idx && rf.skip_self) {
+            F.plist = PairList{b->plist_idx, b->plist_count, b->total, b->plist_cap, 1u, nullptr, nullptr};
+            D.plist = PairList{b->plist_idx, b->plist_count, b->total, b->plist_cap, 2u, rf.d_radii, rf.d_see_ctx};
+        }
+        a->K->force_adj(F, 0, st);
     }
-    a->K->force_adj(F, 0, st);
     a->K->density_adj(D, 0, st);
 
     PassIO sa = io;
@@ -334,6 +365,16 @@ int tgpu_adjoint_create(TgpuBatch *b, int steps, int checkpoint_every, int keep_
     if (!rc) rc = alloc(a, &a->rhobar, n);
     if (!rc) rc = alloc(a, &a->theta, n);
     if (!rc) rc = alloc(a, &a->d_theta, 2 * (size_t)b->nseg);
+    // per-step lists of one segment when the batch pairs its density and force passes
+    // through a list (checkpoint mode only: a list per step of the whole rollout would not fit)
+    if (!rc && checkpoint_every > 0 && b->plist_idx && b->runs.size() == 2 && b->runs[0].list_mode == 1u &&
+        b->runs[1].list_mode == 2u) {
+        a->lists.resize((size_t)checkpoint_every);
+        for (auto &l : a->lists) {
+            if ((rc = alloc(a, &l.idx, (size_t)(b->plist_cap / 4u) * n))) break;
+            if ((rc = alloc(a, &l.count, n))) break;
+        }
+    }
     if (!rc && (cudaEventCreate(&a->e0) != cudaSuccess || cudaEventCreate(&a->e1) != cudaSuccess))
         rc = fail(TGPU_ERR_CUDA, "adjoint: cudaEventCreate failed");
     if (rc) {
@@ -359,7 +400,9 @@ int tgpu_adjoint_forward(TgpuAdjoint *a) {
         } else {
             const int seg = s / a->every;
             if (s % a->every == 0) save_checkpoint(b, a->cp[seg]);
-            recorded_step(a, seg >= first_kept ? &a->rec[(seg - first_kept) * a->every + s % a->every] : nullptr);
+            // the last segment's lists stay for the first segment of the backward sweep
+            const StepList *pl = seg == segs - 1 && !a->lists.empty() ? &a->lists[s % a->every] : nullptr;
+            recorded_step(a, seg >= first_kept ? &a->rec[(seg - first_kept) * a->every + s % a->every] : nullptr, pl);
         }
     }
     if (a->every > 0) save_checkpoint(b, a->cp.back());
@@ -396,13 +439,16 @@ int tgpu_adjoint_backward(TgpuAdjoint *a, const float *dl_dpos, const float *dl_
             const int first = k * a->every;
             const int len = std::min(a->every, a->steps - first);
             int base = 0;
+            // stored pair lists: the last segment's from the forward run, a recomputed
+            // segment's from its recomputation; other kept segments walk
+            const bool lists = !a->lists.empty() && (k == segs - 1 || k < first_kept);
             if (k >= first_kept) {
                 base = (k - first_kept) * a->every;  // recorded by the forward run
             } else {
                 restore_checkpoint(b, a->cp[k]);  // recompute the segment, recording it
-                for (int s = 0; s < len; ++s) recorded_step(a, &a->rec[s]);
+                for (int s = 0; s < len; ++s) recorded_step(a, &a->rec[s], lists ? &a->lists[s] : nullptr);
             }
-            for (int s = len - 1; s >= 0; --s) backward_step(a, a->rec[base + s]);
+            for (int s = len - 1; s >= 0; --s) backward_step(a, a->rec[base + s], lists ? &a->lists[s] : nullptr);
         }
         restore_checkpoint(b, a->cp.back());  // the batch ends where the forward run ended
     }

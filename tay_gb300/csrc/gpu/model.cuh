@@ -76,8 +76,10 @@ struct SphAdjointKernels {
     bool (*force_record)(const SeeLaunch &L, size_t smem, cudaStream_t st);  // force + integrate, also stores a
     cudaError_t (*force_record_prepare)(size_t smem);
     void (*integrate_adj)(const ActLaunch &L, cudaStream_t st);
-    bool (*force_adj)(const SeeLaunch &L, size_t smem, cudaStream_t st);
+    bool (*force_adj)(const SeeLaunch &L, size_t smem, cudaStream_t st);  // walks, records the pair list
     cudaError_t (*force_adj_prepare)(size_t smem);
+    bool (*force_adj_replay)(const SeeLaunch &L, size_t smem, cudaStream_t st);  // replays a stored list
+    cudaError_t (*force_adj_replay_prepare)(size_t smem);
     bool (*density_adj)(const SeeLaunch &L, size_t smem, cudaStream_t st);
     cudaError_t (*density_adj_prepare)(size_t smem);
     void (*scatter_adj)(const ActLaunch &L, cudaStream_t st);

@@ -65,7 +65,7 @@ TGPU_D float dist2(float dx, float dy, float dz) {
 
 TGPU_D float kernel_d2w(float q, float sigma, float inv_h) {
     const float s2 = sigma * inv_h * inv_h;
-    if (q < 1.0f) return s2 * (-3.0f + 4.5f * q);
+    if (q < 1.0f) return s2 * __fmaf_rn(4.5f, q, -3.0f);
     if (q < 2.0f) return s2 * (1.5f * (2.0f - q));
     return 0.0f;
 }
@@ -299,6 +299,9 @@ struct ForceAdjSeer {
 //   theta += (abar_k.d) dc/d(alpha, c0)
 // then the pressure adjoint: rhobar_k += Pbar_k dP/drho, dL/dc0 += Pbar_k 2 P_k / c0.
 // The adjoint decides nothing, so it uses the fast reciprocal square root and divisions.
+// Every product and sum is an explicit rounded operation (or an explicit fused one), so
+// the walk that records the pair list and the replay of a stored list (ForceAdjReplay)
+// give the same bits.
 struct ForceAdj {
     using SeeCtx = Ctx;
     using ActCtx = Ctx;
@@ -330,46 +333,47 @@ struct ForceAdj {
         if (!(r2 < c.support2 && r2 > 0.0f)) return;
         const float4 bv = acc.f4(1, j), brp = acc.f4(2, j), bab = acc.f4(3, j);
         const float rinv = rsqrtf(r2);
-        const float r = r2 * rinv;
-        const float q = r * c.inv_h;
+        const float r = __fmul_rn(r2, rinv);
+        const float q = __fmul_rn(r, c.inv_h);
         const float dw = kernel_dw(q, c.sigma, c.inv_h);
         const float d2w = kernel_d2w(q, c.sigma, c.inv_h);
-        const float D = dw * rinv;
-        const float Dp_r = (d2w - D) * rinv * rinv;  // (dD/dr) / r
+        const float D = __fmul_rn(dw, rinv);
+        const float Dp_r = __fmul_rn(__fmul_rn(__fsub_rn(d2w, D), rinv), rinv);  // (dD/dr) / r
         const float vx = s.v.x - bv.x, vy = s.v.y - bv.y, vz = s.v.z - bv.z;
-        const float sv = (vx * dx + vy * dy) + vz * dz;
+        const float sv = __fmaf_rn(vz, dz, __fmaf_rn(vy, dy, __fmul_rn(vx, dx)));
         float Pi = 0.0f, Pi_s = 0.0f, Pi_r2 = 0.0f, Pi_rb = 0.0f, Pi_al = 0.0f, Pi_c0 = 0.0f;
         if (sv < 0.0f) {
-            const float inv_rb = __fdividef(2.0f, s.rho + brp.x);
-            const float inv_den = __fdividef(1.0f, r2 + c.eta2);
-            const float k0 = c.h * inv_den * inv_rb;
-            Pi_al = -c.c0 * k0 * sv;
-            Pi_c0 = -c.alpha * k0 * sv;
-            Pi = c.alpha * Pi_al;
-            Pi_s = -c.alpha * c.c0 * k0;
-            Pi_r2 = -Pi * inv_den;
-            Pi_rb = -Pi * inv_rb;
+            const float inv_rb = __fdividef(2.0f, __fadd_rn(s.rho, brp.x));
+            const float inv_den = __fdividef(1.0f, __fadd_rn(r2, c.eta2));
+            const float k0 = __fmul_rn(__fmul_rn(c.h, inv_den), inv_rb);
+            Pi_al = __fmul_rn(__fmul_rn(-c.c0, k0), sv);
+            Pi_c0 = __fmul_rn(__fmul_rn(-c.alpha, k0), sv);
+            Pi = __fmul_rn(c.alpha, Pi_al);
+            Pi_s = __fmul_rn(__fmul_rn(-c.alpha, c.c0), k0);
+            Pi_r2 = __fmul_rn(-Pi, inv_den);
+            Pi_rb = __fmul_rn(-Pi, inv_rb);
         }
-        const float T = (s.A + brp.z) + Pi;
-        const float mD = -c.m * D;
-        const float cc = mD * T;
+        const float T = __fadd_rn(__fadd_rn(s.A, brp.z), Pi);
+        const float mD = __fmul_rn(-c.m, D);
+        const float cc = __fmul_rn(mD, T);
         const float wx = s.ab.x - bab.x, wy = s.ab.y - bab.y, wz = s.ab.z - bab.z;
-        const float xw = (dx * wx + dy * wy) + dz * wz;
-        const float coef_d = -c.m * (2.0f * Pi_r2 * D + T * Dp_r);
-        const float coef_v = mD * Pi_s;
-        s.xb[0] += cc * wx + xw * (coef_v * vx + coef_d * dx);
-        s.xb[1] += cc * wy + xw * (coef_v * vy + coef_d * dy);
-        s.xb[2] += cc * wz + xw * (coef_v * vz + coef_d * dz);
-        const float xwv = xw * coef_v;
-        s.vb[0] += xwv * dx;
-        s.vb[1] += xwv * dy;
-        s.vb[2] += xwv * dz;
-        const float xmD = xw * mD;
-        s.rhob += xmD * (s.drho_A + 0.5f * Pi_rb);
-        s.Pb += xmD;
-        const float ad = ((s.ab.x * dx + s.ab.y * dy) + s.ab.z * dz) * mD;
-        s.ta += ad * Pi_al;
-        s.tc += ad * Pi_c0;
+        const float xw = __fmaf_rn(dz, wz, __fmaf_rn(dy, wy, __fmul_rn(dx, wx)));
+        const float coef_d = __fmul_rn(-c.m, __fmaf_rn(T, Dp_r, __fmul_rn(__fmul_rn(2.0f, Pi_r2), D)));
+        const float coef_v = __fmul_rn(mD, Pi_s);
+        const float dd[3] = {dx, dy, dz}, ww[3] = {wx, wy, wz}, vv[3] = {vx, vy, vz};
+        const float xwv = __fmul_rn(xw, coef_v);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float inner = __fmaf_rn(coef_d, dd[k], __fmul_rn(coef_v, vv[k]));
+            s.xb[k] = __fadd_rn(s.xb[k], __fmaf_rn(xw, inner, __fmul_rn(cc, ww[k])));
+            s.vb[k] = __fmaf_rn(xwv, dd[k], s.vb[k]);
+        }
+        const float xmD = __fmul_rn(xw, mD);
+        s.rhob = __fmaf_rn(xmD, __fmaf_rn(0.5f, Pi_rb, s.drho_A), s.rhob);
+        s.Pb = __fadd_rn(s.Pb, xmD);
+        const float ad = __fmul_rn(__fmaf_rn(s.ab.z, dz, __fmaf_rn(s.ab.y, dy, __fmul_rn(s.ab.x, dx))), mD);
+        s.ta = __fmaf_rn(ad, Pi_al, s.ta);
+        s.tc = __fmaf_rn(ad, Pi_c0, s.tc);
     }
     TGPU_D static void finish(Seer &s, const float4 &, const PassIO &io, uint32_t i, const Ctx &c, const Ctx &) {
         s.Pb *= s.inv_rho2;  // dc/dP_k = -m D / rho_k^2
@@ -384,6 +388,14 @@ struct ForceAdj {
         io.out_f4[A_VBAR][i] = make_float4(vb.x + s.vb[0], vb.y + s.vb[1], vb.z + s.vb[2], 0.0f);
         io.out_f4[A_THETA][i] = make_float4(s.ta, s.tc, 0.0f, 0.0f);
     }
+};
+
+// The force adjoint over a stored pair list of the step (the list its forward density pass
+// recorded): the same see function, no walk and no recording; DensityAdj then replays the
+// same list.
+struct ForceAdjReplay : ForceAdj {
+    static constexpr int kPairList = 2;
+    TGPU_D static bool replay_ok(const Ctx &mine, const Ctx &rec) { return mine.support2 <= rec.support2; }
 };
 
 struct DensityAdjSeer {
@@ -436,6 +448,7 @@ const SphAdjointKernels kAdjoint = {
     launch_see_t<Force<true, true>>, prepare_see_t<Force<true, true>>,
     launch_act_t<IntegrateAdj>,
     launch_see_t<ForceAdj>, prepare_see_t<ForceAdj>,
+    launch_see_t<ForceAdjReplay>, prepare_see_t<ForceAdjReplay>,
     launch_see_t<DensityAdj>, prepare_see_t<DensityAdj>,
     launch_act_t<ScatterAdj>,
     (uint32_t)sizeof(Ctx),
