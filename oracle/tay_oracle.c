@@ -316,7 +316,7 @@ static void o_z_grid_sort(OGroup *g) {
 /* tay/cpu_grid.c:74-156.  Returns 0, without touching the cells, when the grid has more
  * cells than the structure's memory holds: the reference's shrink step rounds every axis
  * up (tay/cpu_grid.c:100-108), which can leave cells_count above max_cells, and the
- * reference then indexes past its cell array (it faults on the 1M-boid workload with 256 MB).
+ * reference then indexes past its cell array (the 1M-boid workload with 256 MB does this).
  * Every other grid is the reference's, unchanged. */
 static int o_grid_sort(OGroup *g) {
     o_update_box(g);
