@@ -74,6 +74,16 @@ TGPU_D void see_fn(Seer &s, const float4 &a, const float4 &b, const Acc &acc, ui
     }
 }
 
+// The pairs see_fn acts on: 0 < d2 < r2, d2 rounded exactly as see_fn rounds it (the walk
+// enters the see body only for these).
+TGPU_D bool keep_fn(const float4 &a, const float4 &b, const Ctx &c) {
+    const float dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
+    float d2 = __fmul_rn(dx, dx);
+    d2 = __fadd_rn(d2, __fmul_rn(dy, dy));
+    d2 = __fadd_rn(d2, __fmul_rn(dz, dz));
+    return d2 < c.r2 && d2 > 0.0f;
+}
+
 TGPU_D float len3(float x, float y, float z) {
     float s = x * x;
     s = s + y * y;
@@ -129,6 +139,8 @@ struct SeeOnly {
     using Seer = boids::Seer;
     static constexpr int kSeenF4 = 2;
     static constexpr int kLaneUnroll = 4;
+    static constexpr bool kKeepGate = true;
+    TGPU_D static bool keep(const float4 &a, const float4 &b, const Ctx &c) { return keep_fn(a, b, c); }
     TGPU_D static int seen_stream(int k) { return k == 0 ? POS : VEL; }
     TGPU_D static void load(Seer &s, const PassIO &, uint32_t, const Ctx &, const Ctx &) { zero(s); }
     template <class Acc>
@@ -149,6 +161,8 @@ struct SeeAct {
     using Seer = boids::Seer;
     static constexpr int kSeenF4 = 2;
     static constexpr int kLaneUnroll = 4;
+    static constexpr bool kKeepGate = true;
+    TGPU_D static bool keep(const float4 &a, const float4 &b, const Ctx &c) { return keep_fn(a, b, c); }
     TGPU_D static int seen_stream(int k) { return k == 0 ? POS : VEL; }
     TGPU_D static void load(Seer &s, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {
         zero(s);

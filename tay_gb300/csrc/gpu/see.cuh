@@ -186,13 +186,48 @@ struct UnrollOf<P, decltype((void)P::kLaneUnroll)> {
 
 // Per-lane walk over candidates [j0, j1): UnrollOf<P> candidates per iteration for
 // independent loads in flight; a recording pass passes its recorder as `rec`.
-template <class P, class Acc, class Rec = NoRec>
+// Whether pass P gates its see body on its keep test (P::kKeepGate): the see function
+// does nothing for a pair that passed the box test but not P::keep, so the walk counts the
+// box-test pass without a branch and enters the body only for kept pairs.  keep(a, a) must
+// be false (a seer never keeps itself, as for a distance test with d2 > 0): the gated walk
+// then tests the seer like any candidate and takes its one box-test pass off the counter
+// at the end, instead of comparing every index with the seer's.
+template <class P, class = void>
+struct GateOf {
+    static constexpr bool value = false;
+};
+template <class P>
+struct GateOf<P, decltype((void)P::kKeepGate)> {
+    static constexpr bool value = P::kKeepGate;
+};
+
+// One candidate of a lane's walk: the reference's box test and self skip, the pair
+// counter, the recorder, and the see function (behind P::keep when the pass gates on it).
+template <class P, bool kGate, class Acc, class Rec>
+TGPU_D void lane_one(typename P::Seer &s, const float4 &sp, const float4 &b, const float4 &r4, uint32_t j,
+                     uint32_t self, const Acc &acc, const typename P::SeeCtx &sctx, uint32_t &pairs, Rec *rec) {
+    constexpr bool kRec = std::is_same_v<Rec, ListRec>;
+    if constexpr (kGate && !kRec) {
+        // the reference's test on d = seer - seen; |seen - seer| is the same float, and the
+        // model's keep and see compute seen - seer, which the compiler then shares
+        const bool hit = !(fabsf(b.x - sp.x) > r4.x) && !(fabsf(b.y - sp.y) > r4.y) && !(fabsf(b.z - sp.z) > r4.z);
+        pairs += hit ? 1u : 0u;
+        if (hit && P::keep(sp, b, sctx)) P::see(s, sp, b, acc, j, sctx);
+    } else {
+        if (j != self && box_hit(sp, b, r4)) {
+            ++pairs;
+            if constexpr (kRec) record_pair<P>(*rec, sp, b, j, sctx);
+            P::see(s, sp, b, acc, j, sctx);
+        }
+    }
+}
+
+template <class P, class Acc, class Rec = NoRec, bool kGate = false>
 TGPU_D void lane_run(typename P::Seer &s, const float4 &sp, const float4 &r4, uint32_t j0, uint32_t j1, uint32_t self,
                      const float4 *src, const Acc &acc, const typename P::SeeCtx &sctx, uint32_t &pairs,
                      uint32_t &tested, Rec *rec = nullptr) {
     constexpr bool kGlobal = Acc::kGlobal;
     constexpr int U = UnrollOf<P>::value;
-    constexpr bool kRec = std::is_same_v<Rec, ListRec>;
     if (j1 <= j0) return;
     tested += j1 - j0;
     uint32_t j = j0;
@@ -203,21 +238,9 @@ TGPU_D void lane_run(typename P::Seer &s, const float4 &sp, const float4 &r4, ui
 #pragma unroll
         for (int u = 0; u < U; ++u) b[u] = load_pos(src, j + u, kGlobal);
 #pragma unroll
-        for (int u = 0; u < U; ++u)
-            if (j + u != self && box_hit(sp, b[u], r4)) {
-                ++pairs;
-                if constexpr (kRec) record_pair<P>(*rec, sp, b[u], j + u, sctx);
-                P::see(s, sp, b[u], acc, j + u, sctx);
-            }
+        for (int u = 0; u < U; ++u) lane_one<P, kGate>(s, sp, b[u], r4, j + u, self, acc, sctx, pairs, rec);
     }
-    for (; j < j1; ++j) {
-        const float4 b0 = load_pos(src, j, kGlobal);
-        if (j != self && box_hit(sp, b0, r4)) {
-            ++pairs;
-            if constexpr (kRec) record_pair<P>(*rec, sp, b0, j, sctx);
-            P::see(s, sp, b0, acc, j, sctx);
-        }
-    }
+    for (; j < j1; ++j) lane_one<P, kGate>(s, sp, load_pos(src, j, kGlobal), r4, j, self, acc, sctx, pairs, rec);
 }
 
 // Replay of a recorded pair list: the see function over the seer's n entries in their
@@ -853,8 +876,13 @@ __global__ void __launch_bounds__(kSeeThreads, kStage ? 1 : 8) see_rows_kernel(S
                         lane_run_boxes<P>(s, sp, smax, r4, jr.x, jr.y, self, pos, L.io.in_f4[1], acc, sctx, pairs,
                                           tested);
                     else
-                        lane_run<P>(s, sp, r4, jr.x, jr.y, self, pos, acc, sctx, pairs, tested);
+                        lane_run<P, decltype(acc), NoRec, GateOf<P>::value>(s, sp, r4, jr.x, jr.y, self, pos, acc,
+                                                                             sctx, pairs, tested);
                 }
+            // the gated walk tested the seer too (it lies in its own range): its box-test
+            // pass comes off the counter when the pass skips self
+            if constexpr (GateOf<P>::value && !kBox)
+                if (self != 0xFFFFFFFFu && box_hit(sp, sp, r4)) --pairs;
         }
     } else if (recording && active) {
         L.plist.count[i] = make_uint2(0u, 0u);  // no cell to walk: an empty, complete list
