@@ -240,7 +240,17 @@ TGPU_D void lane_run(typename P::Seer &s, const float4 &sp, const float4 &r4, ui
 #pragma unroll
         for (int u = 0; u < U; ++u) lane_one<P, kGate>(s, sp, b[u], r4, j + u, self, acc, sctx, pairs, rec);
     }
-    for (; j < j1; ++j) lane_one<P, kGate>(s, sp, load_pos(src, j, kGlobal), r4, j, self, acc, sctx, pairs, rec);
+    // the last j1 - j < U candidates: their loads issued together (indices clamped into the
+    // range, so every load is in bounds), then tested in order
+    const uint32_t rem = j1 - j;
+    if (rem) {
+        float4 b[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) b[u] = load_pos(src, j + min((uint32_t)u, rem - 1u), kGlobal);
+#pragma unroll
+        for (int u = 0; u < U - 1; ++u)
+            if ((uint32_t)u < rem) lane_one<P, kGate>(s, sp, b[u], r4, j + u, self, acc, sctx, pairs, rec);
+    }
 }
 
 // Replay of a recorded pair list: the see function over the seer's n entries in their
