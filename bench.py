@@ -217,7 +217,26 @@ def batched_workload(states):
     return groups
 
 
-def batched_vs_plain(states, steps, tune=True):
+def batched_cpu_baseline(groups, steps=1):
+    """The batched workload on the host: every state one by one on CpuZGrid (oracle
+    restatement, all host threads), `steps` steps each from its initial state."""
+    from oracle import pyoracle as O
+
+    threads = os.cpu_count() or 1
+    pairs, secs = 0, 0.0
+    for setup, recs in groups:
+        ctx = setup.passes[0].ctx
+        r = O.port().run(O.MODEL_BOIDS, "z_grid", recs, ctx, ctx, setup.passes[0].radius, setup.part, steps,
+                         O.PASS_SEE0 | O.PASS_ACT0, threads=threads, mb=setup.mb)
+        pairs += r.pairs
+        secs += r.ms_per_step * steps / 1000.0
+    return {"value": pairs / secs, "unit": "pair-interactions/s", "cores": threads, "kind": "port",
+            "ms_per_step": 1000.0 * secs / steps,
+            "sample": f"{steps} step(s) of each of the {len(groups)} states, one state after another, on CpuZGrid "
+                      f"(oracle restatement, {threads} threads)"}
+
+
+def batched_vs_plain(states, steps, tune=True, cpu_steps=0):
     """Device-resident comparison on the same GPU: one batch of all states (one launch per
     kernel per step) against the states run one by one (each its own batch and step)."""
     from tay_gb300 import api, autotune
@@ -254,12 +273,15 @@ def batched_vs_plain(states, steps, tune=True):
         s.close()
     tuning = api.get_tuning()
     api.set_tuning()
-    return {"tuning": tuning, "states": states, "agents": agents, "steps": steps, "plain_steps": plain_steps,
-            "batched_ms_per_step": wall_b * 1000.0, "batched_device_ms_per_step": dev_ms / steps,
-            "batched_pairs_per_s": pairs / (wall_b * steps),
-            "plain_ms_per_step": wall_p * 1000.0, "plain_device_ms_per_step": dev_p / plain_steps,
-            "plain_pairs_per_s": pairs_p / (wall_p * plain_steps),
-            "speedup": wall_p / wall_b}
+    out = {"tuning": tuning, "states": states, "agents": agents, "steps": steps, "plain_steps": plain_steps,
+           "batched_ms_per_step": wall_b * 1000.0, "batched_device_ms_per_step": dev_ms / steps,
+           "batched_pairs_per_s": pairs / (wall_b * steps),
+           "plain_ms_per_step": wall_p * 1000.0, "plain_device_ms_per_step": dev_p / plain_steps,
+           "plain_pairs_per_s": pairs_p / (wall_p * plain_steps),
+           "speedup": wall_p / wall_b}
+    if cpu_steps:
+        out["cpu_baseline"] = batched_cpu_baseline(groups, cpu_steps)
+    return out
 
 
 def sph_leg(steps, tune=True, cpu_steps=0):
@@ -306,7 +328,27 @@ def sph_leg(steps, tune=True, cpu_steps=0):
     return out
 
 
-def adjoint_leg(steps=200, every=20, instances=32, keep=1, tune=True):
+def adjoint_cpu_baseline(points, tank, steps=2, instances=32):
+    """The calibration rollout's forward on the host: one instance (the instances are the
+    same lattice) on CpuZGrid, all four SPH passes, `steps` steps (oracle restatement, all
+    host threads); the batch's time is that of its instances one after another."""
+    from oracle import pyoracle as O
+    from tay_gb300 import models as M
+
+    threads = os.cpu_count() or 1
+    setup = M.sph_setup(alpha=0.05, c0=20.0, tank_min=(0.0, 0.0, 0.0), tank_max=tank, mb=64)
+    recs = M.records(M.SPH_RECORD, points.p, points.v)
+    ctx = setup.passes[0].ctx
+    r = O.port().run(O.MODEL_SPH, "z_grid", recs, ctx, ctx, setup.passes[0].radius, setup.part, steps, 15,
+                     threads=threads, mb=setup.mb)
+    batch_ms = r.ms_per_step * instances
+    return {"value": r.pairs / (r.ms_per_step * steps / 1000.0), "unit": "pair-interactions/s", "cores": threads,
+            "kind": "port", "ms_per_step": batch_ms, "forward_ms_for_the_rollout_steps": None,
+            "sample": f"{steps} forward steps of one {points.n}-particle instance on CpuZGrid (oracle restatement, "
+                      f"{threads} threads); ms_per_step is that of the {instances} instances one after another"}
+
+
+def adjoint_leg(steps=200, every=20, instances=32, keep=1, tune=True, cpu_steps=0):
     """The differentiable SPH calibration: `instances` SPH instances of 20,480
     particles (32x40x16 lattice, spacing 0.01, h 0.02), a `steps`-step rollout, loss = MSE
     of final positions against a target rollout (alpha 0.08, c0 22, same initial state);
@@ -346,11 +388,16 @@ def adjoint_leg(steps=200, every=20, instances=32, keep=1, tune=True):
     roll.close()
     tuning = api.get_tuning()
     api.set_tuning()
-    return {"instances": instances, "particles_per_instance": n, "steps": steps, "checkpoint_every": every,
-            "kept_segments": keep if every else None, "tuning": tuning,
-            "forward_ms": fwd_ms, "recorded_forward_ms": rec_ms, "backward_ms": bwd_ms,
-            "fwd_plus_bwd_over_fwd": (rec_ms + bwd_ms) / fwd_ms, "device_bytes": mem, "loss": loss,
-            "dloss_dalpha_mean": float(dp[:, 0].mean()), "dloss_dc0_mean": float(dp[:, 1].mean())}
+    out = {"instances": instances, "particles_per_instance": n, "steps": steps, "checkpoint_every": every,
+           "kept_segments": keep if every else None, "tuning": tuning,
+           "forward_ms": fwd_ms, "recorded_forward_ms": rec_ms, "backward_ms": bwd_ms,
+           "fwd_plus_bwd_over_fwd": (rec_ms + bwd_ms) / fwd_ms, "device_bytes": mem, "loss": loss,
+           "dloss_dalpha_mean": float(dp[:, 0].mean()), "dloss_dc0_mean": float(dp[:, 1].mean())}
+    if cpu_steps:
+        cb = adjoint_cpu_baseline(s.points, tank, cpu_steps, instances)
+        cb["forward_ms_for_the_rollout_steps"] = cb["ms_per_step"] * steps
+        out["cpu_baseline"] = cb
+    return out
 
 
 def c1_leg(steps=100, cpu_steps=100):
@@ -677,7 +724,8 @@ def run_gb300(args, rank, world, D):
         if args.c1:
             line["c1"] = c1_leg(cpu_steps=100 if cpu else 0)
         if args.batched_states > 0:
-            line["batched"] = batched_vs_plain(args.batched_states, min(args.steps, 20), not args.no_autotune)
+            line["batched"] = batched_vs_plain(args.batched_states, min(args.steps, 20), not args.no_autotune,
+                                               cpu_steps=1 if cpu else 0)
         if args.sph:
             line["sph"] = sph_leg(min(args.steps, 20), not args.no_autotune, cpu_steps=2 if cpu else 0)
         if args.adjoint:
@@ -685,7 +733,7 @@ def run_gb300(args, rank, world, D):
             for i, keep in enumerate(int(k) for k in args.adjoint_keeps.split(",") if k.strip()):
                 name = "adjoint_record_all" if keep == 0 else ("adjoint" if i == 0 else f"adjoint_keep{keep}")
                 line[name] = adjoint_leg(steps=args.adjoint_steps, every=0 if keep == 0 else 20, keep=max(keep, 1),
-                                         tune=tune)
+                                         tune=tune, cpu_steps=2 if cpu and i == 0 else 0)
         if args.features:
             line["features"] = features_leg(setup, recs, line["tuning"])
         if cpu:

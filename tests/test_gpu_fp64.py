@@ -96,3 +96,19 @@ def test_sph_vs_fp64(gpu, port):
         o32 = oracle_run(port, O.MODEL_SPH, setup, recs, steps)
         o64 = oracle_run(port, O.MODEL_SPH, setup, recs, steps, real=np.float64)
         _check(f"SPH 8192 particles, {steps} steps", fields, _xyz(g, fields), _xyz(o32, fields), _xyz(o64, fields), tol)
+
+
+def test_full_size_boids_steps_vs_fp64(gpu, port):
+    """The benchmark's 1,048,576 boids, 5 see+act steps at the default tuning, against the FP32
+    oracle (CpuZGrid), its FP64 build and CpuGrid (another FP32 summation order; 2048 MB, since
+    the reference's CpuGrid cannot hold this grid in 256 MB), bounded as the 100k case is."""
+    ps = W.boids_points(1 << 20, seed=2)
+    recs = M.records(M.BOIDS_RECORD, ps.p, ps.v)
+    full = M.boids_setup(mb=256)
+    g = M.run(full, recs, 5)
+    o32 = oracle_run(port, O.MODEL_BOIDS, full, recs, 5)
+    o64 = oracle_run(port, O.MODEL_BOIDS, full, recs, 5, real=np.float64)
+    grid = M.boids_setup(mb=2048)
+    og = oracle_run(port, O.MODEL_BOIDS, grid, recs, 5, space="grid")
+    f = ("p", "v")
+    _check("boids 1M, 5 steps", f, _xyz(g, f), _xyz(o32, f), _xyz(o64, f), 1e-3, _xyz(og, f))
