@@ -140,6 +140,8 @@ struct SeeOnly {
     static constexpr int kSeenF4 = 2;
     static constexpr int kLaneUnroll = 4;
     static constexpr bool kKeepGate = true;
+    static constexpr bool kKeepRejectsSelf = true;  // 0 < d2
+    static constexpr bool kSeenMinusSeer = true;    // d = b - a
     TGPU_D static bool keep(const float4 &a, const float4 &b, const Ctx &c) { return keep_fn(a, b, c); }
     TGPU_D static int seen_stream(int k) { return k == 0 ? POS : VEL; }
     TGPU_D static void load(Seer &s, const PassIO &, uint32_t, const Ctx &, const Ctx &) { zero(s); }
@@ -162,6 +164,8 @@ struct SeeAct {
     static constexpr int kSeenF4 = 2;
     static constexpr int kLaneUnroll = 4;
     static constexpr bool kKeepGate = true;
+    static constexpr bool kKeepRejectsSelf = true;  // 0 < d2
+    static constexpr bool kSeenMinusSeer = true;    // d = b - a
     TGPU_D static bool keep(const float4 &a, const float4 &b, const Ctx &c) { return keep_fn(a, b, c); }
     TGPU_D static int seen_stream(int k) { return k == 0 ? POS : VEL; }
     TGPU_D static void load(Seer &s, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {

@@ -96,6 +96,8 @@ struct Density {
     // records the pairs inside the support for the force pass that follows (positions do
     // not change between the two)
     static constexpr int kPairList = 1;
+    // the see body runs only for pairs inside the support (keep), the particle itself included
+    static constexpr bool kKeepGate = true;
     TGPU_D static int seen_stream(int) { return POS; }
     TGPU_D static bool keep(const float4 &a, const float4 &b, const Ctx &c) {
         return dist2(a.x - b.x, a.y - b.y, a.z - b.z) < c.support2;
@@ -136,6 +138,13 @@ struct Force {
     // wider here; for the other candidates the see function does nothing
     static constexpr int kPairList = 2;
     TGPU_D static bool replay_ok(const Ctx &mine, const Ctx &rec) { return mine.support2 <= rec.support2; }
+    // when it walks: the see body runs only for 0 < r2 < support2
+    static constexpr bool kKeepGate = true;
+    static constexpr bool kKeepRejectsSelf = true;
+    TGPU_D static bool keep(const float4 &a, const float4 &b, const Ctx &c) {
+        const float r2 = dist2(a.x - b.x, a.y - b.y, a.z - b.z);
+        return r2 < c.support2 && r2 > 0.0f;
+    }
     TGPU_D static int seen_stream(int k) { return k == 0 ? POS : (k == 1 ? VEL : RP); }
     TGPU_D static void load(Seer &s, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {
         s.ax = s.ay = s.az = 0.0f;
@@ -309,6 +318,7 @@ struct ForceAdj {
     static constexpr int kSeenF4 = 4;
     // records the step's pairs inside the support for the density adjoint that follows
     static constexpr int kPairList = 1;
+    static constexpr bool kKeepGate = true;
     TGPU_D static bool keep(const float4 &a, const float4 &b, const Ctx &c) {
         return dist2(a.x - b.x, a.y - b.y, a.z - b.z) < c.support2;
     }
@@ -412,6 +422,13 @@ struct DensityAdj {
     // replays the force adjoint's list (same pairs: r2 < support2, r2 > 0)
     static constexpr int kPairList = 2;
     TGPU_D static bool replay_ok(const Ctx &mine, const Ctx &rec) { return mine.support2 <= rec.support2; }
+    // when it walks: the see body runs only for 0 < r2 < support2
+    static constexpr bool kKeepGate = true;
+    static constexpr bool kKeepRejectsSelf = true;
+    TGPU_D static bool keep(const float4 &a, const float4 &b, const Ctx &c) {
+        const float r2 = dist2(a.x - b.x, a.y - b.y, a.z - b.z);
+        return r2 < c.support2 && r2 > 0.0f;
+    }
     TGPU_D static int seen_stream(int k) { return k == 0 ? A_POS : A_RHOBAR; }
     TGPU_D static void load(Seer &s, const PassIO &io, uint32_t i, const Ctx &, const Ctx &) {
         s.rhob = io.in_f4[A_RHOBAR][i].x;

@@ -188,10 +188,11 @@ struct UnrollOf<P, decltype((void)P::kLaneUnroll)> {
 // independent loads in flight; a recording pass passes its recorder as `rec`.
 // Whether pass P gates its see body on its keep test (P::kKeepGate): the see function
 // does nothing for a pair that passed the box test but not P::keep, so the walk counts the
-// box-test pass without a branch and enters the body only for kept pairs.  keep(a, a) must
-// be false (a seer never keeps itself, as for a distance test with d2 > 0): the gated walk
-// then tests the seer like any candidate and takes its one box-test pass off the counter
-// at the end, instead of comparing every index with the seer's.
+// box-test pass without a branch and enters the body (and the recorder) only for kept
+// pairs.  The gated walk tests the seer like any other candidate (it lies in its own range
+// and is met exactly once) and takes its box-test pass off the counter at the end when the
+// pass skips self.  When keep(a, a) is false (P::kKeepRejectsSelf: a distance test with
+// d2 > 0) no index is compared with the seer's; otherwise only kept candidates are.
 template <class P, class = void>
 struct GateOf {
     static constexpr bool value = false;
@@ -200,6 +201,32 @@ template <class P>
 struct GateOf<P, decltype((void)P::kKeepGate)> {
     static constexpr bool value = P::kKeepGate;
 };
+template <class P, class = void>
+struct SelfSafeOf {
+    static constexpr bool value = false;
+};
+template <class P>
+struct SelfSafeOf<P, decltype((void)P::kKeepRejectsSelf)> {
+    static constexpr bool value = P::kKeepRejectsSelf;
+};
+
+// The direction of the difference a gated pass's keep and see functions compute: seen -
+// seer when P::kSeenMinusSeer (boids), else seer - seen (the reference's d); the gated box
+// test computes the same one (|d| is the same float either way), so the compiler shares it.
+template <class P, class = void>
+struct SeenMinusSeerOf {
+    static constexpr bool value = false;
+};
+template <class P>
+struct SeenMinusSeerOf<P, decltype((void)P::kSeenMinusSeer)> {
+    static constexpr bool value = P::kSeenMinusSeer;
+};
+
+// A kept candidate into the recorder's list (the gated walk counts box-test passes itself).
+TGPU_D void record_kept(ListRec &r, uint32_t j) {
+    if (r.n < r.cap) reinterpret_cast<uint32_t *>(r.idx)[((size_t)(r.n >> 2) * r.stride + r.seer) * 4u + (r.n & 3u)] = j;
+    ++r.n;
+}
 
 // One candidate of a lane's walk: the reference's box test and self skip, the pair
 // counter, the recorder, and the see function (behind P::keep when the pass gates on it).
@@ -207,12 +234,19 @@ template <class P, bool kGate, class Acc, class Rec>
 TGPU_D void lane_one(typename P::Seer &s, const float4 &sp, const float4 &b, const float4 &r4, uint32_t j,
                      uint32_t self, const Acc &acc, const typename P::SeeCtx &sctx, uint32_t &pairs, Rec *rec) {
     constexpr bool kRec = std::is_same_v<Rec, ListRec>;
-    if constexpr (kGate && !kRec) {
-        // the reference's test on d = seer - seen; |seen - seer| is the same float, and the
-        // model's keep and see compute seen - seer, which the compiler then shares
-        const bool hit = !(fabsf(b.x - sp.x) > r4.x) && !(fabsf(b.y - sp.y) > r4.y) && !(fabsf(b.z - sp.z) > r4.z);
+    if constexpr (kGate) {
+        // the reference's test on d = seer - seen, computed in the direction the model's keep
+        // and see use (|seen - seer| is the same float), so the compiler shares it
+        bool hit;
+        if constexpr (SeenMinusSeerOf<P>::value)
+            hit = !(fabsf(b.x - sp.x) > r4.x) && !(fabsf(b.y - sp.y) > r4.y) && !(fabsf(b.z - sp.z) > r4.z);
+        else
+            hit = !(fabsf(sp.x - b.x) > r4.x) && !(fabsf(sp.y - b.y) > r4.y) && !(fabsf(sp.z - b.z) > r4.z);
         pairs += hit ? 1u : 0u;
-        if (hit && P::keep(sp, b, sctx)) P::see(s, sp, b, acc, j, sctx);
+        if (hit && (SelfSafeOf<P>::value || j != self) && P::keep(sp, b, sctx)) {
+            if constexpr (kRec) record_kept(*rec, j);
+            P::see(s, sp, b, acc, j, sctx);
+        }
     } else {
         if (j != self && box_hit(sp, b, r4)) {
             ++pairs;
@@ -851,12 +885,20 @@ __global__ void __launch_bounds__(kSeeThreads, kStage ? 1 : 8) see_rows_kernel(S
                 // plain walks it costs the non-recording kernels registers)
                 if (active) {
                     ListRec rec{L.plist.idx, L.plist.stride, L.plist.cap, i, 0u, 0u};
+                    const uint32_t before = pairs;
                     for (int z = lo[2]; z <= hi[2]; ++z)
                         for (int y = lo[1]; y <= hi[1]; ++y) {
                             const uint2 jr =
                                 row_range(words, hdr, (uint32_t)z * dy0 + (uint32_t)y, dx0, lo[0], hi[0]);
-                            lane_run<P>(s, sp, r4, jr.x, jr.y, self, pos, acc, sctx, pairs, tested, &rec);
+                            lane_run<P, decltype(acc), ListRec, GateOf<P>::value>(s, sp, r4, jr.x, jr.y, self, pos,
+                                                                                   acc, sctx, pairs, tested, &rec);
                         }
+                    if constexpr (GateOf<P>::value) {
+                        // the gated walk counted the seer's own box-test pass (met once)
+                        const uint32_t own = box_hit(sp, sp, r4) ? 1u : 0u;
+                        rec.other = pairs - before - own;
+                        if (L.skip_self) pairs -= own;
+                    }
                     L.plist.count[i] = make_uint2(rec.n, rec.other);
                 }
                 walked = true;
@@ -892,7 +934,7 @@ __global__ void __launch_bounds__(kSeeThreads, kStage ? 1 : 8) see_rows_kernel(S
             // the gated walk tested the seer too (it lies in its own range): its box-test
             // pass comes off the counter when the pass skips self
             if constexpr (GateOf<P>::value && !kBox)
-                if (self != 0xFFFFFFFFu && box_hit(sp, sp, r4)) --pairs;
+                if (L.skip_self && box_hit(sp, sp, r4)) --pairs;
         }
     } else if (recording && active) {
         L.plist.count[i] = make_uint2(0u, 0u);  // no cell to walk: an empty, complete list
