@@ -343,7 +343,7 @@ def adjoint_cpu_baseline(points, tank, steps=2, instances=32):
                      threads=threads, mb=setup.mb)
     batch_ms = r.ms_per_step * instances
     return {"value": r.pairs / (r.ms_per_step * steps / 1000.0), "unit": "pair-interactions/s", "cores": threads,
-            "kind": "port", "ms_per_step": batch_ms, "forward_ms_for_the_rollout_steps": None,
+            "kind": "port", "ms_per_step": batch_ms,
             "sample": f"{steps} forward steps of one {points.n}-particle instance on CpuZGrid (oracle restatement, "
                       f"{threads} threads); ms_per_step is that of the {instances} instances one after another"}
 

@@ -101,10 +101,10 @@ def build(verbose: bool = False, ptxas_verbose: bool = False, jobs: int = 0) -> 
     return LIB
 
 
-def build_model(src: str, out: str, verbose: bool = False) -> str:
+def build_model(src: str, out: str, verbose: bool = False, defines=()) -> str:
     """Compiles a host's own device model (a .cu written against include/tay_gpu_model.cuh)
     into the shared library `out`, for tgpu_register_model_library.  Rebuilt only when the
-    source or the engine's headers are newer."""
+    source or the engine's headers are newer.  `defines`: extra -D options."""
     gpu = os.path.join(CSRC, "gpu")
     deps = [src] + [os.path.join(gpu, f) for f in os.listdir(gpu) if f.endswith(".cuh")]
     deps += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
@@ -112,7 +112,8 @@ def build_model(src: str, out: str, verbose: bool = False) -> str:
         return out
     os.makedirs(os.path.dirname(os.path.abspath(out)), exist_ok=True)
     _run([nvcc_path(), "-gencode", GENCODE, "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
-          "-Xcompiler", "-fPIC", "-shared", "--cudart", "shared", "-I", INCLUDE, "-I", gpu, src, "-o", out], verbose)
+          "-Xcompiler", "-fPIC", "-shared", "--cudart", "shared", "-I", INCLUDE, "-I", gpu] +
+         ["-D" + d for d in defines] + [src, "-o", out], verbose)
     return out
 
 

@@ -70,6 +70,18 @@ def test_model_library_registers(soft_model):
         api.register_model_library(api.LIB_PATH)
 
 
+def test_model_library_func_name_clash_refused(built):
+    """The same model built to claim boids_see, a func name of the library's boids model: the
+    registration is refused and names both models; boids_see still selects boids."""
+    from tay_gb300 import _build
+
+    out = os.path.join(HERE, "models", "_build", "libtaymodel_soft_clash.so")
+    _build.build_model(SRC, out, defines=('SOFT_SEE_NAME="boids_see"',))
+    with pytest.raises(api.TayError, match="boids_see.*already provided by model 'boids'"):
+        api.register_model_library(out)
+    assert api.lib().tgpu_model_of(b"boids_see") == b"boids"
+
+
 def _setup(passes):
     ctx = _ctx()
     lst = [M.Pass(p, p == "soft_see", ctx, R, False) for p in passes]
