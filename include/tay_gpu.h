@@ -219,7 +219,11 @@ void tgpu_get_tuning(TgpuTuning *tuning);
  *                         the record's id field), returns dL/d(initial positions),
  *                         dL/d(initial velocities) in the same layout and dL/d(alpha, c0)
  *                         per group (2 doubles per group).  Neighbour sets are held fixed
- *                         within each step.  Any output pointer may be NULL. */
+ *                         within each step.  Any output pointer may be NULL.  When it
+ *                         recomputed a segment, the recomputation was recorded over the
+ *                         forward run's records, and the next backward needs another
+ *                         tgpu_adjoint_forward (it returns TGPU_ERR_ARG until then); with
+ *                         every step recorded, or every segment kept, it may run again. */
 typedef struct TgpuAdjoint TgpuAdjoint;
 int tgpu_adjoint_create(TgpuBatch *batch, int steps, int checkpoint_every, int keep_segments, TgpuAdjoint **out);
 int tgpu_adjoint_forward(TgpuAdjoint *adjoint);

@@ -451,6 +451,9 @@ int tgpu_adjoint_backward(TgpuAdjoint *a, const float *dl_dpos, const float *dl_
             for (int s = len - 1; s >= 0; --s) backward_step(a, a->rec[base + s], lists ? &a->lists[s] : nullptr);
         }
         restore_checkpoint(b, a->cp.back());  // the batch ends where the forward run ended
+        // a recomputed segment was recorded over the first kept segment's records (and its
+        // lists over the last segment's): another backward needs another forward run
+        if (first_kept > 0) a->recorded = false;
     }
     cudaEventRecord(a->e1, st);
     if (dpos0) cudaMemcpyAsync(dpos0, a->xbar_id, n * sizeof(float4), cudaMemcpyDeviceToHost, st);

@@ -719,15 +719,20 @@ int tgpu_register_model(const void *desc, unsigned abi) {
 
 int tgpu_register_model_library(const char *path) {
     if (!path) return fail(TGPU_ERR_ARG, "tgpu_register_model_library: null path");
-    // kept loaded for the life of the process: the registry points into it
+    // kept loaded for the life of the process once registered: the registry points into it
     void *h = dlopen(path, RTLD_NOW | RTLD_LOCAL);
     if (!h) return fail(TGPU_ERR_ARG, "tgpu_register_model_library: %s", dlerror());
     using Entry = const void *(*)(unsigned *);
     Entry entry = reinterpret_cast<Entry>(dlsym(h, "tgpu_model_entry"));
-    if (!entry) return fail(TGPU_ERR_ARG, "tgpu_register_model_library: %s exports no tgpu_model_entry", path);
+    if (!entry) {
+        dlclose(h);
+        return fail(TGPU_ERR_ARG, "tgpu_register_model_library: %s exports no tgpu_model_entry", path);
+    }
     unsigned abi = 0;
     const void *desc = entry(&abi);
-    return tgpu_register_model(desc, abi);
+    const int rc = tgpu_register_model(desc, abi);
+    if (rc != TGPU_OK) dlclose(h);  // nothing of it was kept
+    return rc;
 }
 
 const char *tgpu_model_of(const char *func_name) {

@@ -187,3 +187,29 @@ def test_fit_viscosity_and_sound_speed_to_a_target_rollout(gpu):
     assert min(losses[-5:]) < 0.1 * losses[0], losses
     assert np.all(np.abs(roll.params[:, 0] - 0.08) < 0.012), roll.params
     assert np.all(np.abs(roll.params[:, 1] - 22.0) < 2.0), roll.params
+
+
+def test_second_backward_needs_a_forward(gpu_grads):
+    """A checkpointed backward that recomputed a segment recorded it over the forward run's
+    records: a second backward is refused until the next forward; with every step recorded
+    the backward can run again and gives the same gradients."""
+    from tay_gb300 import api
+
+    roll = SphRollout(_instances(), STEPS, checkpoint_every=10, keep_segments=1)
+    x, _ = roll.forward()
+    g = _dl_dx(x, gpu_grads["target"], roll)
+    first = roll.backward(g)
+    with pytest.raises(api.TayError, match="tgpu_adjoint_forward first"):
+        roll.backward(g)
+    roll.forward()
+    again = roll.backward(g)
+    for a, b in zip(first, again):
+        assert np.array_equal(a, b)
+    roll.close()
+    roll = SphRollout(_instances(), STEPS, checkpoint_every=0)
+    x, _ = roll.forward()
+    first = roll.backward(g)
+    again = roll.backward(g)
+    for a, b in zip(first, again):
+        assert np.array_equal(a, b)
+    roll.close()
