@@ -184,8 +184,6 @@ struct UnrollOf<P, decltype((void)P::kLaneUnroll)> {
     static constexpr int value = P::kLaneUnroll;
 };
 
-// Per-lane walk over candidates [j0, j1): UnrollOf<P> candidates per iteration for
-// independent loads in flight; a recording pass passes its recorder as `rec`.
 // Whether pass P gates its see body on its keep test (P::kKeepGate): the see function
 // does nothing for a pair that passed the box test but not P::keep, so the walk counts the
 // box-test pass without a branch and enters the body (and the recorder) only for kept
@@ -256,6 +254,9 @@ TGPU_D void lane_one(typename P::Seer &s, const float4 &sp, const float4 &b, con
     }
 }
 
+// Per-lane walk over candidates [j0, j1): UnrollOf<P> candidates per iteration for
+// independent loads in flight; a recording pass passes its recorder as `rec`; kGate: the
+// keep-gated candidate step (GateOf).
 template <class P, class Acc, class Rec = NoRec, bool kGate = false>
 TGPU_D void lane_run(typename P::Seer &s, const float4 &sp, const float4 &r4, uint32_t j0, uint32_t j1, uint32_t self,
                      const float4 *src, const Acc &acc, const typename P::SeeCtx &sctx, uint32_t &pairs,
