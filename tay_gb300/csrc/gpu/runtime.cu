@@ -705,14 +705,21 @@ int tgpu_register_model(const void *desc, unsigned abi) {
                 return fail(TGPU_ERR_ARG, "model '%s': program %d uses kernel %d of %d", m->name, p,
                             pr.kernel_index[q], m->nkernels);
     }
-    // a func name selects exactly one model
-    for (int k = 0; k < m->nkernels; ++k)
-        for (const char *fn : {m->kernels[k].see, m->kernels[k].act})
-            if (fn)
-                if (const ModelDesc *other = find_model(fn))
-                    return fail(TGPU_ERR_ARG, "model '%s': func '%s' is already provided by model '%s'", m->name, fn,
-                                other->name);
+    // a func name selects exactly one model (checked and added under one lock, so two
+    // registrations of the same name cannot both pass)
     std::lock_guard<std::mutex> guard(g_models_lock);
+    for (int k = 0; k < m->nkernels; ++k)
+        for (const char *fn : {m->kernels[k].see, m->kernels[k].act}) {
+            if (!fn) continue;
+            const ModelDesc *other = nullptr;
+            for (int i = 0; i < 4 && !other; ++i)
+                if (model_has_func(model_list(i), fn)) other = model_list(i);
+            for (size_t i = 0; i < g_registered.size() && !other; ++i)
+                if (model_has_func(g_registered[i], fn)) other = g_registered[i];
+            if (other)
+                return fail(TGPU_ERR_ARG, "model '%s': func '%s' is already provided by model '%s'", m->name, fn,
+                            other->name);
+        }
     g_registered.push_back(m);
     return TGPU_OK;
 }
