@@ -135,11 +135,10 @@ void free_batch(TgpuBatch *b) {
         cudaFree(b->vals[k]);
     }
     cudaFree(b->sort_scratch);
-    cudaFree(b->d_err);
+    cudaFree(b->d_status);  // also the error word, the pair counter and the telemetry
+    cudaFreeHost(b->h_status);
     cudaFree(b->table);
     cudaFree(b->d_aos);
-    cudaFree(b->d_pairs);
-    cudaFree(b->d_telemetry);
     cudaFree(b->plist_idx);
     cudaFree(b->plist_count);
     for (auto &r : b->runs) {
@@ -210,7 +209,18 @@ void *pinned_device_ptr(const void *host) {
 int upload_contexts(TgpuBatch *b, int seg) {
     std::vector<char> buf(b->ctx_stride);
     const HostSeg &h = b->hs[seg];
-    for (auto &r : b->runs) {
+    if (b->ctx_shadow.size() != b->runs.size() * 3 * (size_t)b->nseg) b->ctx_shadow.assign(b->runs.size() * 3 * b->nseg, {});
+    bool copied = false;
+    // uploads `bytes` to `dst` unless they equal what the last upload to that slot sent
+    auto upload = [&](size_t slot, void *dst, const void *src, size_t bytes) -> cudaError_t {
+        std::string &shadow = b->ctx_shadow[slot * b->nseg + seg];
+        if (shadow.size() == bytes && !memcmp(shadow.data(), src, bytes)) return cudaSuccess;
+        shadow.assign(static_cast<const char *>(src), bytes);
+        copied = true;
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, b->st);
+    };
+    for (size_t k = 0; k < b->runs.size(); ++k) {
+        const KernelRun &r = b->runs[k];
         for (int which = 0; which < 2; ++which) {
             int p = which == 0 ? r.see_pass : r.act_pass;
             char *dst = which == 0 ? r.d_see_ctx : r.d_act_ctx;
@@ -219,16 +229,15 @@ int upload_contexts(TgpuBatch *b, int seg) {
             const TgpuPass &tp = h.passes[p];
             if (tp.context && tp.context_size)
                 memcpy(buf.data(), tp.context, std::min((size_t)tp.context_size, b->ctx_stride));
-            CK(cudaMemcpyAsync(dst + (size_t)seg * b->ctx_stride, buf.data(), b->ctx_stride, cudaMemcpyHostToDevice,
-                               b->st));
+            CK(upload(3 * k + (size_t)which, dst + (size_t)seg * b->ctx_stride, buf.data(), b->ctx_stride));
         }
         if (r.see_pass >= 0) {
             const TgpuPass &tp = h.passes[r.see_pass];
             float4 rr = pass_radii(tp, seg_dims(b->specs[seg]));
-            CK(cudaMemcpyAsync(r.d_radii + seg, &rr, sizeof(float4), cudaMemcpyHostToDevice, b->st));
+            CK(upload(3 * k + 2, r.d_radii + seg, &rr, sizeof(float4)));
         }
     }
-    CK(cudaStreamSynchronize(b->st));
+    if (copied) CK(cudaStreamSynchronize(b->st));
     return TGPU_OK;
 }
 
@@ -861,11 +870,14 @@ int alloc_batch(TgpuBatch *b) {
         CKR(cudaMalloc(&b->vals[k], sizeof(uint32_t) * n));
     }
     CKR(cudaMalloc(&b->sort_scratch, sort_scratch_bytes((uint32_t)b->nseg, std::max<uint32_t>(b->tiles, 1))));
-    CKR(cudaMalloc(&b->d_err, sizeof(uint32_t)));
-    CKR(cudaMemset(b->d_err, 0, sizeof(uint32_t)));
+    // status block: [0] pair counter, [1..8] telemetry, [9] the device error word (low half)
+    CKR(cudaMalloc(&b->d_status, sizeof(unsigned long long) * kStatusWords));
+    CKR(cudaMemset(b->d_status, 0, sizeof(unsigned long long) * kStatusWords));
+    CKR(cudaMallocHost(&b->h_status, sizeof(unsigned long long) * kStatusWords));
+    b->d_pairs = b->d_status;
+    b->d_telemetry = b->d_status + 1;
+    b->d_err = reinterpret_cast<uint32_t *>(b->d_status + 9);
     CKR(cudaMalloc(&b->d_aos, (size_t)m->agent_bytes * n));
-    CKR(cudaMalloc(&b->d_pairs, sizeof(unsigned long long)));
-    CKR(cudaMalloc(&b->d_telemetry, sizeof(unsigned long long) * 8));
     b->ctx_stride = (std::max(m->see_ctx_bytes, m->act_ctx_bytes) + 15u) & ~15u;
     return TGPU_OK;
 }
@@ -1163,8 +1175,7 @@ int tgpu_batch_enqueue(TgpuBatch *b, int steps) {
     if (!b || steps < 0) return fail(TGPU_ERR_ARG, "bad run");
     int rc = prepare_specs(b);
     if (rc) return rc;
-    CK(cudaMemsetAsync(b->d_pairs, 0, sizeof(unsigned long long), b->st));
-    CK(cudaMemsetAsync(b->d_telemetry, 0, sizeof(unsigned long long) * 8, b->st));
+    CK(cudaMemsetAsync(b->d_status, 0, sizeof(unsigned long long) * 9, b->st));  // pairs, telemetry
     bool any_wt = false;
     for (int s = 0; s < b->nseg; ++s) {
         b->wt_done[s] = 0;
@@ -1196,6 +1207,9 @@ int tgpu_batch_enqueue(TgpuBatch *b, int steps) {
         CK(cudaGraphLaunch(exec, b->st));
     }
     CK(cudaEventRecord(b->e1, b->st));
+    // the run's status (pairs, telemetry, error word) comes back with the run
+    CK(cudaMemcpyAsync(b->h_status, b->d_status, sizeof(unsigned long long) * kStatusWords, cudaMemcpyDeviceToHost,
+                       b->st));
     CK(cudaGetLastError());
     if (any_wt && steps > 0)
         for (int s = 0; s < b->nseg; ++s) b->wt_done[s] = b->wt_dev[s] != nullptr;
@@ -1227,9 +1241,10 @@ int tgpu_batch_sync(TgpuBatch *b) {
     float ms = 0.0f;
     CK(cudaEventElapsedTime(&ms, b->e0, b->e1));
     b->last_ms = ms;
-    CK(cudaMemcpy(&b->last_pairs, b->d_pairs, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(b->last_telemetry, b->d_telemetry, sizeof(b->last_telemetry), cudaMemcpyDeviceToHost));
-    return check_device_error(b);
+    b->last_pairs = b->h_status[0];
+    for (int k = 0; k < 8; ++k) b->last_telemetry[k] = b->h_status[1 + k];
+    if (!(uint32_t)b->h_status[9]) return TGPU_OK;
+    return check_device_error(b);  // reads and clears the word, and reports it
 }
 
 int tgpu_batch_run(TgpuBatch *b, int steps) {

@@ -2,12 +2,17 @@
 #pragma once
 
 #include <map>
+#include <string>
 #include <vector>
 
 #include "model.cuh"
 #include "tay_gpu.h"
 
 namespace tgpu {
+
+// 64-bit words of a batch's status block: the pair counter, 8 telemetry counters, the
+// device error word.
+constexpr int kStatusWords = 10;
 
 struct KernelRun {
     const KernelDesc *k;
@@ -74,8 +79,14 @@ struct TgpuBatch {
     uint2 *table = nullptr;
     size_t table_entries = 0;
     uint32_t *d_aos = nullptr;
-    unsigned long long *d_pairs = nullptr;
-    unsigned long long *d_telemetry = nullptr;  // kTelemetry counters, summed over a run
+    // one device block for the run's status (pair counter, telemetry, error word), read back
+    // by one copy into page-locked h_status at the end of every run
+    unsigned long long *d_status = nullptr, *h_status = nullptr;
+    unsigned long long *d_pairs = nullptr;      // d_status[0]
+    unsigned long long *d_telemetry = nullptr;  // d_status[1..8]: kTelemetry counters, summed over a run
+    // the context and radii bytes last uploaded per (run, see context / act context / radii,
+    // segment): a run uploads only what the host changed
+    std::vector<std::string> ctx_shadow;
     unsigned long long last_telemetry[8] = {};
     size_t ctx_stride = 0;
     std::vector<KernelRun> runs;
