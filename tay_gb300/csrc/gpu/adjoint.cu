@@ -192,7 +192,6 @@ void recorded_step(TgpuAdjoint *a, Record *r, const StepList *pl = nullptr) {
     launch_box(L, st);
     uint32_t *skeys = nullptr, *perm = nullptr;
     launch_sort(L, st, &skeys, &perm);
-    launch_cell_table(L, skeys, 1, st);
     GatherSet g{};
     for (int c = 0; c < b->m->nf4; ++c) {
         if (b->m->role_f4[c] != kState) continue;
@@ -207,7 +206,7 @@ void recorded_step(TgpuAdjoint *a, Record *r, const StepList *pl = nullptr) {
         b->cur_u32[c] ^= 1;
         ++g.nu32;
     }
-    launch_gather(b->total, perm, g, st);
+    launch_cell_table(L, skeys, 1, st, perm, &g);  // and the reorder into cell order
     // density + pressure (recording the batch's pair list, when it keeps one)
     const KernelRun &rd = b->runs[0];
     SeeLaunch SD = see_launch(b, rd, make_io(b, rd.k, true, 0));

@@ -180,13 +180,12 @@ extern "C" int tgpu_see_noalloc(const float *positions, unsigned n, const float 
     launch_box(L, st);
     uint32_t *skeys = nullptr, *perm = nullptr;
     launch_sort(L, st, &skeys, &perm);
-    launch_cell_table(L, skeys, 1, st);
     float4 *pos_sorted = reinterpret_cast<float4 *>(scratch + kOffPos);
     GatherSet gs{};
     gs.src_f4[0] = L.pos;
     gs.dst_f4[0] = pos_sorted;
     gs.nf4 = 1;
-    launch_gather(n, perm, gs, st);
+    launch_cell_table(L, skeys, 1, st, perm, &gs);  // and the positions into cell order
 
     // the test model's see pass (agent_see alone): accumulators into the acc array
     const KernelDesc &k = model_test_basic()->kernels[0];

@@ -303,8 +303,12 @@ int tgpu::prepare_specs(TgpuBatch *b) {
     CK(cudaMemcpyAsync(b->d_specs, b->specs.data(), sizeof(SegmentSpec) * b->nseg, cudaMemcpyHostToDevice, b->st));
     for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
     b->graphs.clear();
+    // box reset, bounding box (+ grids), keys and histograms (+ digit offsets), one kernel
+    // per radix pass, cell table (+ reorder), the passes, and the table clear when it is
+    // a kernel (Morton order, or more segments than separate header memsets)
     const int passes = sort_passes(b->key_bits);
-    b->launches_per_step = 2 + passes * 5 + 1 + 1 + (int)b->runs.size() + 1;
+    const bool clear_kernel = b->cell_order != kOrderRows || b->nseg > kMemsetClearSegments;
+    b->launches_per_step = 2 + 1 + passes + 1 + (int)b->runs.size() + (clear_kernel ? 1 : 0);
     return TGPU_OK;
 }
 
@@ -353,9 +357,6 @@ SortLaunch tgpu::sort_launch(TgpuBatch *b) {
 }
 
 namespace {
-
-// Segments up to which a row-order step clears its table with one memset per segment.
-constexpr int kMemsetClearSegments = 4;
 
 void mark(const StepEvents *e, int k, cudaStream_t st) {
     if (e) cudaEventRecord(e->ev[k], st);
@@ -413,10 +414,6 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E, bool write_through) {
     mark(E, 2, st);
     launch_sort(L, st, &skeys, &perm);
     mark(E, 3, st);
-    mark(E, 4, st);
-    launch_cell_table(L, skeys, 1, st);
-    mark(E, 5, st);
-
     GatherSet g{};
     for (int c = 0; c < b->m->nf4; ++c) {
         if (b->m->role_f4[c] != kState) continue;
@@ -432,8 +429,11 @@ void tgpu::enqueue_step(TgpuBatch *b, const StepEvents *E, bool write_through) {
         b->cur_u32[c] ^= 1;
         ++g.nu32;
     }
+    // the cell table and the reorder into cell order, one launch
+    mark(E, 4, st);
+    launch_cell_table(L, skeys, 1, st, perm, &g);
+    mark(E, 5, st);
     mark(E, 6, st);
-    launch_gather(b->total, perm, g, st);
     mark(E, 7, st);
 
     int kidx = 0;

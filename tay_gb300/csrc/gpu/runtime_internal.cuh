@@ -14,6 +14,9 @@ namespace tgpu {
 // device error word.
 constexpr int kStatusWords = 10;
 
+// Segments up to which a row-order step clears its table with one memset per segment.
+constexpr int kMemsetClearSegments = 4;
+
 struct KernelRun {
     const KernelDesc *k;
     int see_pass;  // index into the group's pass list, or -1

@@ -52,77 +52,116 @@ TGPU_D uint32_t warp_incl_scan(uint32_t v) {
 
 // ------------------------------------------------------------------ bounding box
 
+// Each segment's grid for this step from its box (or fixed box), with its rounding pad.
+TGPU_D void write_grid(const SegmentSpec &sp, const BoxAcc &b, SegGrid *grids, uint32_t seg) {
+    SegGrid out;
+    out.g = segment_grid(sp, b);
+    out.pad = grid_pad(out.g, sp, b);
+    grids[seg] = out;
+}
+
 // Bounding box of the positions (the min corners of non-point agents) per segment, and
 // for non-point agents (pos_max != nullptr) the largest box edge per axis, which widens
-// every seer's search over the seen agents' min corners.
+// every seer's search over the seen agents' min corners.  The segment's last block to
+// finish (a counter in `done`, zeroed by box_reset_kernel) then derives its grid.
 __global__ void __launch_bounds__(kSortThreads) bbox_kernel(const SegmentSpec *__restrict__ specs,
                                                             const uint32_t *__restrict__ tile_seg,
                                                             const float4 *__restrict__ pos,
-                                                            const float4 *__restrict__ pos_max, BoxAcc *box) {
+                                                            const float4 *__restrict__ pos_max, BoxAcc *box,
+                                                            SegGrid *__restrict__ grids, uint32_t *done) {
     const uint32_t seg = tile_seg[blockIdx.x];
     const SegmentSpec s = specs[seg];
-    if (s.fixed_box && !pos_max) return;
     const uint32_t t = blockIdx.x - s.tile_begin;
     const uint32_t beg = s.begin + t * kSortTile;
     const uint32_t end = min(beg + (uint32_t)kSortTile, s.begin + s.count);
-    uint32_t lo[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
-    uint32_t hi[3] = {0u, 0u, 0u};
-    uint32_t sz[3] = {0u, 0u, 0u};
+    __shared__ uint32_t red[6][kSortThreads / 32];
+    __shared__ bool s_last;
+    if (!s.fixed_box || pos_max) {
+        uint32_t lo[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+        uint32_t hi[3] = {0u, 0u, 0u};
+        uint32_t sz[3] = {0u, 0u, 0u};
 #pragma unroll
-    for (uint32_t k = 0; k < kSortTile / kSortThreads; ++k) {  // every load of the thread in flight
-        const uint32_t i = beg + k * kSortThreads + threadIdx.x;
-        if (i >= end) continue;
-        float4 p = pos[i];
-        float c[3] = {p.x, p.y, p.z};
-        for (int a = 0; a < 3; ++a) {
-            uint32_t o = float_to_ordered(c[a]);
-            lo[a] = min(lo[a], o);
-            hi[a] = max(hi[a], o);
+        for (uint32_t k = 0; k < kSortTile / kSortThreads; ++k) {  // every load of the thread in flight
+            const uint32_t i = beg + k * kSortThreads + threadIdx.x;
+            if (i >= end) continue;
+            float4 p = pos[i];
+            float c[3] = {p.x, p.y, p.z};
+            for (int a = 0; a < 3; ++a) {
+                uint32_t o = float_to_ordered(c[a]);
+                lo[a] = min(lo[a], o);
+                hi[a] = max(hi[a], o);
+            }
+            if (pos_max) {
+                const float4 q = pos_max[i];
+                const float d[3] = {q.x - p.x, q.y - p.y, q.z - p.z};
+                for (int a = 0; a < 3; ++a) sz[a] = max(sz[a], float_to_ordered(fmaxf(d[a], 0.0f)));
+            }
         }
         if (pos_max) {
-            const float4 q = pos_max[i];
-            const float d[3] = {q.x - p.x, q.y - p.y, q.z - p.z};
-            for (int a = 0; a < 3; ++a) sz[a] = max(sz[a], float_to_ordered(fmaxf(d[a], 0.0f)));
+            for (int a = 0; a < 3; ++a) {
+                const uint32_t v = warp_max(sz[a]);
+                if (lane_id() == 0 && v) atomicMax(&box[seg].size[a], v);
+            }
         }
-    }
-    if (pos_max) {
-        for (int a = 0; a < 3; ++a) {
-            const uint32_t v = warp_max(sz[a]);
-            if (lane_id() == 0 && v) atomicMax(&box[seg].size[a], v);
-        }
-        if (s.fixed_box) return;
-    }
-    __shared__ uint32_t red[6][kSortThreads / 32];
-    for (int a = 0; a < 3; ++a) {
-        uint32_t l = warp_min(lo[a]);
-        uint32_t h = warp_max(hi[a]);
-        if (lane_id() == 0) {
-            red[a][threadIdx.x >> 5] = l;
-            red[3 + a][threadIdx.x >> 5] = h;
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        for (int a = 0; a < 3; ++a) {
-            uint32_t l = threadIdx.x < kSortThreads / 32 ? red[a][threadIdx.x] : 0xFFFFFFFFu;
-            uint32_t h = threadIdx.x < kSortThreads / 32 ? red[3 + a][threadIdx.x] : 0u;
-            l = warp_min(l);
-            h = warp_max(h);
-            if (threadIdx.x == 0) {
-                atomicMin(&box[seg].lo[a], l);
-                atomicMax(&box[seg].hi[a], h);
+        if (!s.fixed_box) {
+            for (int a = 0; a < 3; ++a) {
+                uint32_t l = warp_min(lo[a]);
+                uint32_t h = warp_max(hi[a]);
+                if (lane_id() == 0) {
+                    red[a][threadIdx.x >> 5] = l;
+                    red[3 + a][threadIdx.x >> 5] = h;
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x < 32) {
+                for (int a = 0; a < 3; ++a) {
+                    uint32_t l = threadIdx.x < kSortThreads / 32 ? red[a][threadIdx.x] : 0xFFFFFFFFu;
+                    uint32_t h = threadIdx.x < kSortThreads / 32 ? red[3 + a][threadIdx.x] : 0u;
+                    l = warp_min(l);
+                    h = warp_max(h);
+                    if (threadIdx.x == 0) {
+                        atomicMin(&box[seg].lo[a], l);
+                        atomicMax(&box[seg].hi[a], h);
+                    }
+                }
             }
         }
     }
+    // every thread's box updates ordered before the block counts itself done
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(done + seg, 1u) == s.tile_count - 1u;
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+        __threadfence();
+        BoxAcc b;
+        for (int a = 0; a < 3; ++a) {
+            b.lo[a] = __ldcg(&box[seg].lo[a]);
+            b.hi[a] = __ldcg(&box[seg].hi[a]);
+            b.size[a] = __ldcg(&box[seg].size[a]);
+        }
+        write_grid(s, b, grids, seg);
+    }
 }
 
-__global__ void box_reset_kernel(BoxAcc *box, uint32_t segments) {
+// Resets the box accumulators (and, with `done`, the bbox kernel's block counters); a
+// segment without agents gets its grid here, from the reset box, since no bbox block
+// runs for it.
+__global__ void box_reset_kernel(BoxAcc *box, uint32_t segments, const SegmentSpec *__restrict__ specs,
+                                 SegGrid *__restrict__ grids, uint32_t *done) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= segments) return;
+    BoxAcc b;
     for (int a = 0; a < 3; ++a) {
-        box[s].lo[a] = 0xFFFFFFFFu;
-        box[s].hi[a] = 0u;
-        box[s].size[a] = float_to_ordered(0.0f);
+        b.lo[a] = 0xFFFFFFFFu;
+        b.hi[a] = 0u;
+        b.size[a] = float_to_ordered(0.0f);
+    }
+    box[s] = b;
+    if (done) {
+        done[s] = 0u;
+        const SegmentSpec sp = specs[s];
+        if (sp.tile_count == 0) write_grid(sp, b, grids, s);
     }
 }
 
@@ -135,23 +174,54 @@ TGPU_D uint32_t count_index(const SegmentSpec &s, uint32_t digit, uint32_t local
     return 256u * s.tile_begin + digit * s.tile_count + local_tile;
 }
 
-// Each segment's grid for this step from its box (or fixed box), with its rounding pad:
-// one thread per segment.
+// Each segment's grid from its box as it stands (restored boxes of recorded steps): one
+// thread per segment.
 __global__ void grid_kernel(const SegmentSpec *__restrict__ specs, const BoxAcc *__restrict__ box,
                             SegGrid *__restrict__ grids, uint32_t segments) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= segments) return;
-    const SegmentSpec sp = specs[s];
-    const BoxAcc b = box[s];
-    SegGrid out;
-    out.g = segment_grid(sp, b);
-    out.pad = grid_pad(out.g, sp, b);
-    grids[s] = out;
+    write_grid(specs[s], box[s], grids, s);
 }
 
-// One pass over the positions: the grid from the box, the cell key of every agent, and
-// per-segment histograms of every D-bit digit of the keys (order-independent, so all
-// passes' digit offsets are known before the first scatter).  hist layout:
+// One segment's histograms become each digit's first output slot (the segment's begin
+// plus the exclusive prefix over digits), pass by pass; run by one block of kSortThreads
+// threads, each owning R / kSortThreads consecutive digits.  The counts are read from L2
+// (other blocks added them).
+template <uint32_t R>
+TGPU_D void segment_digit_offsets(const SegmentSpec &s, uint32_t *seg_hist, int passes, uint32_t *warp_sums) {
+    constexpr uint32_t kPer = R / kSortThreads;
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    for (int p = 0; p < passes; ++p) {
+        uint32_t *h = seg_hist + (size_t)p * kMaxRadix + threadIdx.x * kPer;
+        uint32_t v[kPer], sum = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) {
+            v[k] = __ldcg(h + k);
+            sum += v[k];
+        }
+        const uint32_t incl = warp_incl_scan(sum);
+        if (lane == 31) warp_sums[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t w = lane < kSortThreads / 32 ? warp_sums[lane] : 0u;
+            const uint32_t wi = warp_incl_scan(w);
+            if (lane < kSortThreads / 32) warp_sums[lane] = wi - w;
+        }
+        __syncthreads();
+        uint32_t run = s.begin + warp_sums[warp] + incl - sum;
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) {
+            h[k] = run;
+            run += v[k];
+        }
+        __syncthreads();
+    }
+}
+
+// One pass over the positions: the cell key of every agent, and per-segment histograms of
+// every D-bit digit of the keys (order-independent, so all passes' digit offsets are known
+// before the first scatter).  The segment's last block to finish (a counter in `done`,
+// zeroed with the histograms) turns its histograms into digit offsets.  hist layout:
 // [segment][pass][kMaxRadix].
 template <int D>
 __global__ void __launch_bounds__(kSortThreads) keys_hist_kernel(const SegmentSpec *__restrict__ specs,
@@ -159,10 +229,12 @@ __global__ void __launch_bounds__(kSortThreads) keys_hist_kernel(const SegmentSp
                                                                  const SegGrid *__restrict__ grids,
                                                                  const float4 *__restrict__ pos,
                                                                  uint32_t *__restrict__ keys,
-                                                                 uint32_t *__restrict__ hist, int passes,
-                                                                 uint32_t key_bits) {
+                                                                 uint32_t *__restrict__ hist, uint32_t *done,
+                                                                 int passes, uint32_t key_bits) {
     constexpr uint32_t R = 1u << D;
     __shared__ uint32_t h[kMaxSortPasses][R];
+    __shared__ uint32_t warp_sums[kSortThreads / 32];
+    __shared__ bool s_last;
     const uint32_t seg = tile_seg[blockIdx.x];
     const SegmentSpec s = specs[seg];
     const Grid g = grids[seg].g;
@@ -194,47 +266,20 @@ __global__ void __launch_bounds__(kSortThreads) keys_hist_kernel(const SegmentSp
         }
     }
     __syncthreads();
+    uint32_t *seg_hist = hist + (size_t)seg * kMaxSortPasses * kMaxRadix;
     for (int p = 0; p < passes; ++p)
         for (uint32_t d = threadIdx.x; d < R; d += kSortThreads) {
             const uint32_t c = h[p][d];
-            if (c) atomicAdd(&hist[((size_t)seg * kMaxSortPasses + p) * kMaxRadix + d], c);
+            if (c) atomicAdd(&seg_hist[(size_t)p * kMaxRadix + d], c);
         }
-}
-
-// Per segment and pass: the histogram becomes each digit's first output slot (the
-// segment's begin plus the exclusive prefix over digits).  One 256-thread block per
-// segment; each thread owns R / 256 consecutive digits.
-template <uint32_t R>
-__global__ void __launch_bounds__(256) digit_offsets_kernel(const SegmentSpec *__restrict__ specs,
-                                                            uint32_t *__restrict__ hist, int passes) {
-    constexpr uint32_t kPer = R / 256u;
-    __shared__ uint32_t warp_sums[8];
-    const SegmentSpec s = specs[blockIdx.x];
-    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
-    for (int p = 0; p < passes; ++p) {
-        uint32_t *h = hist + ((size_t)blockIdx.x * kMaxSortPasses + p) * kMaxRadix + threadIdx.x * kPer;
-        uint32_t v[kPer], sum = 0;
-#pragma unroll
-        for (uint32_t k = 0; k < kPer; ++k) {
-            v[k] = h[k];
-            sum += v[k];
-        }
-        const uint32_t incl = warp_incl_scan(sum);
-        if (lane == 31) warp_sums[warp] = incl;
-        __syncthreads();
-        if (warp == 0) {
-            const uint32_t w = lane < 8 ? warp_sums[lane] : 0u;
-            const uint32_t wi = warp_incl_scan(w);
-            if (lane < 8) warp_sums[lane] = wi - w;
-        }
-        __syncthreads();
-        uint32_t run = s.begin + warp_sums[warp] + incl - sum;
-#pragma unroll
-        for (uint32_t k = 0; k < kPer; ++k) {
-            h[k] = run;
-            run += v[k];
-        }
-        __syncthreads();
+    // every thread's counts ordered before the block counts itself done
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(done + seg, 1u) == s.tile_count - 1u;
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        segment_digit_offsets<R>(s, seg_hist, passes, warp_sums);
     }
 }
 
@@ -455,11 +500,14 @@ constexpr uint32_t kTableBlocks = kSortTile / kSortThreads;
 // agent of each cell writes its index into the start entries of the empty cells before
 // it in its row and its own; the last agent of a row writes the row's end into the
 // entries after its cell; a row's first agent clears the whole row.
+// With perm, the launch also reorders the streams of `set` into cell order (the reorder
+// of the reference's sort, which copies each agent to its slot).
 __global__ void __launch_bounds__(kSortThreads) cell_table_kernel(const SegmentSpec *__restrict__ specs,
                                                                   const uint32_t *__restrict__ tile_seg,
                                                                   const SegGrid *__restrict__ grids,
                                                                   const uint32_t *__restrict__ keys,
-                                                                  uint2 *__restrict__ table, int write_runs) {
+                                                                  uint2 *__restrict__ table, int write_runs,
+                                                                  const uint32_t *__restrict__ perm, GatherSet set) {
     // kTableBlocks blocks per radix tile, one key per thread
     const uint32_t tile = blockIdx.x / kTableBlocks, part = blockIdx.x % kTableBlocks;
     const uint32_t seg = tile_seg[tile];
@@ -469,6 +517,15 @@ __global__ void __launch_bounds__(kSortThreads) cell_table_kernel(const SegmentS
     const uint32_t seg_end = s.begin + s.count;
     const uint32_t end = min(beg + (uint32_t)kSortThreads, seg_end);
     const uint32_t i = beg + threadIdx.x;
+    if (perm && i < end) {
+        const uint32_t src = perm[i];
+#pragma unroll
+        for (int c = 0; c < kMaxF4; ++c)
+            if (c < set.nf4) set.dst_f4[c][i] = __ldg(set.src_f4[c] + src);
+#pragma unroll
+        for (int c = 0; c < kMaxU32; ++c)
+            if (c < set.nu32) set.dst_u32[c][i] = __ldg(set.src_u32[c] + src);
+    }
     if (s.order == kOrderRows) {
         // The first agent of a row writes its header's x_first / first, the last agent
         // x_last / end, and the first agent of every other cell the start entries of the
@@ -538,28 +595,38 @@ __global__ void __launch_bounds__(kSortThreads) cell_table_kernel(const SegmentS
     }
 }
 
-// ------------------------------------------------------------------ reorder
-
-__global__ void __launch_bounds__(256) gather_kernel(uint32_t n, const uint32_t *__restrict__ perm, GatherSet set) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t src = perm[i];
-#pragma unroll
-    for (int c = 0; c < kMaxF4; ++c)
-        if (c < set.nf4) set.dst_f4[c][i] = __ldg(set.src_f4[c] + src);
-#pragma unroll
-    for (int c = 0; c < kMaxU32; ++c)
-        if (c < set.nu32) set.dst_u32[c][i] = __ldg(set.src_u32[c] + src);
-}
-
 // ------------------------------------------------------------------ host-side launchers
 
-void reset_extent(BoxAcc *out, cudaStream_t st) { box_reset_kernel<<<1, 32, 0, st>>>(out, 1); }
+void reset_extent(BoxAcc *out, cudaStream_t st) {
+    box_reset_kernel<<<1, 32, 0, st>>>(out, 1, nullptr, nullptr, nullptr);
+}
+
+namespace {
+
+// The sort scratch (sort_scratch_bytes): digit histograms [segments][kMaxSortPasses]
+// [kMaxRadix], tile counters [kMaxSortPasses], the keys/histogram kernel's block counters
+// [segments], the bbox kernel's block counters [segments], then the look-back words
+// [pass][tile][radix].
+struct Scratch {
+    uint32_t *hist, *tile_ctr, *hist_done, *box_done, *look;
+};
+Scratch scratch_of(const SortLaunch &L) {
+    Scratch c;
+    c.hist = L.sort_scratch;
+    c.tile_ctr = c.hist + (size_t)L.segments * kMaxSortPasses * kMaxRadix;
+    c.hist_done = c.tile_ctr + kMaxSortPasses;
+    c.box_done = c.hist_done + L.segments;
+    c.look = c.box_done + L.segments;
+    return c;
+}
+
+}  // namespace
 
 void launch_box(const SortLaunch &L, cudaStream_t st) {
-    box_reset_kernel<<<(L.segments + 127) / 128, 128, 0, st>>>(L.box, L.segments);
-    bbox_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.pos, L.pos_max, L.box);
-    launch_grids(L, st);
+    const Scratch c = scratch_of(L);
+    box_reset_kernel<<<(L.segments + 127) / 128, 128, 0, st>>>(L.box, L.segments, L.specs, L.grids, c.box_done);
+    bbox_kernel<<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.pos, L.pos_max, L.box, L.grids,
+                                                  c.box_done);
 }
 
 void launch_grids(const SortLaunch &L, cudaStream_t st) {
@@ -574,17 +641,13 @@ void launch_sort_digits(const SortLaunch &L, cudaStream_t st, uint32_t **sorted_
     uint32_t *kin = L.keys[0], *kout = L.keys[1];
     uint32_t *vin = nullptr, *vout = L.vals[1];
     const int passes = sort_passes(L.key_bits);
-    // zero the histograms, the tile counters and the look-back words of the passes used
-    cudaMemsetAsync(L.sort_scratch, 0,
-                    sizeof(uint32_t) * ((size_t)L.segments * kMaxSortPasses * kMaxRadix + kMaxSortPasses +
-                                        (size_t)passes * L.tiles * R),
+    const Scratch c = scratch_of(L);
+    uint32_t *hist = c.hist, *tile_ctr = c.tile_ctr, *look = c.look;
+    // zero the histograms, the counters and the look-back words of the passes used
+    cudaMemsetAsync(L.sort_scratch, 0, sizeof(uint32_t) * ((size_t)(look - L.sort_scratch) + (size_t)passes * L.tiles * R),
                     st);
-    uint32_t *hist = L.sort_scratch;
-    uint32_t *tile_ctr = hist + (size_t)L.segments * kMaxSortPasses * kMaxRadix;
-    uint32_t *look = tile_ctr + kMaxSortPasses;
-    keys_hist_kernel<D><<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.grids, L.pos, kin, hist, passes,
-                                                          L.key_bits);
-    digit_offsets_kernel<R><<<L.segments, 256, 0, st>>>(L.specs, hist, passes);
+    keys_hist_kernel<D><<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.grids, L.pos, kin, hist,
+                                                          c.hist_done, passes, L.key_bits);
     for (int p = 0; p < passes; ++p) {
         const int bits = std::min(D, (int)L.key_bits - D * p);
         onesweep_kernel<D><<<L.tiles, kSortThreads, 0, st>>>(L.specs, L.tile_seg, kin, vin, kout, vout, hist, look,
@@ -665,14 +728,11 @@ cudaError_t selftest_sort_wait(uint32_t *err_host) {
     return e;
 }
 
-void launch_cell_table(const SortLaunch &L, const uint32_t *sorted_keys, int write_runs, cudaStream_t st) {
-    cell_table_kernel<<<L.tiles * kTableBlocks, kSortThreads, 0, st>>>(L.specs, L.tile_seg, L.grids, sorted_keys,
-                                                                     L.table, write_runs);
-}
-
-void launch_gather(uint32_t n, const uint32_t *perm, const GatherSet &set, cudaStream_t st) {
-    if (n == 0) return;
-    gather_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, perm, set);
+void launch_cell_table(const SortLaunch &L, const uint32_t *sorted_keys, int write_runs, cudaStream_t st,
+                       const uint32_t *perm, const GatherSet *set) {
+    const GatherSet none{};
+    cell_table_kernel<<<L.tiles * kTableBlocks, kSortThreads, 0, st>>>(
+        L.specs, L.tile_seg, L.grids, sorted_keys, L.table, write_runs, set ? perm : nullptr, set ? *set : none);
 }
 
 }  // namespace tgpu

@@ -107,7 +107,8 @@ struct ActLaunch {
     PassIO io;
 };
 
-// Bounding boxes of every segment, then their grids (launch_grids).
+// Bounding boxes of every segment and, from them, their grids (the last block of each
+// segment derives its grid).
 void launch_box(const SortLaunch &L, cudaStream_t st);
 // Grids of every segment from the boxes in L.box (after they were set or restored).
 void launch_grids(const SortLaunch &L, cudaStream_t st);
@@ -122,9 +123,10 @@ constexpr int sort_passes(uint32_t key_bits) {
 }
 
 // Bytes of the sort's scratch: per-segment histograms of every digit, one tile counter per
-// pass, and the look-back words of every (pass, tile, digit).
+// pass, two per-segment block counters (keys/histogram and bounding box), and the
+// look-back words of every (pass, tile, digit).
 constexpr size_t sort_scratch_bytes(uint32_t segments, uint32_t tiles) {
-    return sizeof(uint32_t) * ((size_t)segments * kMaxSortPasses * kMaxRadix + kMaxSortPasses +
+    return sizeof(uint32_t) * ((size_t)segments * kMaxSortPasses * kMaxRadix + kMaxSortPasses + 2u * (size_t)segments +
                                (size_t)kMaxSortPasses * tiles * kMaxRadix);
 }
 
@@ -132,9 +134,11 @@ constexpr size_t sort_scratch_bytes(uint32_t segments, uint32_t tiles) {
 // Resets an extent accumulator (the pack kernel reduces the pushed positions into it).
 void reset_extent(BoxAcc *out, cudaStream_t st);
 void launch_sort(const SortLaunch &L, cudaStream_t st, uint32_t **sorted_keys, uint32_t **perm);
-void launch_cell_table(const SortLaunch &L, const uint32_t *sorted_keys, int write_runs, cudaStream_t st);
+// Writes (write_runs = 1) or clears (0) the cell table of the sorted keys.  With `set`, the
+// same launch reorders its streams into cell order: dst[i] = src[perm[i]] for every agent.
+void launch_cell_table(const SortLaunch &L, const uint32_t *sorted_keys, int write_runs, cudaStream_t st,
+                       const uint32_t *perm = nullptr, const GatherSet *set = nullptr);
 // Runs one radix tile whose predecessor never publishes; returns the device error word.
 cudaError_t selftest_sort_wait(uint32_t *err_host);
-void launch_gather(uint32_t n, const uint32_t *perm, const GatherSet &set, cudaStream_t st);
 
 }  // namespace tgpu
