@@ -66,10 +66,11 @@ struct ModelDesc {
 };
 
 // Layout stamp of the model interface: a model compiled against other definitions of the
-// launch descriptors or of ModelDesc carries another value and is refused at registration.
-constexpr unsigned kModelAbi = 0x01000000u ^ ((unsigned)sizeof(SeeLaunch) << 12) ^ ((unsigned)sizeof(ActLaunch) << 4) ^
+// launch descriptors, of the segment spec they point to or of ModelDesc carries another
+// value and is refused at registration.
+constexpr unsigned kModelAbi = 0x01000001u ^ ((unsigned)sizeof(SeeLaunch) << 12) ^ ((unsigned)sizeof(ActLaunch) << 4) ^
                                (unsigned)sizeof(ModelDesc) ^ ((unsigned)sizeof(KernelDesc) << 20) ^
-                               ((unsigned)sizeof(ProgramDesc) << 8);
+                               ((unsigned)sizeof(ProgramDesc) << 8) ^ ((unsigned)sizeof(SegmentSpec) << 24);
 
 // The SPH model's adjoint kernels (used by adjoint.cu).
 struct SphAdjointKernels {

@@ -263,22 +263,24 @@ int tgpu::prepare_specs(TgpuBatch *b) {
             double cells = floor((double)ext / (double)sp.part[a]) + 1.0;
             want[a] = std::min(1024u, next_pow2((uint32_t)std::min(1024.0, std::max(2.0, ceil(cells * 1.1)))));
         }
-        // Morton order: one bound for all axes; row order: x and (y, z) bounded separately
-        const uint32_t ayz = std::max(want[1], want[2]);
-        const uint32_t axis = b->cell_order == kOrderRows ? want[0] : std::max(want[0], ayz);
+        // Morton order: one bound for all axes; row order: each axis its own bound, so
+        // that the key takes the bits the three budgets need and no more
+        const bool rows = b->cell_order == kOrderRows;
+        const uint32_t axis = rows ? want[0] : std::max(want[0], std::max(want[1], want[2]));
         sp.axis_cells_max = axis;
-        sp.axis_cells_yz = b->cell_order == kOrderRows ? ayz : axis;
-        const uint32_t seg_key_bits = log2u(axis) + 2 * log2u(sp.axis_cells_yz);
+        sp.axis_cells_y = rows ? want[1] : axis;
+        sp.axis_cells_z = rows ? want[2] : axis;
+        const uint32_t seg_key_bits = log2u(axis) + log2u(sp.axis_cells_y) + log2u(sp.axis_cells_z);
         uint64_t cap_mem = ((uint64_t)std::max(h.g.shared_megabytes, 1) << 20) / sizeof(uint2);
-        uint64_t cap_axis = (uint64_t)axis * sp.axis_cells_yz * sp.axis_cells_yz;
+        uint64_t cap_axis = (uint64_t)axis * sp.axis_cells_y * sp.axis_cells_z;
         uint64_t cap = std::min(cap_mem, cap_axis);
         cap = std::max<uint64_t>(cap, 8);
         cap = std::min<uint64_t>(cap, 0x7FFFFFFEull);
         cap = (cap + 1) & ~1ull;  // even: every segment's table starts 16-byte aligned (row headers)
-        // row order: headers for up to axis^2 rows, at most a quarter of the table
-        sp.row_cap = b->cell_order == kOrderRows
-                         ? (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)ayz * ayz, cap / 4))
-                         : 0u;
+        // row order: headers for up to y x z bound rows, at most a quarter of the table
+        sp.row_cap = rows ? (uint32_t)std::max<uint64_t>(
+                                1, std::min<uint64_t>((uint64_t)sp.axis_cells_y * sp.axis_cells_z, cap / 4))
+                          : 0u;
         sp.table_base = (uint32_t)table_total;
         sp.table_cap = (uint32_t)cap;
         table_total += cap;

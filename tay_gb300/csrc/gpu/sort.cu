@@ -283,22 +283,73 @@ __global__ void __launch_bounds__(kSortThreads) keys_hist_kernel(const SegmentSp
     }
 }
 
-// Decoupled look-back words: a tile's count for one digit (kLookAgg) or its inclusive
-// prefix (kLookPrefix), with the flag in the top two bits.
+// Decoupled look-back words: a count for one digit (kLookAgg) or an inclusive prefix
+// (kLookPrefix), with the flag in the top two bits.
 constexpr uint32_t kLookAgg = 1u << 30;
 constexpr uint32_t kLookPrefix = 2u << 30;
 constexpr uint32_t kLookValue = (1u << 30) - 1u;
 constexpr uint32_t kLookSpinLimit = 1u << 20;  // polls of one predecessor word before giving up
+// Tiles per look-back group: the last tile of each group of a segment publishes the
+// group's count and then its inclusive prefix in its own slot, so that a later tile adds at
+// most kLookGroup - 1 tile words of its own group and then one word per earlier group.
+constexpr uint32_t kLookGroup = 16;
+
+// Adds to excl[] the look-back words of `count` tiles: from, from - stride, ... (windows of
+// up to 8 loaded together for every digit still open), stopping per digit at the first
+// inclusive prefix (done[]).  A word not yet published is polled, bounded: a wait that
+// runs out reports kErrSortLookback and counts as a prefix.
+template <uint32_t kPer, uint32_t R>
+TGPU_D void look_back(const uint32_t *tile_look, uint32_t from, uint32_t count, uint32_t stride, uint32_t d0,
+                      uint32_t *excl, bool *done, uint32_t *err) {
+    bool open = false;
+#pragma unroll
+    for (uint32_t k = 0; k < kPer; ++k) open = open || !done[k];
+    for (uint32_t i = 0; i < count && open;) {
+        const uint32_t n = min(8u, count - i);
+        uint32_t v[kPer][8];
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k)
+#pragma unroll
+            for (uint32_t q = 0; q < 8; ++q)
+                v[k][q] = (!done[k] && q < n)
+                              ? *(const volatile uint32_t *)(tile_look + (size_t)(from - (i + q) * stride) * R + d0 + k)
+                              : 0u;
+        open = false;
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) {
+            for (uint32_t q = 0; q < n && !done[k]; ++q) {
+                const volatile uint32_t *w = tile_look + (size_t)(from - (i + q) * stride) * R + d0 + k;
+                uint32_t x = v[k][q];
+                for (uint32_t spin = 0; (x >> 30) == 0u; ++spin) {
+                    if (spin == kLookSpinLimit) {
+                        atomicOr(err, kErrSortLookback);
+                        break;
+                    }
+                    __nanosleep(32);
+                    x = *w;
+                }
+                excl[k] += x & kLookValue;
+                if ((x >> 30) != 1u) done[k] = true;  // an inclusive prefix (or a wait that ran out)
+            }
+            open = open || !done[k];
+        }
+        i += n;
+    }
+}
 
 // One radix pass as a single kernel (the "onesweep" scheme): a block takes the next tile in
-// input order from an atomic counter, ranks its 2048 keys stably (8 warps, each owning 256
-// consecutive items in 8 rounds of 32: __match_any_sync ranks and per-warp running digit
-// counts), publishes its per-digit counts, and finds its per-digit output offsets by looking
-// back over the earlier tiles of its segment (a tile's first tile starts from the segment's
-// digit offsets).  Tiles take ids in order, so every tile a block waits for is already
-// running; each wait is bounded and reports kErrSortLookback through *err when it runs out.
-// D-bit digits (R = 2^D bins); each thread owns R / 256 consecutive digits for the per-digit
-// work, and looks back for all of them together.
+// input order from an atomic counter, counts its 2048 keys per digit, publishes the counts,
+// ranks its keys stably (8 warps, each owning 256 consecutive items in 8 rounds of 32:
+// __match_any_sync ranks and per-warp running digit counts), and finds its per-digit output
+// offsets by looking back over the earlier tiles of its segment (the segment's first tile
+// starts from the segment's digit offsets).  The look-back is two-level: a tile adds the
+// words of the earlier tiles of its group of kLookGroup, then one word per earlier group
+// (its last tile's slot: the group's count, then its inclusive prefix), so the chain a tile
+// may wait along grows with the number of groups, not of tiles.  Tiles take ids in order
+// and wait only on lower ids, so every tile a block waits for is already running; each wait
+// is bounded and reports kErrSortLookback through *err when it runs out.  D-bit digits
+// (R = 2^D bins); each thread owns R / 256 consecutive digits for the per-digit work, and
+// looks back for all of them together.
 template <int D>
 __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(const SegmentSpec *__restrict__ specs,
                                                                 const uint32_t *__restrict__ tile_seg,
@@ -335,6 +386,8 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(const Segment
     const uint32_t *seg_hist = hist + ((size_t)seg * kMaxSortPasses + pass) * kMaxRadix;
     uint32_t *tile_look = look + ((size_t)pass * gridDim.x) * R;  // [tile][R] of this pass
     const uint32_t d0 = threadIdx.x * kPer;                         // this thread's first digit
+    const uint32_t g0 = tile - t % kLookGroup;                      // first tile of this tile's group
+    const bool group_last = t % kLookGroup == kLookGroup - 1u || t + 1u == s.tile_count;
 
     uint32_t key[kRounds], val[kRounds], rank[kRounds], dig[kRounds];
     // the tile's digit counts first, published before the ranking so that later tiles
@@ -353,13 +406,16 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(const Segment
         if (dig[r] < R && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&tile_hist[dig[r]], (uint32_t)__popc(peers));
     }
     __syncthreads();
+    uint32_t cnt[kPer], excl[kPer];
 #pragma unroll
     for (uint32_t k = 0; k < kPer; ++k) {
+        cnt[k] = tile_hist[d0 + k];
+        excl[k] = t == 0 ? seg_hist[d0 + k] : 0u;
         volatile uint32_t *mine = tile_look + (size_t)tile * R + d0 + k;
         if (t == 0)
-            *mine = kLookPrefix | ((seg_hist[d0 + k] + tile_hist[d0 + k]) & kLookValue);
-        else
-            *mine = kLookAgg | tile_hist[d0 + k];
+            *mine = kLookPrefix | ((excl[k] + cnt[k]) & kLookValue);
+        else if (!group_last)
+            *mine = kLookAgg | cnt[k];  // (a group's last tile publishes the group's count below)
     }
 #pragma unroll
     for (int r = 0; r < kRounds; ++r) {
@@ -379,10 +435,32 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(const Segment
         dig[r] = d;
     }
     __syncthreads();
+    // the look-back, after the ranking: by then the earlier tiles have published their
+    // counts, and most their prefixes
+    if (t != 0) {
+        bool done[kPer];
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) done[k] = false;
+        // the earlier tiles of this group (tile words)
+        look_back<kPer, R>(tile_look, tile - 1u, tile - g0, 1u, d0, excl, done, err);
+        if (group_last) {
+#pragma unroll
+            for (uint32_t k = 0; k < kPer; ++k)
+                if (!done[k]) *(volatile uint32_t *)(tile_look + (size_t)tile * R + d0 + k) = kLookAgg | (excl[k] + cnt[k]);
+        }
+        // the earlier groups (their last tiles' slots)
+        look_back<kPer, R>(tile_look, g0 - 1u, (g0 - s.tile_begin) / kLookGroup, kLookGroup, d0, excl, done, err);
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) {
+            // counts only, down to the segment's first tile: start from its digit offsets
+            if (!done[k]) excl[k] += seg_hist[d0 + k];
+            *(volatile uint32_t *)(tile_look + (size_t)tile * R + d0 + k) = kLookPrefix | ((excl[k] + cnt[k]) & kLookValue);
+        }
+    }
     {
-        // per digit (kPer consecutive ones per thread): prefix over warps, the tile's count,
-        // the look-back
-        uint32_t run[kPer], excl[kPer];
+        // per digit (kPer consecutive ones per thread): prefix over warps, then the tile's
+        // own digit-sorted layout (exclusive scan of its digit counts)
+        uint32_t sum = 0;
 #pragma unroll
         for (uint32_t k = 0; k < kPer; ++k) {
             uint32_t acc = 0;
@@ -391,67 +469,8 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(const Segment
                 warp_hist[w][d0 + k] = acc;
                 acc += c;
             }
-            run[k] = acc;
-            excl[k] = t == 0 ? seg_hist[d0 + k] : 0u;
-        }
-        if (t != 0) {
-            // windows of up to 8 predecessors, loaded together for every digit still open:
-            // add counts back to the nearest inclusive prefix; spin (bounded) only on a
-            // word not yet published
-            bool done[kPer];
-#pragma unroll
-            for (uint32_t k = 0; k < kPer; ++k) done[k] = false;
-            uint32_t next = tile;  // predecessors still to add: [tile_begin, next)
-            bool open = true;
-            while (open) {
-                const uint32_t n = min(8u, next - s.tile_begin);
-                uint32_t v[kPer][8];
-#pragma unroll
-                for (uint32_t k = 0; k < kPer; ++k)
-#pragma unroll
-                    for (int q = 0; q < 8; ++q)
-                        v[k][q] = (!done[k] && (uint32_t)q < n)
-                                      ? *(const volatile uint32_t *)(tile_look + (size_t)(next - 1 - q) * R + d0 + k)
-                                      : 0u;
-#pragma unroll
-                for (uint32_t k = 0; k < kPer; ++k) {
-                    for (uint32_t q = 0; q < n && !done[k]; ++q) {
-                        const volatile uint32_t *w = tile_look + (size_t)(next - 1 - q) * R + d0 + k;
-                        uint32_t x = v[k][q];
-                        for (uint32_t spin = 0; (x >> 30) == 0u; ++spin) {
-                            if (spin == kLookSpinLimit) {
-                                atomicOr(err, kErrSortLookback);
-                                break;
-                            }
-                            __nanosleep(32);
-                            x = *w;
-                        }
-                        excl[k] += x & kLookValue;
-                        if ((x >> 30) != 1u) done[k] = true;  // an inclusive prefix (or a wait that ran out)
-                    }
-                }
-                next -= n;
-                open = false;
-#pragma unroll
-                for (uint32_t k = 0; k < kPer; ++k) {
-                    if (!done[k] && next == s.tile_begin) {
-                        // only counts down to the segment's first tile: start from its digit offsets
-                        excl[k] += seg_hist[d0 + k];
-                        done[k] = true;
-                    }
-                    open = open || !done[k];
-                }
-            }
-#pragma unroll
-            for (uint32_t k = 0; k < kPer; ++k)
-                *(volatile uint32_t *)(tile_look + (size_t)tile * R + d0 + k) = kLookPrefix | ((excl[k] + run[k]) & kLookValue);
-        }
-        // the tile's own digit-sorted layout: exclusive scan of its digit counts
-        uint32_t sum = 0;
-#pragma unroll
-        for (uint32_t k = 0; k < kPer; ++k) {
             digit_base[d0 + k] = excl[k];
-            sum += run[k];
+            sum += cnt[k];
         }
         const uint32_t incl = warp_incl_scan(sum);
         if (lane == 31) warp_sums[warp] = incl;
@@ -462,7 +481,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(const Segment
 #pragma unroll
         for (uint32_t k = 0; k < kPer; ++k) {
             local_start[d0 + k] = start;
-            start += run[k];
+            start += cnt[k];
         }
     }
     __syncthreads();
@@ -546,7 +565,9 @@ __global__ void __launch_bounds__(kSortThreads) cell_table_kernel(const SegmentS
             const uint32_t kp = i == s.begin ? ~k : keys[i - 1];
             const bool row_first = (kp >> b) != row;
             const bool row_last = (i + 1 == seg_end) || (keys[i + 1] >> b) != row;
-            const uint32_t r = compact2_10(row >> 1) * dy + compact2_10(row);
+            uint32_t ry, rz;
+            row_of_code(s, row, ry, rz);
+            const uint32_t r = rz * dy + ry;
             if (!write_runs) {
                 if (row_first) hdr[r] = make_uint4(0u, 0u, 0u, 0u);
             } else {

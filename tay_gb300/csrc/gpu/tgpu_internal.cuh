@@ -45,7 +45,8 @@ struct SegmentSpec {
     uint32_t order;          // cell order of the keys and table layout: kOrderMorton / kOrderRows
     uint32_t dims;           // tay_configure_space dims (1..3; 0 means 3): axes >= dims get one cell
     uint32_t row_cap;        // row order: (y, z) rows the table's header region holds
-    uint32_t axis_cells_yz;  // row order: power-of-two bound of the y and z axes (x: axis_cells_max)
+    uint32_t axis_cells_y;   // row order: power-of-two bounds of the y and z axes (x: axis_cells_max)
+    uint32_t axis_cells_z;
     float part[3];           // minimum cell edge per axis
     float reach[3];          // largest see radius per axis over the segment's see passes
     float box_min[3];        // fixed space box (tay_fix_space_box)
@@ -107,7 +108,7 @@ TGPU_HD int seg_dims(const SegmentSpec &s) { return (s.dims >= 1u && s.dims <= 3
 
 // Two cell orders.  kOrderMorton: the 3-D Morton key, a table entry {first, end} per
 // cell.  kOrderRows: x fastest inside rows of constant (y, z), the rows in 2-D Morton
-// order of (y, z): key = (morton2(y, z) << b) | x with b = log2(axis_cells_max), so the
+// order of (y, z): key = (row_code(y, z) << b) | x with b = log2(axis_cells_max), so the
 // agents of x-adjacent cells are contiguous and a seer's box is one candidate range per
 // row.  Its table holds, per row, a 16-byte header {x_first, x_last, first, end} (the
 // occupied cells and the row's agent range; zero for an empty row) and, per cell x in
@@ -134,7 +135,11 @@ TGPU_HD bool table_fits(const SegmentSpec &s, const int *d) {
 // Cell budget of axis i: in row order the x axis (whose cells only tighten each row's
 // candidate range) and the y / z axes (whose cells make the rows) have their own bounds.
 TGPU_HD uint32_t axis_max(const SegmentSpec &s, int i) {
-    return (i > 0 && s.order == kOrderRows && s.axis_cells_yz) ? s.axis_cells_yz : s.axis_cells_max;
+    if (i > 0 && s.order == kOrderRows) {
+        const uint32_t a = i == 1 ? s.axis_cells_y : s.axis_cells_z;
+        if (a) return a;
+    }
+    return s.axis_cells_max;
 }
 
 TGPU_HD Grid derive_grid(const SegmentSpec &s, const float *mn, const float *mx) {
@@ -225,18 +230,46 @@ TGPU_HD uint32_t compact2_10(uint32_t v) {
 }
 
 
-TGPU_HD uint32_t axis_bits(const SegmentSpec &s) {
+// log2 of a power-of-two bound of at most 1024 cells (0 for 0 or 1).
+TGPU_HD uint32_t bound_bits(uint32_t v) {
 #ifdef __CUDA_ARCH__
-    return 31u - (uint32_t)__clz(s.axis_cells_max | 1u);
+    return 31u - (uint32_t)__clz(v | 1u);
 #else
     uint32_t b = 0;
-    while ((2u << b) <= s.axis_cells_max && b < 10) ++b;
+    while ((2u << b) <= v && b < 10) ++b;
     return b;
 #endif
 }
 
+TGPU_HD uint32_t axis_bits(const SegmentSpec &s) { return bound_bits(s.axis_cells_max); }
+
+// Row order's code of row (y, z): a 2-D Morton code of the low min(by, bz) bits of both
+// (by, bz: the bits of the y and z bounds), with the remaining high bits of the longer
+// axis above it, so that the code takes by + bz bits and rows close in (y, z) are close
+// in the order.
+TGPU_HD uint32_t row_code(const SegmentSpec &s, uint32_t y, uint32_t z) {
+    const uint32_t by = bound_bits(s.axis_cells_y), bz = bound_bits(s.axis_cells_z);
+    const uint32_t m = by < bz ? by : bz;
+    const uint32_t low = (1u << m) - 1u;
+    const uint32_t code = spread2_10(y & low) | (spread2_10(z & low) << 1);
+    return code | ((by > bz ? (y >> m) : (z >> m)) << (2u * m));
+}
+
+// The (y, z) of a row code.
+TGPU_HD void row_of_code(const SegmentSpec &s, uint32_t code, uint32_t &y, uint32_t &z) {
+    const uint32_t by = bound_bits(s.axis_cells_y), bz = bound_bits(s.axis_cells_z);
+    const uint32_t m = by < bz ? by : bz;
+    const uint32_t lo = code & ((1u << (2u * m)) - 1u), hi = code >> (2u * m);
+    y = compact2_10(lo);
+    z = compact2_10(lo >> 1);
+    if (by > bz)
+        y |= hi << m;
+    else
+        z |= hi << m;
+}
+
 TGPU_HD uint32_t cell_key(const SegmentSpec &s, uint32_t x, uint32_t y, uint32_t z) {
-    if (s.order == kOrderRows) return ((spread2_10(y) | (spread2_10(z) << 1)) << axis_bits(s)) | x;
+    if (s.order == kOrderRows) return (row_code(s, y, z) << axis_bits(s)) | x;
     return morton3(x, y, z);
 }
 
