@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(const Segment
     const uint32_t g0 = tile - t % kLookGroup;                      // first tile of this tile's group
     const bool group_last = t % kLookGroup == kLookGroup - 1u || t + 1u == s.tile_count;
 
-    uint32_t key[kRounds], val[kRounds], rank[kRounds], dig[kRounds];
+    uint32_t key[kRounds], val[kRounds], rank[kRounds], dig[kRounds], peer[kRounds];
     // the tile's digit counts first, published before the ranking so that later tiles
     // find them when they look back
 #pragma unroll
@@ -401,9 +401,10 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(const Segment
 #pragma unroll
     for (int r = 0; r < kRounds; ++r) {
         // one shared atomic per distinct digit of the warp (a tile's keys share their upper
-        // digits, which per-key atomics would serialize on one address)
-        const uint32_t peers = __match_any_sync(0xffffffffu, dig[r]);
-        if (dig[r] < R && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&tile_hist[dig[r]], (uint32_t)__popc(peers));
+        // digits, which per-key atomics would serialize on one address); the lanes with
+        // the same digit are kept for the ranking
+        peer[r] = __match_any_sync(0xffffffffu, dig[r]);
+        if (dig[r] < R && lane == (uint32_t)(__ffs(peer[r]) - 1)) atomicAdd(&tile_hist[dig[r]], (uint32_t)__popc(peer[r]));
     }
     __syncthreads();
     uint32_t cnt[kPer], excl[kPer];
@@ -423,7 +424,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(const Segment
         const bool valid = i < end;
         const uint32_t k = key[r];
         const uint32_t d = dig[r];
-        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t peers = peer[r];
         const uint32_t below = __popc(peers & ((1u << lane) - 1u));
         const uint32_t before = valid ? warp_hist[warp][d] : 0u;
         __syncwarp();
