@@ -137,6 +137,7 @@ void free_batch(TgpuBatch *b) {
     cudaFree(b->sort_scratch);
     cudaFree(b->d_status);  // also the error word, the pair counter and the telemetry
     cudaFreeHost(b->h_status);
+    cudaFreeHost(b->h_extent);
     cudaFree(b->table);
     cudaFree(b->d_aos);
     cudaFree(b->plist_idx);
@@ -876,6 +877,7 @@ int alloc_batch(TgpuBatch *b) {
     CKR(cudaMalloc(&b->d_status, sizeof(unsigned long long) * kStatusWords));
     CKR(cudaMemset(b->d_status, 0, sizeof(unsigned long long) * kStatusWords));
     CKR(cudaMallocHost(&b->h_status, sizeof(unsigned long long) * kStatusWords));
+    CKR(cudaMallocHost(&b->h_extent, sizeof(BoxAcc) * (size_t)std::max(b->nseg, 1)));
     b->d_pairs = b->d_status;
     b->d_telemetry = b->d_status + 1;
     b->d_err = reinterpret_cast<uint32_t *>(b->d_status + 9);
@@ -976,6 +978,28 @@ int upload_state_contexts(TgpuBatch *b) {
     }
     CK(cudaStreamSynchronize(b->st));
     return TGPU_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// The extents of the pushes that completed (the stream was synchronized since): each
+// pending one becomes its group's host extent, and a changed extent re-sizes the grid
+// budgets at the next run.
+void apply_extents(TgpuBatch *b) {
+    for (int s = 0; s < b->nseg; ++s) {
+        HostSeg &h = b->hs[s];
+        if (!h.extent_pending) continue;
+        h.extent_pending = false;
+        const BoxAcc &ext = b->h_extent[s];
+        for (int a = 0; a < 3; ++a) {
+            const float lo = ordered_to_float(ext.lo[a]), hi = ordered_to_float(ext.hi[a]);
+            if (lo != h.host_min[a] || hi != h.host_max[a]) b->specs_dirty = true;
+            h.host_min[a] = lo;
+            h.host_max[a] = hi;
+        }
+    }
 }
 
 }  // namespace
@@ -1135,11 +1159,17 @@ int tgpu_batch_push(TgpuBatch *b, int group, const void *host) {
     HostSeg &h = b->hs[group];
     const SegmentSpec &sp = b->specs[group];
     const uint32_t n = sp.count;
+    // A group whose grid budget was already sized by a push gets this push's extent at the
+    // next sync, without waiting here: every step derives its grid from the device's box,
+    // so a budget one run behind only bounds the cells differently (the pairs are the
+    // same), and the host does not stall between the push and the run.
+    const bool sized = h.pushed && b->table != nullptr;
     h.pushed = true;
     b->wt_done[group] = 0;
-    b->specs_dirty = true;
     if (!n) {
         for (int a = 0; a < 3; ++a) h.host_min[a] = h.host_max[a] = 0.0f;
+        h.extent_pending = false;
+        b->specs_dirty = true;
         return TGPU_OK;
     }
     uint32_t *aos = static_cast<uint32_t *>(pinned_device_ptr(host));
@@ -1162,14 +1192,15 @@ int tgpu_batch_push(TgpuBatch *b, int group, const void *host) {
     // grid budget) on the device
     reset_extent(b->d_extent, b->st);
     b->m->pack(aos, n, io, b->d_extent, b->st);
-    BoxAcc ext;
-    CK(cudaMemcpyAsync(&ext, b->d_extent, sizeof(BoxAcc), cudaMemcpyDeviceToHost, b->st));
+    CK(cudaMemcpyAsync(b->h_extent + group, b->d_extent, sizeof(BoxAcc), cudaMemcpyDeviceToHost, b->st));
     CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(b->st));
-    for (int a = 0; a < 3; ++a) {
-        h.host_min[a] = ordered_to_float(ext.lo[a]);
-        h.host_max[a] = ordered_to_float(ext.hi[a]);
+    if (sized) {
+        h.extent_pending = true;
+        return TGPU_OK;
     }
+    CK(cudaStreamSynchronize(b->st));
+    h.extent_pending = true;
+    apply_extents(b);
     return TGPU_OK;
 }
 
@@ -1240,6 +1271,7 @@ int tgpu_batch_write_through(TgpuBatch *b, int group, void *host) {
 int tgpu_batch_sync(TgpuBatch *b) {
     if (!b) return fail(TGPU_ERR_ARG, "null batch");
     CK(cudaStreamSynchronize(b->st));
+    apply_extents(b);
     float ms = 0.0f;
     CK(cudaEventElapsedTime(&ms, b->e0, b->e1));
     b->last_ms = ms;

@@ -38,6 +38,7 @@ struct HostSeg {
     std::vector<TgpuPass> passes;
     float host_min[3], host_max[3];
     bool pushed = false;
+    bool extent_pending = false;  // a push's extent is on its way to h_extent (read at the next sync)
 };
 
 // Optional per-class timing of one enqueued step: an event is recorded before and after
@@ -107,6 +108,7 @@ struct TgpuBatch {
     bool use_graphs = true;
     uint32_t cell_order = kOrderMorton;  // key order and table layout of every segment
     BoxAcc *d_extent = nullptr;          // pushed extent of one group
+    BoxAcc *h_extent = nullptr;          // page-locked, per segment: the extent of its last push
     uint32_t hit_masks = 0;              // see walk: hit masks (row order)
     std::map<uint64_t, cudaGraphExec_t> graphs;
 
