@@ -165,15 +165,6 @@ __global__ void box_reset_kernel(BoxAcc *box, uint32_t segments, const SegmentSp
     }
 }
 
-// ------------------------------------------------------------------ keys + first histogram
-
-// counts layout: segment-major, then digit, then tile within the segment, so that one
-// exclusive scan over the whole array yields absolute output positions
-// (segments are packed: begin(s) = sum of the counts before s).
-TGPU_D uint32_t count_index(const SegmentSpec &s, uint32_t digit, uint32_t local_tile) {
-    return 256u * s.tile_begin + digit * s.tile_count + local_tile;
-}
-
 // Each segment's grid from its box as it stands (restored boxes of recorded steps): one
 // thread per segment.
 __global__ void grid_kernel(const SegmentSpec *__restrict__ specs, const BoxAcc *__restrict__ box,
@@ -182,6 +173,8 @@ __global__ void grid_kernel(const SegmentSpec *__restrict__ specs, const BoxAcc 
     if (s >= segments) return;
     write_grid(specs[s], box[s], grids, s);
 }
+
+// ------------------------------------------------------------------ keys + histograms
 
 // One segment's histograms become each digit's first output slot (the segment's begin
 // plus the exclusive prefix over digits), pass by pass; run by one block of kSortThreads
