@@ -1,8 +1,9 @@
 """Edge cases and full sizes on the GPU, against the oracle: a single agent, coincident
 agents, neighbours exactly at the radius (the reference's test is inclusive,
 tay/space.c:62-68), a flat axis (zero extent), coordinates far from the origin, tiny and
-large states in one batch, the benchmark workloads at full size (1,048,576 boids and
-524,288 SPH particles, one step), and an 8M-agent state (the largest indices of one segment)."""
+large states in one batch, a push that spreads the agents (the grid budget follows one
+run later), the benchmark workloads at full size (1,048,576 boids and 524,288 SPH
+particles, one step), and an 8M-agent state (the largest indices of one segment)."""
 import numpy as np
 import pytest
 
@@ -90,6 +91,35 @@ def test_far_from_origin(gpu, port, tuning):
     o = oracle_run(port, O.MODEL_TEST, setup, recs, 1, space="simple")
     assert g["b_buffer_count"].sum() > 0
     assert np.array_equal(g["b_buffer_count"], o["b_buffer_count"])
+
+
+def test_push_that_spreads_the_agents(gpu, port):
+    """A push after a group's first does not wait for its extent: the grid budget it sizes
+    (cells per axis, hence key width and radix passes) follows one run later.  The agents
+    spread to 8 times their extent between runs; the run right after the push (old budget,
+    cells enlarged to cover the new box) and the next one (new budget: wider keys, one radix
+    pass more) both give the oracle's neighbour counts."""
+    ps = W.basic_points(20000, seed=73, side=300.0)
+    recs = _test_records(ps.p[:, :3])
+    setup = M.test_setup(radius=20.0, part=20.0, passes=("agent_see",))
+    b = api.Batch([(setup, recs)])
+    try:
+        b.push()
+        b.run(1)
+        before = b.launches_per_step()
+        recs["p"][:, :3] *= np.float32(8.0)
+        b.push()
+        launches = []
+        for k in (1, 2):
+            b.run(1)
+            launches.append(b.launches_per_step())
+            g = M.by_id(b.fetch(0))
+            # the see pass adds to the counters: after k runs, k oracle steps
+            o = oracle_run(port, O.MODEL_TEST, setup, recs, k, space="simple")
+            assert np.array_equal(g["b_buffer_count"], o["b_buffer_count"]), k
+        assert launches[0] == before and launches[1] == before + 1, (before, launches)
+    finally:
+        b.close()
 
 
 def test_tiny_and_large_states_in_one_batch(gpu):
