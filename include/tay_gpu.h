@@ -174,7 +174,9 @@ int tgpu_batch_program(const TgpuBatch *batch);
  *   cell_multiple  grid cell edge = cell_multiple x min_part_sizes (0 = 1)
  *   union_factor   a warp walks the union of its seers' cell boxes (one read serves all
  *                  32 lanes) when that union is at most union_factor times the largest
- *                  single box; otherwise each lane walks its own box (0 = default)
+ *                  single box; otherwise each lane walks its own box.  1 (the default; 0
+ *                  means 1): each lane always walks its own box (cell order 1 then runs a
+ *                  kernel without the warp walks, which holds fewer registers)
  *   use_graphs     capture each step in a CUDA graph and replay it
  *   cell_order     0: cells in 3-D Morton order, a {first, end} table entry per cell;
  *                  1: x-rows (x fastest inside (y, z) rows, rows in 2-D Morton order),

@@ -97,11 +97,15 @@ const ModelDesc *model_box();
 template <class P>
 bool launch_see_t(const SeeLaunch &L, size_t smem, cudaStream_t st) {
     if (!L.ctas) return L.wt != nullptr;  // nothing to write
+    // the row kernel with the warp-union and hit-mask walks only when a tuning asks for them
+    const bool warp_walks = L.hit_masks || L.union_factor > 1;
     if constexpr (!std::is_void_v<typename see_detail::CodecOf<P>::type>) {
         // write-through launch (the last pass of a run): the walk without row staging
         if (L.wt) {
-            if (L.rows)
-                see_rows_kernel<P, false, true><<<L.ctas, kSeeThreads, 0, st>>>(L);
+            if (L.rows && warp_walks)
+                see_rows_kernel<P, false, true, true><<<L.ctas, kSeeThreads, 0, st>>>(L);
+            else if (L.rows)
+                see_rows_kernel<P, false, true, false><<<L.ctas, kSeeThreads, 0, st>>>(L);
             else
                 see_kernel<P, true><<<L.ctas, kSeeThreads, smem, st>>>(L);
             return true;
@@ -109,8 +113,10 @@ bool launch_see_t(const SeeLaunch &L, size_t smem, cudaStream_t st) {
     }
     if (L.rows && L.stage_cap)
         see_rows_kernel<P, true><<<L.ctas, kSeeThreads, smem, st>>>(L);
-    else if (L.rows)
+    else if (L.rows && warp_walks)
         see_rows_kernel<P><<<L.ctas, kSeeThreads, 0, st>>>(L);
+    else if (L.rows)
+        see_rows_kernel<P, false, false, false><<<L.ctas, kSeeThreads, 0, st>>>(L);
     else
         see_kernel<P><<<L.ctas, kSeeThreads, smem, st>>>(L);
     return false;

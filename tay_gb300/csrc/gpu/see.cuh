@@ -690,7 +690,12 @@ __global__ void __launch_bounds__(kSeeThreads) see_kernel(SeeLaunch L) {
 // ranges with the two-phase batches instead.
 // At most 64 registers (8 CTAs of 128 threads per SM) except for the staged walk: a few
 // spills cost less than the occupancy step above 64 (measured on the boids and SPH passes).
-template <class P, bool kStage = false, bool kWrite = false>
+// kWarpWalks: the instance also holds the warp-union and hit-mask walks (tunings union_factor
+// > 1 or hit_masks).  Without them (the default tunings) lanes always walk their own boxes,
+// which gives the same bits, and the kernel holds no spills at 64 registers: measured with
+// them compiled in, their register needs spilled into the lane walk (SPH step 1.509 ->
+// 1.458 ms and the 1M-boid see pass 395.7 -> 391.3 us without).
+template <class P, bool kStage = false, bool kWrite = false, bool kWarpWalks = true>
 __global__ void __launch_bounds__(kSeeThreads, kStage ? 1 : 8) see_rows_kernel(SeeLaunch L) {
     using namespace see_detail;
     const uint2 cta = L.cta_table[L.cta_offset + blockIdx.x];
@@ -876,8 +881,8 @@ __global__ void __launch_bounds__(kSeeThreads, kStage ? 1 : 8) see_rows_kernel(S
     if (!staged && !replayed && wl0 <= wh0) {
         const int lane_vol = active ? (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) * (hi[0] - lo[0] + 1) : 0;
         const long long union_vol = (long long)(wh0 - wl0 + 1) * (wh1 - wl1 + 1) * (wh2 - wl2 + 1);
-        const bool union_mode =
-            !kBox && !recording && union_vol <= (long long)L.union_factor * warp_max_i(lane_vol);
+        const bool union_mode = kWarpWalks && !kBox && !recording &&
+                                union_vol <= (long long)L.union_factor * warp_max_i(lane_vol);
         if (L.telemetry && lane == 0) atomicAdd(L.telemetry + (union_mode ? 3 : 4), 1ull);
         bool walked = false;
         if constexpr (kList == 1 && !kBox) {
@@ -912,7 +917,7 @@ __global__ void __launch_bounds__(kSeeThreads, kStage ? 1 : 8) see_rows_kernel(S
                     const uint2 jr = row_range(words, hdr, (uint32_t)z * dy0 + (uint32_t)y, dx0, wl0, wh0);
                     union_batches<P>(s, sp, r4, active, jr.x, jr.y, self, pos, acc, sctx, pairs, tested);
                 }
-        } else if (!kBox && L.hit_masks) {
+        } else if (kWarpWalks && !kBox && L.hit_masks) {
             // rows of the warp's union box (a warp-uniform loop), each lane's own x range
             for (int z = wl2; z <= wh2; ++z)
                 for (int y = wl1; y <= wh1; ++y) {
