@@ -873,16 +873,31 @@ __global__ void __launch_bounds__(kSeeThreads, kStage ? 1 : 8) see_rows_kernel(S
     }
     if (L.telemetry && threadIdx.x == 0) atomicAdd(L.telemetry + (staged ? 1 : 2), 1ull);
 
-    const int wl0 = warp_min_i(lo[0]), wl1 = warp_min_i(lo[1]), wl2 = warp_min_i(lo[2]);
-    const int wh0 = warp_max_i(hi[0]), wh1 = warp_max_i(hi[1]), wh2 = warp_max_i(hi[2]);
+    // the warp's union box (only the warp walks use it; without them a vote says whether any
+    // lane has cells)
+    int wl0 = 0, wl1 = 0, wl2 = 0, wh0 = -1, wh1 = -1, wh2 = -1;
+    bool warp_cells;
+    if constexpr (kWarpWalks) {
+        wl0 = warp_min_i(lo[0]);
+        wl1 = warp_min_i(lo[1]);
+        wl2 = warp_min_i(lo[2]);
+        wh0 = warp_max_i(hi[0]);
+        wh1 = warp_max_i(hi[1]);
+        wh2 = warp_max_i(hi[2]);
+        warp_cells = wl0 <= wh0;
+    } else {
+        warp_cells = __any_sync(0xffffffffu, lo[0] <= hi[0]);
+    }
     // a recording pass (launch-uniform) takes the per-lane walk, which records (every walk
     // visits a lane's hits in the same order; recording along the union walk measured slower)
     const bool recording = kList == 1 && !kBox && L.plist.mode == 1u;
-    if (!staged && !replayed && wl0 <= wh0) {
-        const int lane_vol = active ? (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) * (hi[0] - lo[0] + 1) : 0;
-        const long long union_vol = (long long)(wh0 - wl0 + 1) * (wh1 - wl1 + 1) * (wh2 - wl2 + 1);
-        const bool union_mode = kWarpWalks && !kBox && !recording &&
-                                union_vol <= (long long)L.union_factor * warp_max_i(lane_vol);
+    if (!staged && !replayed && warp_cells) {
+        bool union_mode = false;
+        if constexpr (kWarpWalks) {
+            const int lane_vol = active ? (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) * (hi[0] - lo[0] + 1) : 0;
+            const long long union_vol = (long long)(wh0 - wl0 + 1) * (wh1 - wl1 + 1) * (wh2 - wl2 + 1);
+            union_mode = !kBox && !recording && union_vol <= (long long)L.union_factor * warp_max_i(lane_vol);
+        }
         if (L.telemetry && lane == 0) atomicAdd(L.telemetry + (union_mode ? 3 : 4), 1ull);
         bool walked = false;
         if constexpr (kList == 1 && !kBox) {
